@@ -1,0 +1,214 @@
+/*
+ * mdsm_gb300.h -- C ABI of the GB300 implementation of MDSM's incoherent dedispersion search
+ * path.  Plain pointers and sizes only; every entry point returns an mdsm_status (0 = OK) and
+ * mdsm_last_error() describes the last failure on the calling thread.
+ *
+ * Buffers:
+ *   *_device entry points take device pointers (caller-owned) and a cudaStream_t as void*.
+ *   *_host   entry points take host pointers (caller-owned; pinned buffers copy fastest) and do
+ *            the host<->device copies inside the call, on library-owned device buffers.
+ *   Filterbank input is channel-major: channel c's samples start at element c*stride, the
+ *   layout of the reference's input buffer (src/mdsm/dedispersion_thread.cu:284-298).
+ *   Dedispersed output is DM-major [ndms][nsamp] (src/mdsm/dedispersion_kernel.cu:46,75).
+ *
+ * Thread safety: different plans may be used from different threads concurrently; one plan is
+ * used by one thread at a time.  The compatibility functions at the end keep the reference's
+ * single global instance (src/mdsm/dedispersion_manager.cpp:14-34).
+ */
+#ifndef MDSM_GB300_H_
+#define MDSM_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include "survey.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    MDSM_OK = 0,
+    MDSM_EINVAL = 1,   /* bad argument or configuration                                  */
+    MDSM_ENOMEM = 2,   /* host or device allocation failed                               */
+    MDSM_ECUDA = 3,    /* a CUDA call failed                                             */
+    MDSM_ETIMEOUT = 4, /* a bounded device-side wait ran out; the kernel returned early  */
+    MDSM_ESTATE = 5,   /* call out of protocol order                                     */
+    MDSM_ERANGE = 6,   /* a buffer is smaller than the plan needs                        */
+    MDSM_EBUDGET = 7,  /* HBM budget refused an admission                                */
+    MDSM_EPARSE = 8,   /* observation file could not be parsed                           */
+    MDSM_EIO = 9,      /* file could not be opened                                       */
+    MDSM_EAGAIN = 10   /* nothing ready yet (serving poll)                               */
+} mdsm_status;
+
+/* input sample types */
+enum { MDSM_U8 = 0, MDSM_U16 = 1, MDSM_I16 = 2, MDSM_F32 = 3, MDSM_I32 = 4 };
+/* output (dedispersed series) types */
+enum { MDSM_OUT_F32 = 0, MDSM_OUT_I32 = 1 };
+/* accumulation: AUTO = exact INT32 for integer samples, FP32 for float samples */
+enum { MDSM_ACC_AUTO = 0, MDSM_ACC_I32 = 1, MDSM_ACC_F32 = 2 };
+
+/* How a DM trial's integer sample shift is formed (all computed once, on the host, into a
+ * table; the kernels index with integers only). */
+enum {
+    MDSM_SHIFT_L1 = 0,         /* trunc(dmshift_f32[c] * fma(i, dmstep/tsamp, lowdm/tsamp)):
+                                  src/mdsm/dedispersion_kernel.cu:27,36 (the default kernel)   */
+    MDSM_SHIFT_L1_MULADD = 1,  /* the same, start + i*step evaluated without contraction      */
+    MDSM_SHIFT_OPT = 2,        /* floor(dmshift_f32[c] * (fma(i, dmstep, lowdm)/tsamp)):
+                                  src/mdsm/dedispersion_kernel.cu:54,70                        */
+    MDSM_SHIFT_OPT_MULADD = 3,
+    MDSM_SHIFT_FP64_TRUNC = 4, /* trunc(K*(f^-2 - ftop^-2)*DM/tsamp) in double               */
+    MDSM_SHIFT_FP64_ROUND = 5  /* the same, rounded to nearest                                */
+};
+
+/* One uniform run of DM trials, dm_i = lowdm + i*dmstep (one reference launch). */
+typedef struct {
+    float lowdm;
+    float dmstep;
+    int ndms;
+} mdsm_segment;
+
+/* Brute-force plan.  Replaces the brute-force set-up of initialiseMDSM
+ * (src/mdsm/dedispersion_manager.cpp:286-318) and the shift upload of the worker
+ * (src/mdsm/dedispersion_thread.cu:261-263). */
+typedef struct {
+    int nchans;
+    float fch1;    /* MHz, frequency of channel 0                                   */
+    float foff;    /* MHz per channel (negative: channel 0 is the top of the band)   */
+    float tsamp;   /* seconds                                                       */
+    int nsamp;     /* output samples per block                                      */
+    const mdsm_segment *segs;
+    int nsegs;
+    int shift_mode;  /* MDSM_SHIFT_*                                                */
+    double K;        /* dispersion constant for the FP64 modes; 0 -> 4148.741601    */
+    int in_dtype;    /* MDSM_U8 / MDSM_U16 / MDSM_I16 / MDSM_F32                    */
+    int out_dtype;   /* MDSM_OUT_F32 / MDSM_OUT_I32                                 */
+    int acc;         /* MDSM_ACC_*                                                  */
+    int dm_block;    /* DM trials per CTA tile; 0 = choose                          */
+    int kernel;      /* 0 = choose, 1 = generic smem kernel, 2 = packed 8-bit kernel */
+} mdsm_brute_desc;
+
+/* Two-stage subband plan, one or more passes with downsample 1.  Replaces the subband set-up
+ * of initialiseMDSM and subband_dedispersion (src/mdsm/dedispersion_thread.cu:97-217).
+ * Pass fields used: lowdm, highdm, dmstep, sub_dmstep, ncalls, calldms (binsize must be 1). */
+typedef struct {
+    int nchans;
+    float fch1, foff, tsamp;
+    int nsamp;
+    int nsubs;
+    const SUBBAND_PASSES *passes;
+    int npasses;
+    int use_fma;   /* 1: start + i*step contracted (as the device code evaluates it)   */
+    int in_dtype, out_dtype, acc;
+} mdsm_subband_desc;
+
+typedef struct mdsm_plan_s mdsm_plan;
+
+typedef struct {
+    int nchans, ndms, nsamp, maxshift;
+    long long in_stride;  /* device row pitch (elements) the device entry points expect      */
+    long long in_bytes;   /* device input bytes the device entry points may read            */
+    long long out_bytes;  /* ndms * nsamp * output element size                              */
+    int in_dtype, out_dtype, acc;
+    int dm_block, time_tile, kernel;
+    int nstages;          /* 1 brute force, 2 subband                                       */
+    long long work_bytes; /* plan-owned device scratch (subband intermediate)               */
+} mdsm_plan_info;
+
+/* src/mdsm/dedispersion_manager.cpp:262-265 */
+float mdsm_dmdelay(float f1, float f2);
+const char *mdsm_last_error(void);
+const char *mdsm_version(void);
+
+mdsm_status mdsm_brute_plan_create(const mdsm_brute_desc *desc, mdsm_plan **out);
+mdsm_status mdsm_subband_plan_create(const mdsm_subband_desc *desc, mdsm_plan **out);
+void mdsm_plan_destroy(mdsm_plan *plan);
+mdsm_status mdsm_plan_get_info(const mdsm_plan *plan, mdsm_plan_info *info);
+/* Integer shifts, row-major [ndms][nchans] (brute) or stage tables (subband: stage 1
+ * [ncalls][nchans] of the first pass when which = 1, stage 2 [ndms][nsubs] when which = 2). */
+mdsm_status mdsm_plan_shift_table(const mdsm_plan *plan, int which, int32_t *out);
+/* DM value of every output row (float). */
+mdsm_status mdsm_plan_dm_values(const mdsm_plan *plan, float *out);
+/* Per-channel delays, float[nchans] (src/mdsm/dedispersion_manager.cpp:286-289). */
+mdsm_status mdsm_plan_dmshifts(const mdsm_plan *plan, float *out);
+
+/* Host-only table builders (no device needed).  Same arithmetic as the plans use.
+ * mdsm_dmshifts: src/mdsm/dedispersion_manager.cpp:286-289.
+ * mdsm_brute_shift_table: S [ndms][nchans], dm values [ndms], *maxshift = max(S); replaces the
+ *   shift formed inside src/mdsm/dedispersion_kernel.cu:27,36 / :54,70.
+ * mdsm_subband_shift_tables: pass `pass`'s S1 [ncalls][nchans] and S2 [ncalls*calldms][nsubs]
+ *   (src/mdsm/dedispersion_kernel.cu:148,163,167 and :54,70 as launched by
+ *   src/mdsm/dedispersion_thread.cu:146-210). */
+mdsm_status mdsm_dmshifts(int nchans, float fch1, float foff, float *out);
+mdsm_status mdsm_brute_shift_table(const mdsm_brute_desc *desc, int32_t *S, float *dm_values,
+                                   int *maxshift);
+mdsm_status mdsm_subband_shift_tables(const mdsm_subband_desc *desc, int pass, int32_t *S1,
+                                      int32_t *S2);
+
+/* Dedisperse one block on the device.  d_in: channel-major with row pitch in_stride elements
+ * (>= nsamp + maxshift, a multiple of 16 bytes) and in_bytes readable bytes (>= info.in_bytes).
+ * d_out: [ndms] rows of out_stride elements.  Replaces call_dedisperse's kernel dispatch
+ * (src/mdsm/dedispersion_wrapper.cu:7-9 -> dedispersion_thread.cu:332-341). */
+mdsm_status mdsm_dedisperse_device(mdsm_plan *plan, const void *d_in, long long in_stride,
+                                   size_t in_bytes, void *d_out, long long out_stride,
+                                   void *stream);
+/* The same through host buffers: h_in channel-major with pitch h_in_stride elements (the
+ * reference's nsamp + maxshift), h_out [ndms][nsamp].  Copies H2D, runs, copies D2H and
+ * synchronises the stream (src/mdsm/dedispersion_thread.cu:284-298,352-355). */
+mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_in_stride,
+                                 void *h_out, void *stream);
+/* Number of kernels the last dedisperse call on this plan launched. */
+int mdsm_plan_last_launches(const mdsm_plan *plan);
+
+/* ---------------------------------------------------------------------------------------- */
+/* RFI clipping (src/prototypes/rfi_clipper.cu:8-67): per-channel then per-spectrum.          */
+/* In place on a channel-major device buffer of len samples per row.  k <= 0 skips a pass.   */
+/* Integer samples are replaced by the mean rounded to nearest even.                          */
+mdsm_status mdsm_rfi_clip_device(void *d_x, int dtype, int nchans, long long stride,
+                                 long long len, double k_chan, double k_spec, void *stream);
+
+/* ---------------------------------------------------------------------------------------- */
+/* Reference detector (src/mdsm/dedispersion_output.cpp:135-213, mean == NULL, one device):  */
+/* global mean/rms over the block, median-of-five, median - mean >= threshold*rms and DM>1.   */
+typedef struct {
+    int32_t dm_idx;
+    int32_t sample;
+    float snr;
+    int32_t width;   /* boxcar width (1 for the median-of-five detector) */
+} mdsm_candidate;
+
+/* d_series: float [ndms][nsamp] on the device.  lowdm/dmstep describe a single uniform plan
+ * as the reference assumes.  Candidates are written to h_cands (up to cap, sorted by dm then
+ * sample); *ncand receives the total found.  mean/rms receive the statistics. */
+mdsm_status mdsm_ref_detect_device(const float *d_series, int ndms, int nsamp, float lowdm,
+                                   float dmstep, float threshold, mdsm_candidate *h_cands,
+                                   long long cap, long long *ncand, float *mean, float *rms,
+                                   void *stream);
+
+/* Boxcar single-pulse search (src/prototypes/singlepulse.cpp:41-146, restated): widths
+ * 1,2,4..2^(nwidths-1); per-DM mean/sigma; SNR = (sum - w*mean)/(sigma*sqrt(w)); per-sample
+ * best width; non-maximum suppression with radius max(w/2,1).  d_series is [ndms][nsamp] of
+ * dtype MDSM_OUT_F32 or MDSM_OUT_I32.  Candidates sorted by dm then sample. */
+mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, int ndms,
+                                      int nsamp, int nwidths, double threshold,
+                                      mdsm_candidate *h_cands, long long cap, long long *ncand,
+                                      void *stream);
+
+/* ---------------------------------------------------------------------------------------- */
+/* Compatibility layer: the reference stage interface (src/mdsm/dedispersion_manager.h:7-12) */
+/* with C linkage.  include/dedispersion_manager.h wraps these under the reference's C++      */
+/* names and default arguments.  Same buffer ownership, one-block latency and stop protocol.  */
+SURVEY *mdsm_processSurveyParameters(const char *xml_path);
+float *mdsm_initialiseMDSM(SURVEY *survey);
+float *mdsm_next_chunk(unsigned int data_read, unsigned *samples, double timestamp,
+                       double blockRate, float *mean, float *rms);
+int mdsm_start_processing(unsigned int data_read);
+void mdsm_tearDownMDSM(void);
+/* Candidates found for the block returned by the last next_chunk (detector output). */
+long long mdsm_compat_candidates(mdsm_candidate *out, long long cap);
+void mdsm_free_survey(SURVEY *survey);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

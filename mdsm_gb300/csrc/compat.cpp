@@ -1,0 +1,518 @@
+// compat.cpp -- the reference's stage interface (src/mdsm/dedispersion_manager.h:7-12) over the
+// GB300 library, with C linkage; include/dedispersion_manager.h gives it the reference's C++
+// names and default arguments.
+//
+// Contract kept from the reference (src/mdsm/dedispersion_manager.cpp:269-501,
+// src/mdsm/dedispersion_thread.cu:246-401, src/mdsm/dedispersion_output.cpp:216-356):
+//  * one global instance; processSurveyParameters -> initialiseMDSM -> (next_chunk,
+//    start_processing)* -> tearDownMDSM from one caller thread;
+//  * initialiseMDSM returns the library-owned input buffer, channel-major
+//    [nchans][nsamp + maxshift] float; block 0 fills every column, later blocks fill columns
+//    [maxshift, maxshift + nsamp) and the library supplies the previous block's last maxshift
+//    samples itself;
+//  * next_chunk returns the dedispersed output of the previous block ([ndms][nsamp] float,
+//    valid until the next next_chunk) or NULL on the first call; `samples` is that block's
+//    sample count;
+//  * start_processing returns once the input buffer may be refilled; data_read == 0 stops,
+//    and the second start_processing(0) returns 0;
+//  * candidates of every block are written as text "time, dm, snr" to the reference's output
+//    files (dedispersion_output.cpp:194-196,233-302).
+// GB300 design: no worker threads and barriers.  The overlap tail stays on the device and is
+// moved there with one device-to-device copy (no host memcpy per channel), only the new
+// samples cross the host link, the input/output buffers are pinned, and detection runs on the
+// device.  Errors set mdsm_last_error() and return NULL / 0 instead of exit(0).
+#include <cctype>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <ctime>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "internal.h"
+
+namespace mdsm {
+
+namespace {
+
+// ------------------------------------------------------------------------------------------
+// a small XML reader for the observation file schema
+// ------------------------------------------------------------------------------------------
+struct XNode {
+    std::string tag;
+    std::vector<std::pair<std::string, std::string>> attrs;
+    std::string text;
+    std::vector<XNode> kids;
+    const char *attr(const char *name) const
+    {
+        for (auto &a : attrs)
+            if (strcasecmp(a.first.c_str(), name) == 0) return a.second.c_str();
+        return nullptr;
+    }
+};
+
+struct XParser {
+    const std::string &s;
+    size_t i = 0;
+    bool ok = true;
+    explicit XParser(const std::string &src) : s(src) {}
+    void ws()
+    {
+        while (i < s.size() && isspace((unsigned char)s[i])) ++i;
+    }
+    void skip_misc()
+    {
+        for (;;) {
+            ws();
+            if (s.compare(i, 4, "<!--") == 0) {
+                size_t e = s.find("-->", i + 4);
+                i = e == std::string::npos ? s.size() : e + 3;
+            } else if (s.compare(i, 2, "<?") == 0 || s.compare(i, 2, "<!") == 0) {
+                size_t e = s.find('>', i);
+                i = e == std::string::npos ? s.size() : e + 1;
+            } else {
+                return;
+            }
+        }
+    }
+    std::string name()
+    {
+        size_t b = i;
+        while (i < s.size() && (isalnum((unsigned char)s[i]) || s[i] == '_' || s[i] == '-' ||
+                                s[i] == ':' || s[i] == '.'))
+            ++i;
+        return s.substr(b, i - b);
+    }
+    bool element(XNode &n)
+    {
+        skip_misc();
+        if (i >= s.size() || s[i] != '<') return false;
+        ++i;
+        n.tag = name();
+        if (n.tag.empty()) return ok = false;
+        for (;;) {
+            ws();
+            if (i >= s.size()) return ok = false;
+            if (s[i] == '/') {
+                if (i + 1 < s.size() && s[i + 1] == '>') {
+                    i += 2;
+                    return true;
+                }
+                return ok = false;
+            }
+            if (s[i] == '>') {
+                ++i;
+                break;
+            }
+            std::string an = name();
+            ws();
+            if (an.empty() || i >= s.size() || s[i] != '=') return ok = false;
+            ++i;
+            ws();
+            if (i >= s.size() || (s[i] != '"' && s[i] != '\'')) return ok = false;
+            char q = s[i++];
+            size_t e = s.find(q, i);
+            if (e == std::string::npos) return ok = false;
+            n.attrs.emplace_back(an, s.substr(i, e - i));
+            i = e + 1;
+        }
+        for (;;) {
+            skip_misc();
+            if (i >= s.size()) return ok = false;
+            if (s.compare(i, 2, "</") == 0) {
+                i += 2;
+                name();
+                ws();
+                if (i < s.size() && s[i] == '>') ++i;
+                return true;
+            }
+            if (s[i] == '<') {
+                XNode k;
+                if (!element(k)) return false;
+                n.kids.push_back(std::move(k));
+            } else {
+                size_t e = s.find('<', i);
+                if (e == std::string::npos) return ok = false;
+                n.text += s.substr(i, e - i);
+                i = e;
+            }
+        }
+    }
+};
+
+float fattr(const XNode &n, const char *a, float dflt)
+{
+    const char *v = n.attr(a);
+    return v ? (float)atof(v) : dflt;
+}
+unsigned uattr(const XNode &n, const char *a, unsigned dflt)
+{
+    const char *v = n.attr(a);
+    return v ? (unsigned)strtoul(v, nullptr, 10) : dflt;
+}
+
+// ------------------------------------------------------------------------------------------
+// the single instance
+// ------------------------------------------------------------------------------------------
+struct Instance {
+    bool live = false;
+    SURVEY *survey = nullptr;
+    mdsm_plan *plan = nullptr;
+    cudaStream_t st = nullptr;
+    float *h_in = nullptr;            // pinned [nchans][nsamp+maxshift]
+    float *h_out[2] = {nullptr, nullptr};
+    void *d_in[2] = {nullptr, nullptr};
+    size_t d_in_bytes = 0;
+    void *d_out = nullptr;
+    long long stride = 0;             // host and device row pitch (elements)
+    long long blocks = 0;             // blocks processed
+    unsigned pending_read = 0;        // data_read given to the last next_chunk
+    unsigned prev_read = 0;           // samples of the last processed block
+    long long returned = 0;           // blocks count when next_chunk last returned output
+    bool stopping = false, stopped_once = false;
+    double ts = 0, rate = 0;
+    std::vector<mdsm_candidate> cands;  // candidates of the last processed block
+    FILE *fp = nullptr;
+    long long written = 0;
+};
+
+Instance g;
+
+void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double ts, double rate)
+{
+    SURVEY *s = g.survey;
+    if (!g.fp || (!s->single_file_mode && g.written == 0)) {
+        char path[512];
+        if (s->single_file_mode) {
+            snprintf(path, sizeof path, "%s/%s.dat", s->basedir, s->fileprefix);
+        } else {
+            time_t now = s->use_pc_time ? time(nullptr) : (time_t)ts;
+            struct tm tmv;
+            localtime_r(&now, &tmv);
+            char tb[32];
+            strftime(tb, sizeof tb, "%F_%T", &tmv);
+            snprintf(path, sizeof path, "%s/%s_%s_%u.dat", s->basedir, s->fileprefix, tb,
+                     s->secs_per_file);
+        }
+        if (g.fp) fclose(g.fp);
+        g.fp = fopen(path, "w");
+    }
+    if (!g.fp) return;
+    std::vector<float> dmv(g.plan->p.ndms);
+    mdsm_plan_dm_values(g.plan, dmv.data());
+    for (long long i = 0; i < nc && i < (long long)c.size(); ++i)
+        fprintf(g.fp, "%lf, %f, %f\n", ts + c[i].sample * rate, dmv[c[i].dm_idx], c[i].snr);
+    fflush(g.fp);
+    if (!s->single_file_mode) {
+        g.written += g.prev_read;
+        if (g.written * rate > s->secs_per_file) {
+            g.written = 0;
+            fclose(g.fp);
+            g.fp = nullptr;
+        }
+    }
+}
+
+void release()
+{
+    if (g.fp) fclose(g.fp);
+    if (g.plan) mdsm_plan_destroy(g.plan);
+    if (g.h_in) cudaFreeHost(g.h_in);
+    for (int i = 0; i < 2; ++i) {
+        if (g.h_out[i]) cudaFreeHost(g.h_out[i]);
+        if (g.d_in[i]) cudaFree(g.d_in[i]);
+    }
+    if (g.d_out) cudaFree(g.d_out);
+    if (g.st) cudaStreamDestroy(g.st);
+    g = Instance();
+}
+
+// One block through the device: tail carry, H2D of the new samples, dedispersion, detection,
+// D2H of the series.
+mdsm_status process_block(unsigned data_read)
+{
+    Plan &p = g.plan->p;
+    const long long ms = p.maxshift, ns = p.nsamp;
+    const int cur = (int)(g.blocks & 1), prv = cur ^ 1;
+    if (g.blocks == 0) {
+        MDSM_CUDA_TRY(cudaMemcpy2DAsync(g.d_in[cur], g.stride * 4, g.h_in, g.stride * 4,
+                                        (size_t)(ns + ms) * 4, p.nchans, cudaMemcpyHostToDevice,
+                                        g.st));
+    } else {
+        if (ms > 0)
+            MDSM_CUDA_TRY(cudaMemcpy2DAsync(g.d_in[cur], g.stride * 4,
+                                            static_cast<float *>(g.d_in[prv]) + ns, g.stride * 4,
+                                            (size_t)ms * 4, p.nchans, cudaMemcpyDeviceToDevice,
+                                            g.st));
+        MDSM_CUDA_TRY(cudaMemcpy2DAsync(static_cast<float *>(g.d_in[cur]) + ms, g.stride * 4,
+                                        g.h_in + ms, g.stride * 4, (size_t)ns * 4, p.nchans,
+                                        cudaMemcpyHostToDevice, g.st));
+    }
+    // The host input buffer may be refilled once the copies above have run.
+    MDSM_CUDA_TRY(cudaStreamSynchronize(g.st));
+    MDSM_TRY(plan_run_device(p, g.d_in[cur], g.stride, g.d_in_bytes, g.d_out, ns, g.st));
+    long long nc = 0;
+    std::vector<mdsm_candidate> c(1 << 16);
+    if (p.kind == 1 && g.survey->useBruteForce) {
+        MDSM_TRY(ref_detect(static_cast<const float *>(g.d_out), p.ndms, (int)ns,
+                            g.survey->lowdm, g.survey->dmstep, g.survey->detection_threshold,
+                            c.data(), (long long)c.size(), &nc, nullptr, nullptr, g.st));
+    }
+    MDSM_CUDA_TRY(cudaMemcpyAsync(g.h_out[cur], g.d_out, (size_t)p.ndms * ns * 4,
+                                  cudaMemcpyDeviceToHost, g.st));
+    MDSM_TRY(check_err_word(p.d_err, g.st));
+    c.resize((size_t)std::min<long long>(nc, (long long)c.size()));
+    g.cands = c;
+    g.prev_read = data_read;
+    write_candidates(c, nc, g.ts, g.rate);
+    g.blocks++;
+    return MDSM_OK;
+}
+
+}  // namespace
+}  // namespace mdsm
+
+using namespace mdsm;
+
+extern "C" {
+
+// src/mdsm/dedispersion_manager.cpp:40-199 (same tags, attributes and defaults).
+SURVEY *mdsm_processSurveyParameters(const char *xml_path)
+{
+    std::ifstream f(xml_path ? xml_path : "");
+    if (!f) {
+        set_error(std::string("Cannot open observation file '") + (xml_path ? xml_path : "") + "'");
+        return nullptr;
+    }
+    std::stringstream ss;
+    ss << f.rdbuf();
+    const std::string src = ss.str();
+    XParser px(src);
+    XNode root;
+    if (!px.element(root) || !px.ok) {
+        set_error("observation file: parse error near byte " + std::to_string(px.i));
+        return nullptr;
+    }
+    if (strcasecmp(root.tag.c_str(), "observation") != 0) {
+        set_error("Invalid root element in observation parameter xml file, should be 'observation'");
+        return nullptr;
+    }
+    SURVEY *s = static_cast<SURVEY *>(calloc(1, sizeof(SURVEY)));
+    // defaults: dedispersion_manager.cpp:84-95
+    s->useBruteForce = 0;
+    s->useL1Cache = 1;
+    s->detection_threshold = 5.0f;
+    strcpy(s->fileprefix, "output");
+    strcpy(s->basedir, ".");
+    s->secs_per_file = 600;
+    s->use_pc_time = 1;
+    s->single_file_mode = 0;
+    std::vector<SUBBAND_PASSES> passes;
+    for (const XNode &e : root.kids) {
+        const char *t = e.tag.c_str();
+        if (!strcasecmp(t, "frequencies")) {
+            s->fch1 = fattr(e, "top", 0);
+            s->foff = fattr(e, "offset", 0);
+        } else if (!strcasecmp(t, "dm")) {
+            s->lowdm = fattr(e, "lowDM", 0);
+            s->tdms = uattr(e, "numDMs", 0);
+            s->dmstep = fattr(e, "dmStep", 0);
+            s->useBruteForce = uattr(e, "useBruteForce", 0) != 0;
+            s->useL1Cache = uattr(e, "useL1Cache", 0) != 0;
+        } else if (!strcasecmp(t, "channels")) {
+            s->nchans = uattr(e, "number", 0);
+            s->nsubs = uattr(e, "subbands", 0);
+        } else if (!strcasecmp(t, "timing")) {
+            s->tsamp = fattr(e, "tsamp", 0);
+        } else if (!strcasecmp(t, "samples")) {
+            s->nsamp = uattr(e, "number", 0);
+        } else if (!strcasecmp(t, "detection")) {
+            s->detection_threshold = fattr(e, "threshold", 5.0f);
+        } else if (!strcasecmp(t, "output")) {
+            const char *v;
+            if ((v = e.attr("filePrefix"))) snprintf(s->fileprefix, sizeof s->fileprefix, "%s", v);
+            if ((v = e.attr("baseDirectory"))) snprintf(s->basedir, sizeof s->basedir, "%s", v);
+            s->secs_per_file = uattr(e, "secondsPerFile", 600);
+            s->use_pc_time = (char)uattr(e, "usePCTime", 1);
+            s->single_file_mode = (char)uattr(e, "singleFileMode", 0);
+        } else if (!strcasecmp(t, "gpus")) {
+            std::vector<unsigned> ids;
+            std::string v = e.attr("ids") ? e.attr("ids") : "";
+            std::stringstream is(v);
+            std::string tok;
+            while (std::getline(is, tok, ','))
+                if (!tok.empty()) ids.push_back((unsigned)strtoul(tok.c_str(), nullptr, 10));
+            s->num_gpus = (unsigned)ids.size();
+            s->gpu_ids = static_cast<unsigned *>(malloc(sizeof(unsigned) * (ids.size() + 1)));
+            for (size_t i = 0; i < ids.size(); ++i) s->gpu_ids[i] = ids[i];
+        } else if (!strcasecmp(t, "passes")) {
+            for (const XNode &pn : e.kids) {
+                SUBBAND_PASSES ps;
+                memset(&ps, 0, sizeof ps);
+                for (const XNode &q : pn.kids) {
+                    const char *qt = q.tag.c_str();
+                    const char *tx = q.text.c_str();
+                    if (!strcasecmp(qt, "lowDm")) ps.lowdm = (float)atof(tx);
+                    else if (!strcasecmp(qt, "highDm")) ps.highdm = (float)atof(tx);
+                    else if (!strcasecmp(qt, "deltaDm")) ps.dmstep = (float)atof(tx);
+                    else if (!strcasecmp(qt, "downsample")) ps.binsize = atoi(tx);
+                    else if (!strcasecmp(qt, "subDm")) ps.sub_dmstep = (float)atof(tx);
+                    else if (!strcasecmp(qt, "numDms")) ps.ndms = atoi(tx);
+                    else if (!strcasecmp(qt, "dmsPerCall")) ps.calldms = atoi(tx);
+                    else if (!strcasecmp(qt, "ncalls")) ps.ncalls = atoi(tx);
+                }
+                passes.push_back(ps);
+            }
+        }
+    }
+    s->num_passes = (unsigned)passes.size();
+    if (!passes.empty()) {
+        s->pass_parameters =
+            static_cast<SUBBAND_PASSES *>(malloc(sizeof(SUBBAND_PASSES) * passes.size()));
+        memcpy(s->pass_parameters, passes.data(), sizeof(SUBBAND_PASSES) * passes.size());
+    }
+    if (!s->useBruteForce) {  // :190-194
+        s->tdms = 0;
+        for (auto &ps : passes) s->tdms += (unsigned)ps.ndms;
+    }
+    return s;
+}
+
+void mdsm_free_survey(SURVEY *s)
+{
+    if (!s) return;
+    free(s->pass_parameters);
+    free(s->gpu_ids);
+    free(s);
+}
+
+// src/mdsm/dedispersion_manager.cpp:269-382
+float *mdsm_initialiseMDSM(SURVEY *s)
+{
+    if (!s) {
+        set_error("initialiseMDSM: null survey");
+        return nullptr;
+    }
+    if (g.live) release();
+    g.survey = s;
+    if (s->nsamp == 0) s->nsamp = 1u << 16;  // reference: fill GPU memory; here a fixed block
+    mdsm_status st;
+    if (s->useBruteForce) {
+        mdsm_segment seg{s->lowdm, s->dmstep, (int)s->tdms};
+        mdsm_brute_desc d;
+        memset(&d, 0, sizeof d);
+        d.nchans = (int)s->nchans;
+        d.fch1 = s->fch1;
+        d.foff = s->foff;
+        d.tsamp = s->tsamp;
+        d.nsamp = (int)s->nsamp;
+        d.segs = &seg;
+        d.nsegs = 1;
+        d.shift_mode = s->useL1Cache ? MDSM_SHIFT_L1 : MDSM_SHIFT_OPT;
+        d.in_dtype = MDSM_F32;
+        d.out_dtype = MDSM_OUT_F32;
+        st = mdsm_brute_plan_create(&d, &g.plan);
+    } else {
+        mdsm_subband_desc d;
+        memset(&d, 0, sizeof d);
+        d.nchans = (int)s->nchans;
+        d.fch1 = s->fch1;
+        d.foff = s->foff;
+        d.tsamp = s->tsamp;
+        d.nsamp = (int)s->nsamp;
+        d.nsubs = (int)s->nsubs;
+        d.passes = s->pass_parameters;
+        d.npasses = (int)s->num_passes;
+        d.use_fma = 1;
+        d.in_dtype = MDSM_F32;
+        d.out_dtype = MDSM_OUT_F32;
+        st = mdsm_subband_plan_create(&d, &g.plan);
+    }
+    if (st != MDSM_OK) {
+        g.survey = nullptr;
+        return nullptr;
+    }
+    Plan &p = g.plan->p;
+    s->maxshift = (unsigned)p.maxshift;
+    s->num_threads = 1;
+    if (s->samplesPerChunk == 0) s->samplesPerChunk = s->nsamp;
+    g.stride = (long long)p.nsamp + p.maxshift;
+    const long long dev_stride = p.in_stride;
+    long long need = 0;
+    if (plan_in_requirements(p, dev_stride, &need) != MDSM_OK) return nullptr;
+    g.stride = dev_stride;  // host pitch = device pitch (>= nsamp + maxshift)
+    if (cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaHostAlloc((void **)&g.h_in, (size_t)g.stride * p.nchans * 4, 0) != cudaSuccess ||
+        cudaHostAlloc((void **)&g.h_out[0], (size_t)p.ndms * p.nsamp * 4, 0) != cudaSuccess ||
+        cudaHostAlloc((void **)&g.h_out[1], (size_t)p.ndms * p.nsamp * 4, 0) != cudaSuccess ||
+        cudaMalloc(&g.d_in[0], (size_t)need + 256) != cudaSuccess ||
+        cudaMalloc(&g.d_in[1], (size_t)need + 256) != cudaSuccess ||
+        cudaMalloc(&g.d_out, (size_t)p.ndms * p.nsamp * 4) != cudaSuccess) {
+        set_error("initialiseMDSM: allocation failed");
+        release();
+        return nullptr;
+    }
+    cudaMemset(g.d_in[0], 0, (size_t)need + 256);
+    cudaMemset(g.d_in[1], 0, (size_t)need + 256);
+    memset(g.h_in, 0, (size_t)g.stride * p.nchans * 4);
+    g.d_in_bytes = (size_t)need + 256;
+    g.live = true;
+    return g.h_in;
+}
+
+// src/mdsm/dedispersion_manager.cpp:416-484
+float *mdsm_next_chunk(unsigned int data_read, unsigned *samples, double timestamp,
+                       double blockRate, float *mean, float *rms)
+{
+    (void)mean;
+    (void)rms;
+    if (!g.live) {
+        set_error("next_chunk before initialiseMDSM");
+        return nullptr;
+    }
+    g.pending_read = data_read;
+    if (data_read == 0) g.stopping = true;
+    g.survey->timestamp = timestamp;
+    g.survey->blockRate = blockRate;
+    g.ts = timestamp;
+    g.rate = blockRate;
+    if (g.blocks == 0) {
+        if (samples) *samples = (unsigned)-1;
+        return nullptr;
+    }
+    // A block's output is reported once; a repeated call with nothing new reports 0 samples.
+    const bool fresh = g.blocks != g.returned;
+    g.returned = g.blocks;
+    if (samples) *samples = fresh ? g.prev_read : 0u;
+    return g.h_out[(g.blocks - 1) & 1];
+}
+
+// src/mdsm/dedispersion_manager.cpp:487-501
+int mdsm_start_processing(unsigned int data_read)
+{
+    if (!g.live) {
+        set_error("start_processing before initialiseMDSM");
+        return 0;
+    }
+    if (data_read == 0) {
+        if (g.stopped_once) return 0;
+        g.stopped_once = true;
+        return (int)(g.blocks + 1);
+    }
+    if (process_block(data_read) != MDSM_OK) return 0;
+    return (int)g.blocks;
+}
+
+void mdsm_tearDownMDSM(void) { release(); }
+
+long long mdsm_compat_candidates(mdsm_candidate *out, long long cap)
+{
+    const long long n = (long long)g.cands.size();
+    for (long long i = 0; i < n && i < cap; ++i) out[i] = g.cands[i];
+    return n;
+}
+
+}  // extern "C"

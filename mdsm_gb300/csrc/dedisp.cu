@@ -1,0 +1,368 @@
+// dedisp.cu -- the shift-and-sum kernel shared by brute-force dedispersion and both subband
+// stages, and the host code that tiles a shift table for it.
+//
+// What it computes (src/mdsm/dedispersion_kernel.cu:11-48 and :51-77, :144-175):
+//     out[g][d][t] = sum_{c < nchans} in[g][c][t + S[g][d][c]],   t < nsamp
+// with the channels summed in increasing c from zero, so float results are bit-identical to
+// the reference kernels' sequential per-thread sums.
+//
+// How (GB300): one CTA owns a block of Db DM trials x a tile of T samples.  For every channel
+// the CTA needs one contiguous segment of the input row, [t0 + smin, t0 + T + smax), where
+// smin/smax are the smallest/largest shift of its DMs in that channel.  Warp 0 stages CC such
+// segments at a time into shared memory with 1-D bulk copies (the TMA engine) completing on an
+// mbarrier, NST stages deep, while all warps accumulate from the previous stage: each lane
+// holds DPW DMs x R samples (strided by 32) in registers, so every staged sample is reused
+// by up to Db DM trials and all shared-memory reads are bank-conflict free.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "internal.h"
+#include "ptx.cuh"
+
+namespace mdsm {
+
+struct KArgs {
+    const unsigned char *in;
+    long long in_stride, in_group_stride;    // elements
+    unsigned char *out;
+    long long out_stride, out_group_stride;  // elements
+    const int32_t *rel;                      // [g][blk][c][DB]
+    const int32_t *sminspan;                 // [g][blk][c][2]
+    int nchans, ndms, nsamp, nblk, rowcap, nst, out_i32;
+    unsigned *err;
+};
+
+__device__ __forceinline__ unsigned warp_sum_u32(unsigned v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+template <typename TAcc>
+__device__ __forceinline__ void store_out(unsigned char *orow, int t, TAcc v, int out_i32)
+{
+    if (out_i32)
+        reinterpret_cast<int32_t *>(orow)[t] = static_cast<int32_t>(v);
+    else
+        reinterpret_cast<float *>(orow)[t] = static_cast<float>(v);
+}
+
+template <typename TIn, typename TAcc, int R, int DPW, int NW, int CC>
+__global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
+{
+    constexpr int T = 32 * R;
+    constexpr int DB = NW * DPW;
+    constexpr int SZ = (int)sizeof(TIn);
+    extern __shared__ __align__(128) unsigned char smem[];
+
+    const int nst = a.nst;
+    const int rowbytes = a.rowcap * SZ;
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);                     // nst x 8 B
+    unsigned char *rows = smem + 128;                                         // nst*CC rows
+    int32_t *relsm = reinterpret_cast<int32_t *>(rows + (size_t)nst * CC * rowbytes);
+    int32_t *basesm = relsm + nst * CC * DB;
+
+    const int blk = blockIdx.x, g = blockIdx.z;
+    const long long t0 = (long long)blockIdx.y * T;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned char *in_g = a.in + (size_t)(g * a.in_group_stride) * SZ;
+    const size_t bofs = (size_t)(g * a.nblk + blk) * a.nchans;
+    const int32_t *rel_b = a.rel + bofs * DB;
+    const int32_t *ss_b = a.sminspan + bofs * 2;
+    const int nchunks = (a.nchans + CC - 1) / CC;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < nst; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    // Warp 0 stages chunk k (channels k*CC ..) into stage s.
+    auto fill = [&](int s, int k) {
+        const int c0 = k * CC;
+        const int nc = min(CC, a.nchans - c0);
+        unsigned bytes = 0;
+        const unsigned char *src = nullptr;
+        if (lane < nc) {
+            const int c = c0 + lane;
+            const long long start = t0 + ss_b[2 * c];
+            const long long end = start + T + ss_b[2 * c + 1];
+            const long long sb = (start * SZ) & ~15LL;
+            const long long eb = (end * SZ + 15) & ~15LL;
+            bytes = (unsigned)(eb - sb);
+            basesm[s * CC + lane] = (int)(start - sb / SZ);
+            src = in_g + (size_t)c * (size_t)a.in_stride * SZ + sb;
+        }
+        const unsigned relbytes = (unsigned)(nc * DB * 4);
+        const unsigned total = warp_sum_u32(bytes) + relbytes;
+        __syncwarp();
+        if (lane == 0) mbar_arrive_expect_tx(&bars[s], total);
+        __syncwarp();
+        if (lane < nc) bulk_g2s(rows + (size_t)(s * CC + lane) * rowbytes, src, bytes, &bars[s]);
+        if (lane == 0) bulk_g2s(relsm + s * CC * DB, rel_b + (size_t)c0 * DB, relbytes, &bars[s]);
+    };
+
+    if (warp == 0)
+        for (int s = 0; s < nst && s < nchunks; ++s) fill(s, s);
+
+    TAcc acc[DPW][R];
+#pragma unroll
+    for (int j = 0; j < DPW; ++j)
+#pragma unroll
+        for (int r = 0; r < R; ++r) acc[j][r] = TAcc(0);
+
+    int k = 0;
+    bool aborted = false;
+    for (; k < nchunks; ++k) {
+        const int s = k % nst;
+        const unsigned par = (unsigned)(k / nst) & 1u;
+        const bool ok = mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
+        if (ok) {
+            const int nc = min(CC, a.nchans - k * CC);
+            const unsigned char *rb = rows + (size_t)s * CC * rowbytes;
+            const int32_t *rs = relsm + s * CC * DB + warp * DPW;
+            const int32_t *bs = basesm + s * CC;
+#pragma unroll 2
+            for (int ci = 0; ci < nc; ++ci) {
+                const TIn *row = reinterpret_cast<const TIn *>(rb + (size_t)ci * rowbytes) +
+                                 bs[ci] + lane;
+#pragma unroll
+                for (int j = 0; j < DPW; ++j) {
+                    const TIn *p = row + rs[ci * DB + j];
+#pragma unroll
+                    for (int r = 0; r < R; ++r) acc[j][r] += static_cast<TAcc>(p[32 * r]);
+                }
+            }
+        }
+        if (__syncthreads_or(!ok)) {
+            aborted = true;
+            break;
+        }
+        if (warp == 0 && k + nst < nchunks) {
+            fence_proxy_async_smem();
+            fill(s, k + nst);
+        }
+    }
+
+    if (aborted) {
+        // Let this CTA's copies still in flight land before it exits (bounded as well).
+        for (int kk = k; kk < nchunks && kk < k + nst; ++kk)
+            mbar_wait_bounded(&bars[kk % nst], (unsigned)(kk / nst) & 1u, nullptr, 0);
+        return;
+    }
+
+    const int osz = a.out_i32 ? 4 : 4;
+#pragma unroll
+    for (int j = 0; j < DPW; ++j) {
+        const int d = blk * DB + warp * DPW + j;
+        if (d >= a.ndms) continue;
+        unsigned char *orow =
+            a.out + (size_t)(g * a.out_group_stride + (long long)d * a.out_stride) * osz;
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const long long t = t0 + lane + 32 * r;
+            if (t < a.nsamp) store_out<TAcc>(orow, (int)t, acc[j][r], a.out_i32);
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
+// host side
+// ------------------------------------------------------------------------------------------
+
+namespace {
+
+constexpr int kR = 8;
+constexpr int kNW = 8;
+
+template <typename TIn, typename TAcc, int DPW, int CC>
+void *kernel_ptr()
+{
+    return reinterpret_cast<void *>(&k_shift_sum<TIn, TAcc, kR, DPW, kNW, CC>);
+}
+
+template <typename TIn, typename TAcc, int CC>
+void *pick_dpw(int dpw)
+{
+    switch (dpw) {
+    case 4: return kernel_ptr<TIn, TAcc, 4, CC>();
+    case 2: return kernel_ptr<TIn, TAcc, 2, CC>();
+    default: return kernel_ptr<TIn, TAcc, 1, CC>();
+    }
+}
+
+void *select_kernel(int in_dtype, int acc_int, int dpw, int cc)
+{
+    // 1- and 2-byte samples stage 16 channels per step, 4-byte samples 8.
+    switch (in_dtype) {
+    case MDSM_U8:
+        return acc_int ? pick_dpw<uint8_t, int, 16>(dpw) : pick_dpw<uint8_t, float, 16>(dpw);
+    case MDSM_U16:
+        return acc_int ? pick_dpw<uint16_t, int, 16>(dpw) : pick_dpw<uint16_t, float, 16>(dpw);
+    case MDSM_I16:
+        return acc_int ? pick_dpw<int16_t, int, 16>(dpw) : pick_dpw<int16_t, float, 16>(dpw);
+    case MDSM_I32:
+        return pick_dpw<int32_t, int, 8>(dpw);
+    case MDSM_F32:
+    default:
+        return pick_dpw<float, float, 8>(dpw);
+    }
+    (void)cc;
+}
+
+size_t smem_for(const StageGeom &g)
+{
+    const size_t SZ = dtype_size(g.in_dtype);
+    return 128 + (size_t)g.nst * g.cc * g.rowcap * SZ + (size_t)g.nst * g.cc * g.Db * 4 +
+           (size_t)g.nst * g.cc * 4;
+}
+
+}  // namespace
+
+size_t dtype_size(int dtype)
+{
+    switch (dtype) {
+    case MDSM_U8: return 1;
+    case MDSM_U16:
+    case MDSM_I16: return 2;
+    default: return 4;
+    }
+}
+
+// Tile S[g][d][c] into per-block relative tables.  Fails if any shift is negative.
+mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
+{
+    const int SZ = (int)dtype_size(g.in_dtype);
+    g.R = kR;
+    g.T = 32 * kR;
+    g.cc = SZ == 4 ? 8 : 16;
+    g.kernel = 1;
+    const long long need = (long long)g.ngroups * g.ndms * g.nchans;
+    if ((long long)S.size() != need) return fail(MDSM_EINVAL, "shift table size mismatch");
+    int mx = 0;
+    for (long long i = 0; i < need; ++i) {
+        if (S[(size_t)i] < 0)
+            return fail(MDSM_EINVAL,
+                        "negative sample shift: channel 0 must be the highest frequency");
+        mx = std::max(mx, (int)S[(size_t)i]);
+    }
+    g.max_shift = mx;
+    // Try Db = 32, 16, 8 until the staged rows fit in shared memory.
+    const int dpws[3] = {4, 2, 1};
+    int first = g.DPW == 4 ? 0 : (g.DPW == 2 ? 1 : 2);
+    for (int i = first; i < 3; ++i) {
+        g.DPW = dpws[i];
+        g.Db = kNW * g.DPW;
+        g.nblk = (g.ndms + g.Db - 1) / g.Db;
+        g.rel.assign((size_t)g.ngroups * g.nblk * g.nchans * g.Db, 0);
+        g.sminspan.assign((size_t)g.ngroups * g.nblk * g.nchans * 2, 0);
+        int maxspan = 0;
+        for (int gi = 0; gi < g.ngroups; ++gi)
+            for (int b = 0; b < g.nblk; ++b) {
+                const int d0 = b * g.Db, d1 = std::min(g.ndms, d0 + g.Db);
+                for (int c = 0; c < g.nchans; ++c) {
+                    int lo = INT32_MAX, hi = INT32_MIN;
+                    for (int d = d0; d < d1; ++d) {
+                        const int v = S[((size_t)gi * g.ndms + d) * g.nchans + c];
+                        lo = std::min(lo, v);
+                        hi = std::max(hi, v);
+                    }
+                    const size_t o = (((size_t)gi * g.nblk + b) * g.nchans + c);
+                    g.sminspan[o * 2] = lo;
+                    g.sminspan[o * 2 + 1] = hi - lo;
+                    maxspan = std::max(maxspan, hi - lo);
+                    for (int d = d0; d < d1; ++d)
+                        g.rel[o * g.Db + (d - d0)] =
+                            S[((size_t)gi * g.ndms + d) * g.nchans + c] - lo;
+                }
+            }
+        g.max_span = maxspan;
+        const long long bytes = (long long)(g.T + maxspan) * SZ + 32;
+        g.rowcap = (int)(((bytes + 15) / 16) * 16 / SZ);
+        g.nst = 3;
+        g.smem_bytes = smem_for(g);
+        if (g.smem_bytes > 200 * 1024) {
+            g.nst = 2;
+            g.smem_bytes = smem_for(g);
+        }
+        if (g.smem_bytes <= 200 * 1024) return MDSM_OK;
+    }
+    return fail(MDSM_EINVAL, "DM plan too wide for shared-memory staging (shift span " +
+                                 std::to_string(g.max_span) + " per 8 DM trials)");
+}
+
+mdsm_status upload_stage(StageGeom &g)
+{
+    free_stage(g);
+    MDSM_CUDA_TRY(cudaMalloc(&g.d_rel, g.rel.size() * sizeof(int32_t)));
+    MDSM_CUDA_TRY(cudaMalloc(&g.d_sminspan, g.sminspan.size() * sizeof(int32_t)));
+    MDSM_CUDA_TRY(cudaMemcpy(g.d_rel, g.rel.data(), g.rel.size() * sizeof(int32_t),
+                             cudaMemcpyHostToDevice));
+    MDSM_CUDA_TRY(cudaMemcpy(g.d_sminspan, g.sminspan.data(),
+                             g.sminspan.size() * sizeof(int32_t), cudaMemcpyHostToDevice));
+    return MDSM_OK;
+}
+
+void free_stage(StageGeom &g)
+{
+    if (g.d_rel) cudaFree(g.d_rel);
+    if (g.d_sminspan) cudaFree(g.d_sminspan);
+    g.d_rel = nullptr;
+    g.d_sminspan = nullptr;
+}
+
+long long stage_in_bytes(const StageGeom &g, long long in_stride, long long in_group_stride)
+{
+    const long long SZ = (long long)dtype_size(g.in_dtype);
+    const long long ntiles = (g.nsamp + g.T - 1) / g.T;
+    const long long last = ((ntiles * g.T + g.max_shift) * SZ + 15) / 16 * 16;
+    return ((long long)(g.ngroups - 1) * in_group_stride + (long long)(g.nchans - 1) * in_stride) *
+               SZ + last;
+}
+
+mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride,
+                         long long in_group_stride, void *out, long long out_stride,
+                         long long out_group_stride, unsigned *d_err, cudaStream_t st,
+                         int *launches)
+{
+    const int SZ = (int)dtype_size(g.in_dtype);
+    if (((uintptr_t)in & 15) != 0) return fail(MDSM_EINVAL, "input must be 16-byte aligned");
+    if ((in_stride * SZ) % 16 != 0)
+        return fail(MDSM_EINVAL, "input row pitch must be a multiple of 16 bytes");
+    if ((in_group_stride * SZ) % 16 != 0)
+        return fail(MDSM_EINVAL, "input group pitch must be a multiple of 16 bytes");
+    void *fn = select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
+    MDSM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)g.smem_bytes));
+    KArgs a;
+    a.in = static_cast<const unsigned char *>(in);
+    a.in_stride = in_stride;
+    a.in_group_stride = in_group_stride;
+    a.out = static_cast<unsigned char *>(out);
+    a.out_stride = out_stride;
+    a.out_group_stride = out_group_stride;
+    a.rel = g.d_rel;
+    a.sminspan = g.d_sminspan;
+    a.nchans = g.nchans;
+    a.ndms = g.ndms;
+    a.nsamp = g.nsamp;
+    a.nblk = g.nblk;
+    a.rowcap = g.rowcap;
+    a.nst = g.nst;
+    a.out_i32 = g.out_i32;
+    a.err = d_err;
+    const long long ntiles = (g.nsamp + g.T - 1) / g.T;
+    if (ntiles > 65535 || g.ngroups > 65535)
+        return fail(MDSM_EINVAL, "block too long for one launch");
+    dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);
+    void *args[] = {&a};
+    MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kNW * 32), args, g.smem_bytes, st));
+    if (launches) *launches += 1;
+    return MDSM_OK;
+}
+
+}  // namespace mdsm

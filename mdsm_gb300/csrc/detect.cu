@@ -1,0 +1,365 @@
+// detect.cu -- single-pulse detection on dedispersed series, on the device.
+//
+// 1. The reference detector (src/mdsm/dedispersion_output.cpp:14-53,135-213): global mean/rms
+//    over the whole block exactly as process_brute forms them (32K-value chunks, double sums,
+//    a float running mean, the last chunk skipped by its loop test), then a median-of-five
+//    filter and the test median - mean >= threshold*rms with DM > 1.  Every operation is an
+//    explicitly rounded IEEE operation so candidates are identical to the host reference's.
+// 2. A boxcar search (src/prototypes/singlepulse.cpp:41-146, restated): per-DM mean/sigma,
+//    boxcar sums of widths 1..2^(nw-1) built by pairwise doubling, SNR per width, the best
+//    width per sample and non-maximum suppression.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <mutex>
+#include <vector>
+
+#include "internal.h"
+
+namespace mdsm {
+
+// ---------------------------------------------------------------------------------------------
+// scratch: one grow-only device buffer per process for detector work arrays
+// ---------------------------------------------------------------------------------------------
+namespace {
+std::mutex g_scratch_mu;
+void *g_scratch = nullptr;
+size_t g_scratch_bytes = 0;
+}  // namespace
+
+static mdsm_status scratch_get(size_t bytes, void **out)
+{
+    std::lock_guard<std::mutex> lk(g_scratch_mu);
+    if (g_scratch_bytes < bytes) {
+        if (g_scratch) cudaFree(g_scratch);
+        g_scratch = nullptr;
+        g_scratch_bytes = 0;
+        MDSM_CUDA_TRY(cudaMalloc(&g_scratch, bytes));
+        g_scratch_bytes = bytes;
+    }
+    *out = g_scratch;
+    return MDSM_OK;
+}
+
+struct DevCand {
+    int32_t dm_idx, sample, width;
+    float snr;
+};
+
+__device__ __forceinline__ float median5(float n1, float n2, float n3, float n4, float n5)
+{
+    // dedispersion_output.cpp:14-53, the same comparison network on values
+    float a = n1, b = n2, c = n3, d = n4, e = n5, t;
+    if (b < a) { t = a; a = b; b = t; }
+    if (d < c) { t = c; c = d; d = t; }
+    if (c < a) { t = b; b = d; d = t; c = a; }
+    a = e;
+    if (b < a) { t = a; a = b; b = t; }
+    if (a < c) { t = b; b = d; d = t; a = c; }
+    return (d < a) ? d : a;
+}
+
+// One thread per 32K chunk: sequential double sums (dedispersion_output.cpp:155-160).
+__global__ void k_ref_chunk_sums(const float *__restrict__ buf, unsigned mod, unsigned nchunks,
+                                 double2 *__restrict__ sums)
+{
+    const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nchunks) return;
+    const float *p = buf + (size_t)i * mod;
+    double t1 = 0.0, t2 = 0.0;
+    for (unsigned j = 0; j < mod; ++j) {
+        const double v = (double)__ldg(p + j);
+        t1 = __dadd_rn(t1, v);
+        t2 = __dadd_rn(t2, __dmul_rn(v, v));
+    }
+    sums[i] = make_double2(t1, t2);
+}
+
+// One thread: dedispersion_output.cpp:161-168.
+__global__ void k_ref_finish(const double2 *__restrict__ sums, unsigned mod, unsigned nchunks,
+                             float *__restrict__ stats)
+{
+    float localmean = 0.0f;
+    double mean2 = 0.0;
+    for (unsigned i = 0; i < nchunks; ++i) {
+        const double2 s = sums[i];
+        localmean = __double2float_rn(__dadd_rn((double)localmean, __ddiv_rn(s.x, (double)mod)));
+        mean2 = __dadd_rn(mean2, __ddiv_rn(s.y, (double)mod));
+    }
+    localmean = __fdiv_rn(localmean, (float)nchunks);
+    const float sq = __fmul_rn(localmean, localmean);
+    const double v = __dadd_rn(__ddiv_rn(mean2, (double)nchunks), -(double)sq);
+    stats[0] = localmean;
+    stats[1] = __double2float_rn(__dsqrt_rn(v));
+}
+
+// dedispersion_output.cpp:176-210 (one device, mean == NULL).
+__global__ void k_ref_detect(const float *__restrict__ buf, int ndms, int nsamp, float lowdm,
+                             float dmstep, float threshold, const float *__restrict__ stats,
+                             DevCand *__restrict__ cands, unsigned long long *__restrict__ count,
+                             long long cap)
+{
+    const int k = blockIdx.y;
+    const float thisdm = __fadd_rn(__fadd_rn(lowdm, 0.0f), __fmul_rn((float)(unsigned)k, dmstep));
+    if (!((double)thisdm > 1.0)) return;
+    const float mean = stats[0], rms = stats[1];
+    const float lim = __fmul_rn(rms, threshold);
+    const float *r = buf + (size_t)k * nsamp;
+    const unsigned nl = (unsigned)nsamp - 4u;
+    for (unsigned l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
+        const float m = median5(__ldg(r + l), __ldg(r + l + 1), __ldg(r + l + 2), __ldg(r + l + 3),
+                                __ldg(r + l + 4));
+        if (__fsub_rn(m, mean) >= lim) {
+            const unsigned long long at = atomicAdd(count, 1ull);
+            if ((long long)at < cap) cands[at] = DevCand{k, (int32_t)l, 1, __fdiv_rn(m, rms)};
+        }
+    }
+}
+
+static void sort_cands(mdsm_candidate *c, long long n)
+{
+    std::sort(c, c + n, [](const mdsm_candidate &a, const mdsm_candidate &b) {
+        return a.dm_idx != b.dm_idx ? a.dm_idx < b.dm_idx : a.sample < b.sample;
+    });
+}
+
+static mdsm_status fetch_cands(DevCand *d_c, unsigned long long *d_count, long long cap,
+                               mdsm_candidate *h, long long *ncand, cudaStream_t st)
+{
+    unsigned long long n = 0;
+    MDSM_CUDA_TRY(cudaMemcpyAsync(&n, d_count, sizeof(n), cudaMemcpyDeviceToHost, st));
+    MDSM_CUDA_TRY(cudaStreamSynchronize(st));
+    *ncand = (long long)n;
+    const long long got = std::min<long long>((long long)n, cap);
+    if (got > 0 && h) {
+        std::vector<DevCand> tmp((size_t)got);
+        MDSM_CUDA_TRY(cudaMemcpy(tmp.data(), d_c, (size_t)got * sizeof(DevCand),
+                                 cudaMemcpyDeviceToHost));
+        for (long long i = 0; i < got; ++i) {
+            h[i].dm_idx = tmp[i].dm_idx;
+            h[i].sample = tmp[i].sample;
+            h[i].width = tmp[i].width;
+            h[i].snr = tmp[i].snr;
+        }
+        sort_cands(h, got);
+    }
+    return MDSM_OK;
+}
+
+mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, float dmstep,
+                       float threshold, mdsm_candidate *h_cands, long long cap,
+                       long long *ncand, float *mean, float *rms, cudaStream_t st)
+{
+    const unsigned long long vals64 = (unsigned long long)ndms * (unsigned long long)nsamp;
+    if (vals64 > 0xFFFFFFFFull / 2)
+        return fail(MDSM_EINVAL, "reference detector counts values in 32 bits");
+    const unsigned vals = (unsigned)vals64;
+    const unsigned mod = vals < 32768u ? vals : 32768u;
+    // iterations of dedispersion_output.cpp:154-165: stops once (iters+1)*mod >= vals
+    unsigned nchunks = 1;
+    while ((unsigned long long)(nchunks + 1) * mod < vals) ++nchunks;
+    if (cap < 0) cap = 0;
+    const size_t off_cnt = 0, off_stats = 16, off_sums = 64;
+    const size_t off_c = off_sums + ((size_t)nchunks * sizeof(double2) + 255) / 256 * 256;
+    const size_t bytes = off_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand);
+    void *sc = nullptr;
+    MDSM_TRY(scratch_get(bytes, &sc));
+    char *base = static_cast<char *>(sc);
+    auto *d_count = reinterpret_cast<unsigned long long *>(base + off_cnt);
+    auto *d_stats = reinterpret_cast<float *>(base + off_stats);
+    auto *d_sums = reinterpret_cast<double2 *>(base + off_sums);
+    auto *d_c = reinterpret_cast<DevCand *>(base + off_c);
+    MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
+    k_ref_chunk_sums<<<(nchunks + 127) / 128, 128, 0, st>>>(d_series, mod, nchunks, d_sums);
+    k_ref_finish<<<1, 1, 0, st>>>(d_sums, mod, nchunks, d_stats);
+    dim3 grid((unsigned)std::min<long long>((nsamp + 255) / 256, 64), (unsigned)ndms);
+    k_ref_detect<<<grid, 256, 0, st>>>(d_series, ndms, nsamp, lowdm, dmstep, threshold, d_stats,
+                                       d_c, d_count, cap);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    float hs[2];
+    MDSM_CUDA_TRY(cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    MDSM_TRY(fetch_cands(d_c, d_count, cap, h_cands, ncand, st));
+    if (mean) *mean = hs[0];
+    if (rms) *rms = hs[1];
+    return MDSM_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// boxcar search
+// ---------------------------------------------------------------------------------------------
+
+template <typename T>
+__device__ __forceinline__ double ld_d(const T *p, long long i)
+{
+    return (double)__ldg(p + i);
+}
+
+// Per (DM, 1024-sample chunk) sums, left to right.
+template <typename T>
+__global__ void k_series_chunk_sums(const T *__restrict__ y, long long n, int nch,
+                                    double2 *__restrict__ part)
+{
+    const int d = blockIdx.y;
+    const int ch = blockIdx.x * blockDim.x + threadIdx.x;
+    if (ch >= nch) return;
+    const T *r = y + (size_t)d * n;
+    const long long c0 = (long long)ch * 1024, c1 = min(c0 + 1024, n);
+    double p1 = 0.0, p2 = 0.0;
+    for (long long i = c0; i < c1; ++i) {
+        const double v = ld_d(r, i);
+        p1 = __dadd_rn(p1, v);
+        p2 = __dadd_rn(p2, __dmul_rn(v, v));
+    }
+    part[(size_t)d * nch + ch] = make_double2(p1, p2);
+}
+
+__global__ void k_series_finish(const double2 *__restrict__ part, int ndms, int nch, long long n,
+                                double2 *__restrict__ musig)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= ndms) return;
+    double s1 = 0.0, s2 = 0.0;
+    for (int i = 0; i < nch; ++i) {
+        const double2 p = part[(size_t)d * nch + i];
+        s1 = __dadd_rn(s1, p.x);
+        s2 = __dadd_rn(s2, p.y);
+    }
+    const double m = __ddiv_rn(s1, (double)n);
+    const double var = __dadd_rn(__ddiv_rn(s2, (double)n), -__dmul_rn(m, m));
+    musig[d] = make_double2(m, var > 0.0 ? __dsqrt_rn(var) : 0.0);
+}
+
+constexpr int kBoxTile = 2048;   // output samples per CTA
+constexpr int kBoxHaloL = 128;   // NMS radius for the widest boxcar (256/2)
+constexpr int kBoxThreads = 256;
+
+// One CTA per (DM, tile).  Region [t0 - HL, t0 + TILE + HL + wmax - 1) is staged as doubles.
+template <typename T>
+__global__ void __launch_bounds__(kBoxThreads)
+    k_boxcar(const T *__restrict__ y, long long n, int nw, double threshold,
+             const double2 *__restrict__ musig, DevCand *__restrict__ cands,
+             unsigned long long *__restrict__ count, long long cap)
+{
+    extern __shared__ __align__(16) unsigned char sm[];
+    const int wmax = 1 << (nw - 1);
+    const int hl = max(wmax / 2, 1);
+    const int span = kBoxTile + 2 * hl + wmax;  // staged samples
+    const int nbest = kBoxTile + 2 * hl;        // positions with a best value
+    double *B = reinterpret_cast<double *>(sm);
+    double *best = B + span;
+    int *bw = reinterpret_cast<int *>(best + nbest);
+
+    const int d = blockIdx.y;
+    const double mu = musig[d].x, sig = musig[d].y;
+    if (!(sig > 0.0)) return;
+    const long long t0 = (long long)blockIdx.x * kBoxTile;
+    const long long r0 = t0 - hl;  // series index of B[0] and best[0]
+    const T *r = y + (size_t)d * n;
+    for (int i = threadIdx.x; i < span; i += blockDim.x) {
+        const long long t = r0 + i;
+        B[i] = (t >= 0 && t < n) ? ld_d(r, t) : 0.0;
+    }
+    for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
+        best[i] = -INFINITY;
+        bw[i] = 0;
+    }
+    __syncthreads();
+    constexpr int PER = (kBoxTile + 2 * 128 + 256 + kBoxThreads - 1) / kBoxThreads;
+    for (int l = 0; l < nw; ++l) {
+        const int w = 1 << l;
+        if (l > 0) {
+            const int h = w >> 1;
+            double nv[PER];
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x + q * kBoxThreads;
+                nv[q] = (i + h < span) ? __dadd_rn(B[i], B[i + h]) : 0.0;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < PER; ++q) {
+                const int i = threadIdx.x + q * kBoxThreads;
+                if (i < span) B[i] = nv[q];
+            }
+            __syncthreads();
+        }
+        const double wm = __dmul_rn((double)w, mu);
+        const double den = __dmul_rn(sig, __dsqrt_rn((double)w));
+        for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
+            const long long t = r0 + i;
+            if (t < 0 || t + w > n) continue;
+            const double s = __ddiv_rn(__dadd_rn(B[i], -wm), den);
+            if (s > best[i]) {
+                best[i] = s;
+                bw[i] = w;
+            }
+        }
+        __syncthreads();
+    }
+    for (int q = threadIdx.x; q < kBoxTile; q += blockDim.x) {
+        const long long t = t0 + q;
+        if (t >= n) break;
+        const int i = q + hl;
+        const double b = best[i];
+        if (!(b >= threshold)) continue;
+        const int h = max(bw[i] / 2, 1);
+        bool keep = true;
+        for (int u = 1; u <= h && keep; ++u)
+            if (t - u >= 0 && !(best[i - u] < b)) keep = false;
+        for (int u = 1; u <= h && keep; ++u)
+            if (t + u <= n - 1 && !(best[i + u] <= b)) keep = false;
+        if (!keep) continue;
+        const unsigned long long at = atomicAdd(count, 1ull);
+        if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw[i], __double2float_rn(b)};
+    }
+}
+
+mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
+                          double threshold, mdsm_candidate *h_cands, long long cap,
+                          long long *ncand, cudaStream_t st)
+{
+    if (dtype != MDSM_OUT_F32 && dtype != MDSM_OUT_I32)
+        return fail(MDSM_EINVAL, "boxcar detector: series must be float32 or int32");
+    if (nwidths > 9) return fail(MDSM_EINVAL, "boxcar detector: widths up to 256");
+    if (cap < 0) cap = 0;
+    const int nch = (nsamp + 1023) / 1024;
+    const size_t off_cnt = 0, off_part = 256;
+    const size_t off_ms = off_part + ((size_t)ndms * nch * sizeof(double2) + 255) / 256 * 256;
+    const size_t off_c = off_ms + ((size_t)ndms * sizeof(double2) + 255) / 256 * 256;
+    const size_t bytes = off_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand);
+    void *sc = nullptr;
+    MDSM_TRY(scratch_get(bytes, &sc));
+    char *base = static_cast<char *>(sc);
+    auto *d_count = reinterpret_cast<unsigned long long *>(base + off_cnt);
+    auto *d_part = reinterpret_cast<double2 *>(base + off_part);
+    auto *d_ms = reinterpret_cast<double2 *>(base + off_ms);
+    auto *d_c = reinterpret_cast<DevCand *>(base + off_c);
+    MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
+    dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
+    const int wmax = 1 << (nwidths - 1);
+    const int hl = std::max(wmax / 2, 1);
+    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 12;
+    dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
+    if (dtype == MDSM_OUT_F32) {
+        const float *y = static_cast<const float *>(d_series);
+        k_series_chunk_sums<float><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
+        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
+        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<float>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_boxcar<float><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
+                                                       d_count, cap);
+    } else {
+        const int32_t *y = static_cast<const int32_t *>(d_series);
+        k_series_chunk_sums<int32_t><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
+        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
+        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<int32_t>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_boxcar<int32_t><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
+                                                         d_count, cap);
+    }
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return fetch_cands(d_c, d_count, cap, h_cands, ncand, st);
+}
+
+}  // namespace mdsm

@@ -1,0 +1,137 @@
+// internal.h -- shared declarations of the mdsm_gb300 library (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "mdsm_gb300.h"
+
+namespace mdsm {
+
+// ----------------------------------------------------------------------------------------
+// errors
+// ----------------------------------------------------------------------------------------
+void set_error(const std::string &msg);
+mdsm_status fail(mdsm_status st, const std::string &msg);
+mdsm_status cuda_fail(cudaError_t e, const char *what);
+
+#define MDSM_CUDA_TRY(x)                                                  \
+    do {                                                                  \
+        cudaError_t e_ = (x);                                             \
+        if (e_ != cudaSuccess) return ::mdsm::cuda_fail(e_, #x);          \
+    } while (0)
+
+#define MDSM_TRY(x)                                                       \
+    do {                                                                  \
+        mdsm_status s_ = (x);                                             \
+        if (s_ != MDSM_OK) return s_;                                     \
+    } while (0)
+
+// device-side error word bits
+enum : unsigned {
+    ERR_WAIT_TIMEOUT = 1u,   // a bounded mbarrier wait ran out
+    ERR_CAND_OVERFLOW = 2u,  // candidate buffer full (count still exact)
+};
+
+size_t dtype_size(int dtype);
+
+// ----------------------------------------------------------------------------------------
+// one launch of the generic shift-and-sum kernel: out[g][d][t] = sum_c in[g][c][t + S[g][d][c]]
+// ----------------------------------------------------------------------------------------
+struct StageGeom {
+    int nchans = 0;   // channels summed per group
+    int ndms = 0;     // output rows per group
+    int ngroups = 1;
+    int nsamp = 0;    // output samples per row
+    long long in_stride = 0, in_group_stride = 0;    // elements
+    long long out_stride = 0, out_group_stride = 0;  // elements
+    int in_dtype = MDSM_U8;
+    int acc_int = 1;      // 1: int32 accumulation, 0: float
+    int out_i32 = 0;      // output element type
+    int Db = 32, T = 256, R = 8, DPW = 4;
+    int cc = 16, nst = 3; // channels per pipeline stage, stages
+    int rowcap = 0;       // elements per staged row
+    int nblk = 0;         // DM blocks per group
+    int max_span = 0;     // max over blocks/channels of smax - smin
+    int max_shift = 0;    // max shift in the table
+    // host tables
+    std::vector<int32_t> rel;     // [ngroups][nblk][nchans][Db]  shift - smin
+    std::vector<int32_t> sminspan;// [ngroups][nblk][nchans][2]   (smin, span)
+    // device copies
+    int32_t *d_rel = nullptr;
+    int32_t *d_sminspan = nullptr;
+    size_t smem_bytes = 0;
+    int kernel = 1;       // 1 generic, 2 packed u8
+};
+
+// Build the blocked tables of a stage from a full shift table S[g][d][c] (row-major).  Picks
+// the tile shape: Db starts at 8*DPW (DPW as set on entry) and shrinks until the staged rows
+// fit in shared memory.
+mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S);
+mdsm_status upload_stage(StageGeom &g);
+void free_stage(StageGeom &g);
+// Bytes of input (from the group base) the kernel may read for in_stride, with tile overrun.
+long long stage_in_bytes(const StageGeom &g, long long in_stride, long long in_group_stride);
+// Launch the stage kernel.  Returns number of kernels launched via *launches.
+mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride,
+                         long long in_group_stride, void *out, long long out_stride,
+                         long long out_group_stride, unsigned *d_err, cudaStream_t st,
+                         int *launches);
+
+// ----------------------------------------------------------------------------------------
+// plans
+// ----------------------------------------------------------------------------------------
+struct Plan {
+    int kind = 0;   // 1 brute, 2 subband
+    int nchans = 0, ndms = 0, nsamp = 0, maxshift = 0;
+    float fch1 = 0, foff = 0, tsamp = 0;
+    int in_dtype = MDSM_U8, out_dtype = MDSM_OUT_F32, acc = MDSM_ACC_AUTO;
+    std::vector<float> dmshifts;     // float[nchans]
+    std::vector<float> dm_values;    // float[ndms]
+    std::vector<int32_t> S;          // brute: [ndms][nchans]
+    std::vector<int32_t> S1, S2;     // subband first pass stage tables (reporting)
+    std::vector<StageGeom> stages;   // brute: 1; subband: 2 per pass
+    // subband intermediate
+    long long n1 = 0;                // stage-1 output samples per row
+    void *d_work = nullptr;
+    size_t work_bytes = 0;
+    std::vector<long long> pass_row0;   // first output row of each pass
+    // host-path buffers
+    void *d_in = nullptr, *d_out = nullptr;
+    size_t d_in_bytes = 0, d_out_bytes = 0;
+    unsigned *d_err = nullptr;
+    int last_launches = 0;
+    long long in_stride = 0;         // device pitch for the host path
+};
+
+mdsm_status plan_in_requirements(const Plan &p, long long in_stride, long long *in_bytes);
+mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size_t in_bytes,
+                            void *d_out, long long out_stride, cudaStream_t st);
+mdsm_status check_err_word(unsigned *d_err, cudaStream_t st);
+
+// host shift formulas (the reference's arithmetic, evaluated on the host)
+float dmdelay_ref(float f1, float f2);
+void dmshifts_ref(int nchans, float fch1, float foff, float *out);
+int32_t shift_of(float dms, double delay64, float lowdm, float dmstep, int idx, float tsamp,
+                 int mode);
+
+// ----------------------------------------------------------------------------------------
+// detection / rfi launchers (detect.cu, rfi.cu)
+// ----------------------------------------------------------------------------------------
+mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, float dmstep,
+                       float threshold, mdsm_candidate *h_cands, long long cap,
+                       long long *ncand, float *mean, float *rms, cudaStream_t st);
+mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
+                          double threshold, mdsm_candidate *h_cands, long long cap,
+                          long long *ncand, cudaStream_t st);
+mdsm_status rfi_clip(void *d_x, int dtype, int nchans, long long stride, long long len,
+                     double k_chan, double k_spec, cudaStream_t st);
+
+}  // namespace mdsm
+
+struct mdsm_plan_s {
+    mdsm::Plan p;
+};

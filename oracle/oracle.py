@@ -1,0 +1,252 @@
+"""ctypes wrapper of the CPU oracle (oracle/mdsm_oracle.c) and of the reference builds.
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline / reference arm.  The product package never imports this module.
+"""
+import ctypes
+import os
+import platform
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "_build", platform.machine(), "libmdsm_oracle.so")
+HARNESS_SO = os.path.join(HERE, "_build", platform.machine(), "libref_gpu_harness.so")
+REF_HOST_SO = os.path.join(HERE, "_ref", "libref_host.so")
+REF_CUBIN = os.path.join(HERE, "_ref", "ref_kernels.cubin")
+REF_TREE = "/root/reference/src"
+
+SHIFT = {"l1": 0, "l1_muladd": 1, "opt": 2, "opt_muladd": 3, "fp64_trunc": 4, "fp64_round": 5}
+
+
+def build(reference=True):
+    """Build the oracle (always) and, when the reference tree is present here, its builds."""
+    subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
+    if reference and os.path.isdir(REF_TREE):
+        subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_TREE], check=True)
+    cuda_lib = any(os.path.exists(os.path.join(d, "libcuda.so")) for d in
+                   ("/usr/local/cuda/lib64/stubs", "/usr/lib/x86_64-linux-gnu",
+                    "/usr/lib/aarch64-linux-gnu", "/usr/local/cuda/lib64"))
+    if cuda_lib:
+        subprocess.run(["make", "-s", "-C", HERE, "harness"], check=True)
+
+
+class Seg(ctypes.Structure):
+    _fields_ = [("lowdm", ctypes.c_float), ("dmstep", ctypes.c_float), ("ndms", ctypes.c_int)]
+
+
+_O = None
+
+
+def lib():
+    global _O
+    if _O is None:
+        if not os.path.exists(ORACLE_SO):
+            build(reference=False)
+        _O = ctypes.CDLL(ORACLE_SO)
+        _O.orc_dmdelay.restype = ctypes.c_float
+        _O.orc_dmdelay.argtypes = [ctypes.c_float, ctypes.c_float]
+        _O.orc_median_of_five.restype = ctypes.c_float
+        _O.orc_median_of_five.argtypes = [ctypes.c_float] * 5
+        _O.orc_ref_maxshift.restype = ctypes.c_uint
+        _O.orc_ref_maxshift.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_float,
+                                        ctypes.c_float, ctypes.c_int, ctypes.c_float]
+        _O.orc_subband_tempval.restype = ctypes.c_int
+        _O.orc_subband_tempval.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_float, ctypes.c_float]
+        _O.orc_ref_detect.restype = ctypes.c_long
+        _O.orc_boxcar_detect.restype = ctypes.c_long
+        _O.orc_unpack.restype = ctypes.c_long
+    return _O
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def dmshifts(nchans, fch1, foff):
+    out = np.empty(nchans, np.float32)
+    lib().orc_dmshifts(nchans, ctypes.c_float(fch1), ctypes.c_float(foff), _p(out))
+    return out
+
+
+def shift_table(nchans, fch1, foff, tsamp, segments, mode="l1", K=4148.741601):
+    dms = dmshifts(nchans, fch1, foff)
+    segs = (Seg * len(segments))(*[Seg(a, b, n) for a, b, n in segments])
+    ndms = sum(n for _, _, n in segments)
+    out = np.empty((ndms, nchans), np.int32)
+    lib().orc_shift_table(_p(dms), nchans, ctypes.c_double(fch1), ctypes.c_double(foff),
+                          ctypes.c_double(K), segs, len(segments), ctypes.c_float(tsamp),
+                          SHIFT[mode], _p(out))
+    return out
+
+
+def ref_maxshift(nchans, fch1, foff, lowdm, dmstep, tdms, tsamp):
+    dms = dmshifts(nchans, fch1, foff)
+    return lib().orc_ref_maxshift(_p(dms), nchans, lowdm, dmstep, tdms, tsamp)
+
+
+def dedisperse(x, S, nsamp, out="auto"):
+    """x [nchans][stride] (f32/u8/u16/i16), S [ndms][nchans] -> [ndms][nsamp]."""
+    S = np.ascontiguousarray(S, np.int32)
+    ndms, nchans = S.shape
+    stride = x.shape[1]
+    x = np.ascontiguousarray(x)
+    if out == "f64":
+        y = np.empty((ndms, nsamp), np.float64)
+        lib().orc_dedisperse_f64(_p(x), nchans, ctypes.c_long(stride), nsamp, _p(S), ndms, _p(y))
+        return y
+    if x.dtype == np.float32:
+        y = np.empty((ndms, nsamp), np.float32)
+        lib().orc_dedisperse_f32(_p(x), nchans, ctypes.c_long(stride), nsamp, _p(S), ndms, _p(y))
+        return y
+    fn = {np.dtype(np.uint8): lib().orc_dedisperse_u8_i32,
+          np.dtype(np.uint16): lib().orc_dedisperse_u16_i32,
+          np.dtype(np.int16): lib().orc_dedisperse_i16_i32}[x.dtype]
+    y = np.empty((ndms, nsamp), np.int32)
+    fn(_p(x), nchans, ctypes.c_long(stride), nsamp, _p(S), ndms, _p(y))
+    return y
+
+
+def subband_tables(nchans, fch1, foff, tsamp, nsubs, lowdm, sub_dmstep, ncalls, dmstep, calldms,
+                   use_fma=True):
+    dms = dmshifts(nchans, fch1, foff)
+    S1 = np.empty((ncalls, nchans), np.int32)
+    S2 = np.empty((ncalls * calldms, nsubs), np.int32)
+    lib().orc_subband_shifts(_p(dms), nchans, nsubs, ctypes.c_float(lowdm),
+                             ctypes.c_float(sub_dmstep), ncalls, ctypes.c_float(dmstep), calldms,
+                             ctypes.c_float(tsamp), int(use_fma), _p(S1), _p(S2))
+    return S1, S2
+
+
+def subband_dedisperse(x, S1, S2, nsubs, nsamp, nsamp1, calldms):
+    """Reference two-stage order: stage 1 to z [ncalls][nsubs][nsamp1], stage 2 to y."""
+    x = np.ascontiguousarray(x, np.float32)
+    ncalls, nchans = S1.shape
+    z = np.empty((ncalls, nsubs, nsamp1), np.float32)
+    lib().orc_subband_stage1_f32(_p(x), nchans, ctypes.c_long(x.shape[1]), nsubs, nsamp1,
+                                 _p(np.ascontiguousarray(S1)), ncalls, _p(z))
+    y = np.empty((ncalls * calldms, nsamp), np.float32)
+    lib().orc_subband_stage2_f32(_p(z), nsubs, nsamp1, nsamp, _p(np.ascontiguousarray(S2)),
+                                 ncalls, calldms, _p(y))
+    return z, y
+
+
+def median_of_five(a, b, c, d, e):
+    return lib().orc_median_of_five(a, b, c, d, e)
+
+
+def ref_stats(buf):
+    buf = np.ascontiguousarray(buf, np.float32)
+    m, r = ctypes.c_float(), ctypes.c_float()
+    lib().orc_ref_stats(_p(buf), ctypes.c_uint(buf.size), ctypes.byref(m), ctypes.byref(r))
+    return m.value, r.value
+
+
+def ref_detect(buf, lowdm, dmstep, threshold, cap=1 << 22):
+    buf = np.ascontiguousarray(buf, np.float32)
+    ndms, nsamp = buf.shape
+    mean, rms = ref_stats(buf)
+    dm = np.empty(cap, np.int32)
+    sa = np.empty(cap, np.int32)
+    sn = np.empty(cap, np.float32)
+    n = lib().orc_ref_detect(_p(buf), ndms, nsamp, ctypes.c_float(lowdm), ctypes.c_float(dmstep),
+                             ctypes.c_float(threshold), ctypes.c_float(mean), ctypes.c_float(rms),
+                             _p(dm), _p(sa), _p(sn), ctypes.c_long(cap))
+    k = min(n, cap)
+    return (dm[:k].copy(), sa[:k].copy(), sn[:k].copy()), mean, rms
+
+
+KIND = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1, np.dtype(np.int16): 2,
+        np.dtype(np.float32): 3}
+
+
+def rfi_clip(x, length, k_chan=4.0, k_spec=4.0):
+    """In place on a channel-major array [nchans][stride]."""
+    assert x.flags.c_contiguous
+    lib().orc_rfi_clip(_p(x), KIND[x.dtype], x.shape[0], ctypes.c_long(x.shape[1]),
+                       ctypes.c_long(length), ctypes.c_double(k_chan), ctypes.c_double(k_spec))
+    return x
+
+
+def boxcar_detect(y, nw=9, threshold=6.0, cap=1 << 22):
+    yd = np.ascontiguousarray(y, np.float64)
+    ndms, n = yd.shape
+    dm = np.empty(cap, np.int32)
+    sa = np.empty(cap, np.int32)
+    wd = np.empty(cap, np.int32)
+    sn = np.empty(cap, np.float32)
+    cnt = lib().orc_boxcar_detect(_p(yd), ndms, ctypes.c_long(n), nw, ctypes.c_double(threshold),
+                                  _p(dm), _p(sa), _p(wd), _p(sn), ctypes.c_long(cap))
+    k = min(cnt, cap)
+    return dm[:k].copy(), sa[:k].copy(), wd[:k].copy(), sn[:k].copy()
+
+
+def unpack(raw, nbits):
+    raw = np.ascontiguousarray(raw, np.uint8)
+    out = np.empty(raw.size * 8, np.float32)
+    n = lib().orc_unpack(_p(raw), ctypes.c_long(raw.size), nbits, _p(out))
+    return out[:n].copy()
+
+
+def detrend_normalise(y, length=1024):
+    y = np.array(y, np.float32, copy=True)
+    lib().orc_detrend_normalise(_p(y), ctypes.c_long(y.size), length)
+    return y
+
+
+# ------------------------------------------------------------------------------------------
+# the reference's own code (oracle/_ref), where it was built
+# ------------------------------------------------------------------------------------------
+
+def ref_host_available():
+    return os.path.exists(REF_HOST_SO)
+
+
+def ref_host():
+    h = ctypes.CDLL(REF_HOST_SO)
+    h.ref_median_of_five.restype = ctypes.c_float
+    h.ref_median_of_five.argtypes = [ctypes.c_float] * 5
+    h.ref_read_block.restype = ctypes.c_long
+    return h
+
+
+class RefGPU:
+    """The reference kernels from oracle/_ref/ref_kernels.cubin, launched on device 0."""
+
+    def __init__(self, cubin=REF_CUBIN):
+        self.h = ctypes.CDLL(HARNESS_SO)
+        self.h.rg_error.restype = ctypes.c_char_p
+        rc = self.h.rg_init(cubin.encode())
+        if rc:
+            raise RuntimeError("rg_init: %d %s" % (rc, self.h.rg_error().decode()))
+
+    def brute(self, kind, x, nsamp, maxshift, lowdm, dmstep, tsamp, tdms, dms):
+        x = np.ascontiguousarray(x, np.float32)
+        nchans = x.shape[0]
+        assert x.shape[1] == nsamp + maxshift
+        out = np.zeros((tdms, nsamp), np.float32)
+        ms = ctypes.c_float()
+        rc = self.h.rg_brute(kind, _p(x), nsamp, nchans, maxshift, ctypes.c_float(lowdm),
+                             ctypes.c_float(dmstep), ctypes.c_float(tsamp), tdms,
+                             _p(np.ascontiguousarray(dms, np.float32)), _p(out), ctypes.byref(ms))
+        if rc:
+            raise RuntimeError("rg_brute: %d %s" % (rc, self.h.rg_error().decode()))
+        return out, ms.value
+
+    def subband(self, x, nsamp, maxshift, nsubs, tempval, lowdm, sub_dmstep, ncalls, dmstep,
+                calldms, tsamp, dms):
+        x = np.ascontiguousarray(x, np.float32)
+        nchans = x.shape[0]
+        z = np.zeros((ncalls, nsubs, nsamp + tempval), np.float32)
+        out = np.zeros((ncalls * calldms, nsamp), np.float32)
+        ms = ctypes.c_float()
+        rc = self.h.rg_subband(_p(x), nsamp, nchans, maxshift, nsubs, tempval,
+                               ctypes.c_float(lowdm), ctypes.c_float(sub_dmstep), ncalls,
+                               ctypes.c_float(dmstep), calldms, ctypes.c_float(tsamp),
+                               _p(np.ascontiguousarray(dms, np.float32)), _p(z), _p(out),
+                               ctypes.byref(ms))
+        if rc:
+            raise RuntimeError("rg_subband: %d %s" % (rc, self.h.rg_error().decode()))
+        return z, out, ms.value

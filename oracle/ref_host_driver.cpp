@@ -1,0 +1,53 @@
+/*
+ * ref_host_driver.cpp -- TEST INFRASTRUCTURE ONLY.  C entry points over the reference's own
+ * host code (src/mdsm/dedispersion_output.cpp and src/mdsm/file_handler.cpp), compiled from
+ * the reference tree by oracle/Makefile into oracle/_ref/.  Used in this container to pin the
+ * oracle (tests/golden/make_golden.py); never shipped, never part of the product.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include "survey.h"
+#include "file_handler.h"
+
+/* dedispersion_output.cpp:135-136 (not declared in any reference header) */
+void process_brute(float *buffer, FILE *output, SURVEY *survey, int read_nsamp, size_t size,
+                   double timestamp, double blockRate, time_t start_time, float *mean, float *rms);
+float medianOfFive(float n1, float n2, float n3, float n4, float n5);
+
+extern "C" int ref_process_brute(float *buf, int tdms, int nsamp, float lowdm, float dmstep,
+                                 float threshold, const char *outpath)
+{
+    SURVEY s;
+    memset(&s, 0, sizeof(s));
+    s.tdms = (unsigned)tdms;
+    s.nsamp = (unsigned)nsamp;
+    s.lowdm = lowdm;
+    s.dmstep = dmstep;
+    s.detection_threshold = threshold;
+    s.num_threads = 1;
+    s.useBruteForce = 1;
+    FILE *fp = fopen(outpath, "w");
+    if (!fp) return -1;
+    process_brute(buf, fp, &s, nsamp, (size_t)tdms * (size_t)nsamp, 0.0, 1.0, time(NULL), NULL,
+                  NULL);
+    fclose(fp);
+    return 0;
+}
+
+extern "C" float ref_median_of_five(float a, float b, float c, float d, float e)
+{
+    return medianOfFive(a, b, c, d, e);
+}
+
+/* file_handler.cpp:193: read_block over a file holding the raw bytes. */
+extern "C" long ref_read_block(const char *path, int nbits, float *out, unsigned long nread)
+{
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return -1;
+    long n = (long)read_block(fp, nbits, out, nread);
+    fclose(fp);
+    return n;
+}

@@ -1,0 +1,120 @@
+"""The C-ABI library loads and exports every symbol include/*.h declares; the SURVEY struct
+and the other ABI structs have the C layout (checked against the C compiler's offsetof)."""
+import ctypes
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+INC = os.path.join(ROOT, "include")
+
+
+def declared_functions():
+    names = set()
+    for fn in os.listdir(INC):
+        if not fn.endswith(".h"):
+            continue
+        src = open(os.path.join(INC, fn)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        if "extern \"C\"" not in src and fn != "mdsm_gb300.h":
+            continue
+        for m in re.finditer(r"\b(mdsm_[A-Za-z0-9_]+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_functions()
+    assert len(names) > 20
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    from mdsm_gb300 import _lib
+    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+
+
+def test_library_has_no_oracle_dependency():
+    """The product library links no oracle code."""
+    from mdsm_gb300 import _lib
+    out = subprocess.run(["nm", "-D", "--defined-only", _lib.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    assert "orc_" not in out
+    ldd = subprocess.run(["ldd", _lib.LIB_PATH], capture_output=True, text=True).stdout
+    assert "oracle" not in ldd
+
+
+C_LAYOUT = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "mdsm_gb300.h"
+#define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f))
+int main(void) {
+  printf("SURVEY %zu\n", sizeof(SURVEY));
+  P(SURVEY, nsamp); P(SURVEY, tsamp); P(SURVEY, useBruteForce); P(SURVEY, useL1Cache);
+  P(SURVEY, lowdm); P(SURVEY, pass_parameters); P(SURVEY, num_passes); P(SURVEY, timestamp);
+  P(SURVEY, noiseMean); P(SURVEY, samplesPerChunk); P(SURVEY, fp); P(SURVEY, fileprefix);
+  P(SURVEY, basedir); P(SURVEY, secs_per_file); P(SURVEY, use_pc_time);
+  P(SURVEY, detection_threshold); P(SURVEY, num_threads); P(SURVEY, gpu_ids); P(SURVEY, num_gpus);
+  printf("SUBBAND_PASSES %zu\n", sizeof(SUBBAND_PASSES));
+  printf("mdsm_brute_desc %zu\n", sizeof(mdsm_brute_desc));
+  P(mdsm_brute_desc, segs); P(mdsm_brute_desc, K); P(mdsm_brute_desc, kernel);
+  printf("mdsm_subband_desc %zu\n", sizeof(mdsm_subband_desc));
+  P(mdsm_subband_desc, passes); P(mdsm_subband_desc, acc);
+  printf("mdsm_plan_info %zu\n", sizeof(mdsm_plan_info));
+  P(mdsm_plan_info, in_stride); P(mdsm_plan_info, work_bytes);
+  printf("mdsm_candidate %zu\n", sizeof(mdsm_candidate));
+  return 0;
+}
+"""
+
+
+def test_struct_layouts_match_c():
+    from mdsm_gb300 import _lib
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "l.c")
+        exe = os.path.join(d, "l")
+        open(src, "w").write(C_LAYOUT)
+        subprocess.run(["gcc", "-I", INC, "-o", exe, src], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    types = {"SURVEY": _lib.SURVEY, "SUBBAND_PASSES": _lib.SUBBAND_PASSES,
+             "mdsm_brute_desc": _lib.BruteDesc, "mdsm_subband_desc": _lib.SubbandDesc,
+             "mdsm_plan_info": _lib.PlanInfo, "mdsm_candidate": _lib.Candidate}
+    for line in out.splitlines():
+        key, val = line.split()
+        val = int(val)
+        if "." in key:
+            t, f = key.split(".")
+            assert getattr(types[t], f).offset == val, key
+        else:
+            assert ctypes.sizeof(types[key]) == val, key
+
+
+def test_cpp_compat_header_compiles_reference_call_sequence():
+    """A caller written like src/MDSM.cpp:132-169 compiles and links against the library."""
+    from mdsm_gb300 import _lib
+    caller = r"""
+#include "dedispersion_manager.h"
+int main(int argc, char **argv) {
+  SURVEY *survey = processSurveyParameters(argc > 1 ? argv[1] : "obs.xml");
+  if (!survey) return 2;
+  float *input_buffer = initialiseMDSM(survey);
+  if (!input_buffer) return 3;
+  unsigned x;
+  next_chunk(survey->nsamp, x, 0.0, survey->tsamp);
+  start_processing(survey->nsamp);
+  next_chunk(0, x);
+  start_processing(0);
+  tearDownMDSM();
+  return 0;
+}
+"""
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "caller.cpp")
+        open(src, "w").write(caller)
+        libdir = os.path.dirname(_lib.LIB_PATH)
+        r = subprocess.run(["g++", "-I", INC, "-o", os.path.join(d, "caller"), src,
+                            "-L" + libdir, "-lmdsm_gb300", "-Wl,-rpath," + libdir],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr

@@ -1,0 +1,109 @@
+"""Brute-force dedispersion on the GPU through the C ABI, against the oracle.
+
+Float input: bit-identical to the oracle's sequential float sum (the reference kernels' order).
+Integer input: exact INT32 sums, equal to the oracle's integer sums.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _run(plan, x, torch):
+    d_in = plan.alloc_input()
+    flat = x.ravel()
+    d_in[: flat.size].copy_(torch.from_numpy(flat))
+    d_out = plan.alloc_output()
+    plan.dedisperse_device(d_in, d_out)
+    torch.cuda.synchronize()
+    return d_out.cpu().numpy()
+
+
+def _input(plan, dtype, rng):
+    nchans, stride = plan.input_shape()
+    if dtype == "f32":
+        return rng.standard_normal((nchans, stride), dtype=np.float32)
+    if dtype == "u8":
+        return rng.integers(0, 256, (nchans, stride), dtype=np.uint8)
+    if dtype == "u16":
+        return rng.integers(0, 65536, (nchans, stride), dtype=np.uint16)
+    return rng.integers(-32768, 32768, (nchans, stride), dtype=np.int16)
+
+
+CASES = [
+    # nchans, nsamp, segments, dtype, mode
+    (64, 3000, [(0.0, 1.5, 40)], "f32", "l1"),
+    (256, 4096, [(0.0, 0.2, 500)], "f32", "l1"),
+    (100, 1000, [(3.0, 0.7, 33)], "u8", "opt"),
+    (48, 777, [(0.0, 2.0, 17), (34.0, 4.0, 9)], "u16", "l1"),
+    (48, 300, [(0.0, 3.0, 70)], "i16", "l1_muladd"),
+    (16, 5, [(0.0, 1.0, 1)], "f32", "fp64_trunc"),
+    (1, 257, [(0.0, 1.0, 8)], "u8", "l1"),
+    (513, 1025, [(0.0, 0.5, 65)], "u8", "fp64_round"),
+]
+
+
+@pytest.mark.parametrize("nchans,nsamp,segs,dtype,mode", CASES)
+def test_brute_matches_oracle(lib, orc, cuda, nchans, nsamp, segs, dtype, mode):
+    import mdsm_gb300 as m
+    torch = cuda
+    out = "f32" if dtype == "f32" else "i32"
+    plan = m.BrutePlan(nchans, 1500.0, -300.0 / max(nchans, 1) if nchans > 1 else -1.0, 64e-6,
+                       nsamp, segs, shift_mode=mode, in_dtype=dtype, out_dtype=out)
+    rng = np.random.default_rng(nchans * 7 + nsamp)
+    x = _input(plan, dtype, rng)
+    got = _run(plan, x, torch)
+    S = plan.shift_table()
+    want = orc.dedisperse(x, S, nsamp)
+    assert got.dtype == want.dtype
+    assert np.array_equal(got, want), "%d mismatches" % int((got != want).sum())
+    assert plan.last_launches == 1
+
+
+def test_known_answer_channel_index(lib, orc, cuda):
+    """x[c][t] = c gives sum_c c for every DM and sample, for any shift table
+    (src/prototypes/brute_dedisp_imp_tex.cu:112-114,168-175)."""
+    import mdsm_gb300 as m
+    torch = cuda
+    nchans, nsamp = 300, 2048
+    plan = m.BrutePlan(nchans, 1400.0, -0.5, 1e-4, nsamp, [(0.0, 5.0, 96)], in_dtype="f32")
+    _, stride = plan.input_shape()
+    x = np.repeat(np.arange(nchans, dtype=np.float32)[:, None], stride, axis=1)
+    got = _run(plan, x, torch)
+    assert np.all(got == nchans * (nchans - 1) / 2)
+
+
+def test_host_path_equals_device_path(lib, orc, cuda):
+    import mdsm_gb300 as m
+    torch = cuda
+    nchans, nsamp = 128, 5000
+    plan = m.BrutePlan(nchans, 1500.0, -1.0, 64e-6, nsamp, [(0.0, 1.0, 64)], in_dtype="u8",
+                       out_dtype="i32")
+    info = plan.info
+    rng = np.random.default_rng(5)
+    # reference host layout: pitch exactly nsamp + maxshift
+    h = rng.integers(0, 256, (nchans, nsamp + info.maxshift), dtype=np.uint8)
+    got = plan.dedisperse_host(h)
+    want = orc.dedisperse(h, plan.shift_table(), nsamp)
+    assert np.array_equal(got, want)
+
+
+def test_cfg1_full_size_bitexact_and_fp64_error(lib, orc, cuda):
+    """Config 1 at full size: 256 ch x 32768 float samples, 500 DMs 0-99.8."""
+    import mdsm_gb300 as m
+    from mdsm_gb300 import synth
+    torch = cuda
+    x, meta = synth.cfg1()
+    S = orc.shift_table(256, meta["fch1"], meta["foff"], meta["tsamp"], synth.cfg1_segments())
+    nsamp = 32768 - int(S.max())
+    plan = m.BrutePlan(256, meta["fch1"], meta["foff"], meta["tsamp"], nsamp,
+                       synth.cfg1_segments(), in_dtype="f32")
+    assert np.array_equal(plan.shift_table(), S)
+    got = plan.dedisperse_host(x)
+    want = orc.dedisperse(x, S, nsamp)
+    assert np.array_equal(got, want)
+    y64 = orc.dedisperse(x, S, nsamp, out="f64")
+    # FP32 error against FP64, relative to the summation scale sum_c |x|
+    scale = orc.dedisperse(np.abs(x), S, nsamp, out="f64")
+    rel = np.abs(got.astype(np.float64) - y64) / scale
+    assert rel.max() < 2e-6

@@ -97,22 +97,43 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+_CPU_CACHE = {}
+
+
 def cpu_sample(orc, ndms, nsamp, nchans, seed=7):
     """Time the oracle's brute force (the reference algorithm, OpenMP over DMs) on a sample."""
-    from mdsm_gb300 import synth
-    S_full = orc.shift_table(nchans, FCH1, -BW / nchans, TSAMP, SEGMENTS, mode="l1")
+    key = ("S", nchans)
+    if key not in _CPU_CACHE:
+        _CPU_CACHE[key] = orc.shift_table(nchans, FCH1, -BW / nchans, TSAMP, SEGMENTS, mode="l1")
+    S_full = _CPU_CACHE[key]
     pick = np.linspace(0, S_full.shape[0] - 1, ndms).astype(int)
     S = np.ascontiguousarray(S_full[pick])
-    x = synth.gaussian_u8(nchans, nsamp + int(S.max()) + 1, seed)
+    ncols = nsamp + int(S_full.max()) + 1
+    xkey = ("x", nchans, ncols)
+    if xkey not in _CPU_CACHE:
+        rng = np.random.default_rng(seed)
+        _CPU_CACHE[xkey] = rng.integers(96, 160, (nchans, ncols), dtype=np.uint8)
+    x = _CPU_CACHE[xkey]
     t0 = time.perf_counter()
     orc.dedisperse(x, S, nsamp)
     return time.perf_counter() - t0
 
 
-def cpu_baseline(orc, budget_s=10.0, nchans=NCHANS, nsamp=16384):
+def calibrate(orc, budget_s, nchans=NCHANS):
+    """(ndms, nsamp) of a sample that takes about budget_s on this host."""
+    nsamp = 16384
+    t_small = cpu_sample(orc, 8, nsamp, nchans)
+    scale = budget_s / max(t_small, 1e-3)
+    ndms = int(max(8, min(4096, 8 * scale)))
+    if ndms == 4096:
+        nsamp = int(min(NSAMP, nsamp * scale * 8 / 4096))
+        nsamp = max(16384, nsamp // 1024 * 1024)
+    return ndms, nsamp
+
+
+def cpu_baseline(orc, budget_s=10.0, nchans=NCHANS):
     cores = os.cpu_count() or 1
-    t_small = cpu_sample(orc, 4, nsamp, nchans)
-    ndms = int(max(4, min(4096, 4 * budget_s / max(t_small, 1e-3))))
+    ndms, nsamp = calibrate(orc, budget_s, nchans)
     t = cpu_sample(orc, ndms, nsamp, nchans)
     return {"value": ndms * nsamp / t, "unit": METRIC, "cores": cores, "kind": "port",
             "sample": "oracle brute force (reference index math, OpenMP over DM trials) on "
@@ -127,9 +148,7 @@ def run_reference(args, rank, world):
         return
     from oracle import oracle as orc
     orc.build(reference=False)
-    nsamp = 16384
-    t_small = cpu_sample(orc, 4, nsamp, NCHANS)
-    ndms = int(max(4, min(4096, 4 * 6.0 / max(t_small, 1e-3))))
+    ndms, nsamp = calibrate(orc, 6.0)
     for _ in range(args.warmup):
         cpu_sample(orc, ndms, nsamp, NCHANS)
     ts = [cpu_sample(orc, ndms, nsamp, NCHANS) for _ in range(args.steps)]
@@ -157,6 +176,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--case", default="full", choices=["full", "small"],
+                    help="small: 2048 ch x 2^16 samples x 512 DM trials (profiling case)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -180,6 +201,12 @@ def main():
         if world > 1:
             dist.barrier()
 
+    global NCHANS, NSAMP, SEGMENTS, WORKLOAD
+    if args.case == "small":
+        NCHANS, NSAMP = 2048, 1 << 16
+        SEGMENTS = [(0.0, 0.9765625, 512)]
+        WORKLOAD = ("profiling case: uint8 2048 ch x 2^16 samples, 512 DM trials 0-500, INT32 "
+                    "accumulation (input 168 MB > L2)")
     plan = m.BrutePlan(NCHANS, FCH1, -BW / NCHANS, TSAMP, NSAMP, SEGMENTS, shift_mode="l1",
                        in_dtype="u8", out_dtype="i32")
     info = plan.info
@@ -254,10 +281,13 @@ def main():
     alg_bytes = info.nchans * (info.nsamp + info.maxshift) * 1 + info.ndms * info.nsamp * 4
     hbm_achieved = alg_bytes / (per_launch_ms / 1e3) / 1e9
     traffic = None
-    tp = os.path.join(ROOT, "profiles", "traffic.json")
+    tp = os.path.join(ROOT, "profiles", "traffic.txt")
+    key = "packed" if info.kernel == 2 else "generic"
     if os.path.exists(tp):
-        with open(tp) as f:
-            traffic = json.load(f).get("k_shift_sum_full_launch_bytes")
+        for ln in open(tp):
+            parts = ln.split()
+            if len(parts) == 2 and parts[0] == key + "_traffic_over_algorithmic":
+                traffic = float(parts[1]) * alg_bytes
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
@@ -277,7 +307,8 @@ def main():
                      "peak": add_peak / 1e12, "unit": "Tadd/s",
                      "frac": achieved_ops / add_peak, "traffic": traffic,
                      "peak_source": "%d SMs x 128 lanes x sm_max_mhz (%s)" % (sm_count, pk_kind),
-                     "kernel": "k_shift_sum", "per_launch_ms": per_launch_ms,
+                     "kernel": "k_shift_sum_u8x4" if info.kernel == 2 else "k_shift_sum",
+                     "per_launch_ms": per_launch_ms,
                      "algorithmic_adds_per_launch": ops},
         "roofline_hbm": {"bound": "hbm", "achieved": hbm_achieved, "peak": pk.get("hbm_gbs"),
                          "unit": "GB/s", "frac": hbm_achieved / pk.get("hbm_gbs", 6800.0),

@@ -32,6 +32,7 @@ struct KArgs {
     const int32_t *rel;                      // [g][blk][c][DB]
     const int32_t *sminspan;                 // [g][blk][c][2]
     int nchans, ndms, nsamp, nblk, rowcap, nst, out_i32;
+    int ps;  // packed kernel: bytes per phase copy of a staged row
     unsigned *err;
 };
 
@@ -171,6 +172,209 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 }
 
 // ------------------------------------------------------------------------------------------
+// Packed 8-bit kernel (uint8 samples, exact integer sums).
+//
+// The generic kernel spends one shared-memory load per add, which caps it at 32 adds per
+// clock per SM (the 128 B/clk shared-memory port).  Here one 32-bit load brings four
+// consecutive samples:
+//  * each staged row is expanded once into four phase copies, P_a[j] = bytes 4j+a .. 4j+a+3,
+//    so any run of 4 samples starting at any offset is one aligned word, and a warp's 32
+//    lanes read 32 consecutive words (no bank conflicts);
+//  * PRMT splits a word into (s0, s2) and (s1, s3) zero-extended 16-bit lanes;
+//  * those lanes are added with HADD2 (fp16x2, on the FMA pipe): a 16-bit pattern v < 2048
+//    is the fp16 number v * 2^-24 (subnormal below 1024, exponent 1 above), sums of such
+//    numbers below 2048 * 2^-24 are exact, so the bit pattern stays the integer sum;
+//  * every 8 channels (8 * 255 < 2048) the fp16 lanes are added as integers into int16x2
+//    accumulators, every 256 channels (32 * 2040 < 65536) those into int32.
+// Per 4 sample-adds: 1 LDS, 2 PRMT, 2 HADD2 and a fraction of an IADD.
+// ------------------------------------------------------------------------------------------
+constexpr int kPNW = 16;            // warps
+constexpr int kPDPW = 2;            // DM trials per warp
+constexpr int kPR4 = 4;             // 4-sample words per lane per DM trial
+constexpr int kPCC = 16;            // channels per stage
+constexpr int kPNR = 3;             // raw stages in flight
+constexpr int kPT = 128 * kPR4;     // samples per tile (512)
+constexpr int kPDB = kPNW * kPDPW;  // DM trials per tile (32)
+
+__device__ __forceinline__ uint32_t hadd2_bits(uint32_t a, uint32_t b)
+{
+    uint32_t d;
+    asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+
+__global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int rawcap = a.rowcap;  // bytes per raw row
+    const int ps = a.ps;          // bytes per phase copy
+    const int nwp = ps >> 2;      // words per phase copy
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    unsigned char *raw = smem + 128;
+    int32_t *offsm = reinterpret_cast<int32_t *>(raw + (size_t)kPNR * kPCC * rawcap);
+    int32_t *offcur = offsm + kPNR * kPCC * kPDB;
+    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + kPCC * kPDB);
+
+    const int blk = blockIdx.x, g = blockIdx.z;
+    const long long t0 = (long long)blockIdx.y * kPT;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const unsigned char *in_g = a.in + (size_t)(g * a.in_group_stride);
+    const size_t bofs = (size_t)(g * a.nblk + blk) * a.nchans;
+    const int32_t *off_b = a.rel + bofs * kPDB;
+    const int32_t *ss_b = a.sminspan + bofs * 2;
+    const int nchunks = (a.nchans + kPCC - 1) / kPCC;
+
+    if (tid == 0) {
+        for (int s = 0; s < kPNR; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+
+    auto fill = [&](int s, int k) {
+        const int c0 = k * kPCC;
+        const int nc = min(kPCC, a.nchans - c0);
+        unsigned bytes = 0;
+        const unsigned char *src = nullptr;
+        if (lane < nc) {
+            const int c = c0 + lane;
+            const long long start = t0 + ss_b[2 * c];
+            const long long end = start + kPT + ss_b[2 * c + 1];
+            const long long sb = start & ~15LL;
+            const long long eb = (end + 15) & ~15LL;
+            bytes = (unsigned)(eb - sb);
+            src = in_g + (size_t)c * (size_t)a.in_stride + sb;
+        }
+        const unsigned offbytes = (unsigned)(nc * kPDB * 4);
+        const unsigned total = warp_sum_u32(bytes) + offbytes;
+        __syncwarp();
+        if (lane == 0) mbar_arrive_expect_tx(&bars[s], total);
+        __syncwarp();
+        if (lane < nc) bulk_g2s(raw + (size_t)(s * kPCC + lane) * rawcap, src, bytes, &bars[s]);
+        if (lane == 0)
+            bulk_g2s(offsm + s * kPCC * kPDB, off_b + (size_t)c0 * kPDB, offbytes, &bars[s]);
+    };
+
+    if (warp == 0)
+        for (int s = 0; s < kPNR && s < nchunks; ++s) fill(s, s);
+
+    uint32_t hl[kPDPW][kPR4], hh[kPDPW][kPR4];  // fp16x2 partials (<= 8 channels)
+    uint32_t il[kPDPW][kPR4], ih[kPDPW][kPR4];  // int16x2 partials (<= 256 channels)
+    int32_t f[kPDPW][kPR4][4];                  // int32 sums
+#pragma unroll
+    for (int j = 0; j < kPDPW; ++j)
+#pragma unroll
+        for (int r = 0; r < kPR4; ++r) {
+            hl[j][r] = hh[j][r] = il[j][r] = ih[j][r] = 0u;
+#pragma unroll
+            for (int e = 0; e < 4; ++e) f[j][r][e] = 0;
+        }
+
+    int k = 0;
+    bool aborted = false;
+    for (; k < nchunks; ++k) {
+        const int s = k % kPNR;
+        const unsigned par = (unsigned)(k / kPNR) & 1u;
+        const int nc = min(kPCC, a.nchans - k * kPCC);
+        const bool ok = mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
+        if (ok) {
+            // expand the staged rows into their four phase copies; take the offsets
+            for (int ci = 0; ci < nc; ++ci) {
+                const uint32_t *W =
+                    reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + ci) * rawcap);
+                uint32_t *Pr = P + (size_t)ci * 4 * nwp;
+                for (int j = tid; j < nwp; j += kPNW * 32) {
+                    const uint32_t w0 = W[j], w1 = W[j + 1];
+                    Pr[j] = w0;
+                    Pr[nwp + j] = __funnelshift_r(w0, w1, 8);
+                    Pr[2 * nwp + j] = __funnelshift_r(w0, w1, 16);
+                    Pr[3 * nwp + j] = __funnelshift_r(w0, w1, 24);
+                }
+            }
+            for (int i = tid; i < nc * kPDB; i += kPNW * 32) offcur[i] = offsm[s * kPCC * kPDB + i];
+        }
+        if (__syncthreads_or(!ok)) {
+            aborted = true;
+            break;
+        }
+        if (warp == 0 && k + kPNR < nchunks) {
+            fence_proxy_async_smem();
+            fill(s, k + kPNR);
+        }
+        // accumulate this chunk
+        const unsigned char *pbase = reinterpret_cast<const unsigned char *>(P) + lane * 4;
+        const int32_t *oc = offcur + warp * kPDPW;
+#pragma unroll 1
+        for (int ci = 0; ci < nc; ++ci) {
+            const unsigned char *prow = pbase + (size_t)ci * 4 * ps;
+#pragma unroll
+            for (int j = 0; j < kPDPW; ++j) {
+                const uint32_t *p = reinterpret_cast<const uint32_t *>(prow + oc[ci * kPDB + j]);
+#pragma unroll
+                for (int r = 0; r < kPR4; ++r) {
+                    const uint32_t w = p[32 * r];
+                    hl[j][r] = hadd2_bits(hl[j][r], __byte_perm(w, 0u, 0x4240));
+                    hh[j][r] = hadd2_bits(hh[j][r], __byte_perm(w, 0u, 0x4341));
+                }
+            }
+            if ((ci & 7) == 7 || ci == nc - 1) {
+#pragma unroll
+                for (int j = 0; j < kPDPW; ++j)
+#pragma unroll
+                    for (int r = 0; r < kPR4; ++r) {
+                        il[j][r] += hl[j][r];
+                        ih[j][r] += hh[j][r];
+                        hl[j][r] = hh[j][r] = 0u;
+                    }
+            }
+        }
+        if (((k + 1) & 15) == 0 || k == nchunks - 1) {
+#pragma unroll
+            for (int j = 0; j < kPDPW; ++j)
+#pragma unroll
+                for (int r = 0; r < kPR4; ++r) {
+                    f[j][r][0] += (int32_t)(il[j][r] & 0xFFFFu);
+                    f[j][r][2] += (int32_t)(il[j][r] >> 16);
+                    f[j][r][1] += (int32_t)(ih[j][r] & 0xFFFFu);
+                    f[j][r][3] += (int32_t)(ih[j][r] >> 16);
+                    il[j][r] = ih[j][r] = 0u;
+                }
+        }
+        __syncthreads();  // P and offcur are rewritten by the next chunk
+    }
+
+    if (aborted) {
+        for (int kk = k; kk < nchunks && kk < k + kPNR; ++kk)
+            mbar_wait_bounded(&bars[kk % kPNR], (unsigned)(kk / kPNR) & 1u, nullptr, 0);
+        return;
+    }
+
+#pragma unroll
+    for (int j = 0; j < kPDPW; ++j) {
+        const int d = blk * kPDB + warp * kPDPW + j;
+        if (d >= a.ndms) continue;
+        unsigned char *orow =
+            a.out + (size_t)(g * a.out_group_stride + (long long)d * a.out_stride) * 4;
+#pragma unroll
+        for (int r = 0; r < kPR4; ++r) {
+            const long long t = t0 + 4 * (lane + 32 * r);
+            if (t + 3 < a.nsamp && ((((uintptr_t)orow) | (t * 4)) & 15) == 0) {
+                if (a.out_i32)
+                    *reinterpret_cast<int4 *>(orow + t * 4) =
+                        make_int4(f[j][r][0], f[j][r][1], f[j][r][2], f[j][r][3]);
+                else
+                    *reinterpret_cast<float4 *>(orow + t * 4) =
+                        make_float4((float)f[j][r][0], (float)f[j][r][1], (float)f[j][r][2],
+                                    (float)f[j][r][3]);
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; ++e)
+                    if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
+            }
+        }
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
 
@@ -233,14 +437,50 @@ size_t dtype_size(int dtype)
     }
 }
 
-// Tile S[g][d][c] into per-block relative tables.  Fails if any shift is negative.
+namespace {
+
+// Per-block (smin, span) and relative shifts of S[g][d][c] for DM blocks of g.Db.
+int tile_tables(StageGeom &g, const std::vector<int32_t> &S)
+{
+    g.nblk = (g.ndms + g.Db - 1) / g.Db;
+    g.rel.assign((size_t)g.ngroups * g.nblk * g.nchans * g.Db, 0);
+    g.sminspan.assign((size_t)g.ngroups * g.nblk * g.nchans * 2, 0);
+    int maxspan = 0;
+    for (int gi = 0; gi < g.ngroups; ++gi)
+        for (int b = 0; b < g.nblk; ++b) {
+            const int d0 = b * g.Db, d1 = std::min(g.ndms, d0 + g.Db);
+            for (int c = 0; c < g.nchans; ++c) {
+                int lo = INT32_MAX, hi = INT32_MIN;
+                for (int d = d0; d < d1; ++d) {
+                    const int v = S[((size_t)gi * g.ndms + d) * g.nchans + c];
+                    lo = std::min(lo, v);
+                    hi = std::max(hi, v);
+                }
+                const size_t o = (((size_t)gi * g.nblk + b) * g.nchans + c);
+                g.sminspan[o * 2] = lo;
+                g.sminspan[o * 2 + 1] = hi - lo;
+                maxspan = std::max(maxspan, hi - lo);
+                for (int d = d0; d < d1; ++d)
+                    g.rel[o * g.Db + (d - d0)] = S[((size_t)gi * g.ndms + d) * g.nchans + c] - lo;
+            }
+        }
+    return maxspan;
+}
+
+size_t packed_smem(int rawcap, int ps)
+{
+    return 128 + (size_t)kPNR * kPCC * rawcap + (size_t)kPNR * kPCC * kPDB * 4 +
+           (size_t)kPCC * kPDB * 4 + (size_t)kPCC * 4 * ps;
+}
+
+}  // namespace
+
+// Tile S[g][d][c] for the kernel.  Fails if any shift is negative.  uint8 samples use the
+// packed kernel (Db 32, T 512) unless g.kernel == 1 asks for the generic one or its staging
+// does not fit; everything else uses the generic kernel with Db 32/16/8.
 mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
 {
     const int SZ = (int)dtype_size(g.in_dtype);
-    g.R = kR;
-    g.T = 32 * kR;
-    g.cc = SZ == 4 ? 8 : 16;
-    g.kernel = 1;
     const long long need = (long long)g.ngroups * g.ndms * g.nchans;
     if ((long long)S.size() != need) return fail(MDSM_EINVAL, "shift table size mismatch");
     int mx = 0;
@@ -251,35 +491,44 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
         mx = std::max(mx, (int)S[(size_t)i]);
     }
     g.max_shift = mx;
+    if (g.in_dtype == MDSM_U8 && g.kernel != 1) {
+        g.Db = kPDB;
+        g.T = kPT;
+        g.R = kPR4 * 4;
+        g.DPW = kPDPW;
+        g.cc = kPCC;
+        g.nst = kPNR;
+        const int maxspan = tile_tables(g, S);
+        const int rawcap = (int)(((long long)kPT + maxspan + 32 + 15) / 16 * 16) + 16;
+        const int ps = rawcap - 16;  // nwp = ps/4 words; the conversion reads word nwp too
+        if (packed_smem(rawcap, ps) <= 220 * 1024) {
+            g.max_span = maxspan;
+            g.rowcap = rawcap;
+            g.ps = ps;
+            // byte offset of (c, d)'s first word inside the phase-expanded row
+            for (size_t o = 0; o < g.sminspan.size() / 2; ++o) {
+                const int lo16 = g.sminspan[o * 2] & 15;
+                for (int j = 0; j < g.Db; ++j) {
+                    const int e = lo16 + g.rel[o * g.Db + j];
+                    g.rel[o * g.Db + j] = (e & 3) * ps + (e >> 2) * 4;
+                }
+            }
+            g.smem_bytes = packed_smem(rawcap, ps);
+            g.kernel = 2;
+            return MDSM_OK;
+        }
+    }
+    g.kernel = 1;
+    g.R = kR;
+    g.T = 32 * kR;
+    g.cc = SZ == 4 ? 8 : 16;
     // Try Db = 32, 16, 8 until the staged rows fit in shared memory.
     const int dpws[3] = {4, 2, 1};
     int first = g.DPW == 4 ? 0 : (g.DPW == 2 ? 1 : 2);
     for (int i = first; i < 3; ++i) {
         g.DPW = dpws[i];
         g.Db = kNW * g.DPW;
-        g.nblk = (g.ndms + g.Db - 1) / g.Db;
-        g.rel.assign((size_t)g.ngroups * g.nblk * g.nchans * g.Db, 0);
-        g.sminspan.assign((size_t)g.ngroups * g.nblk * g.nchans * 2, 0);
-        int maxspan = 0;
-        for (int gi = 0; gi < g.ngroups; ++gi)
-            for (int b = 0; b < g.nblk; ++b) {
-                const int d0 = b * g.Db, d1 = std::min(g.ndms, d0 + g.Db);
-                for (int c = 0; c < g.nchans; ++c) {
-                    int lo = INT32_MAX, hi = INT32_MIN;
-                    for (int d = d0; d < d1; ++d) {
-                        const int v = S[((size_t)gi * g.ndms + d) * g.nchans + c];
-                        lo = std::min(lo, v);
-                        hi = std::max(hi, v);
-                    }
-                    const size_t o = (((size_t)gi * g.nblk + b) * g.nchans + c);
-                    g.sminspan[o * 2] = lo;
-                    g.sminspan[o * 2 + 1] = hi - lo;
-                    maxspan = std::max(maxspan, hi - lo);
-                    for (int d = d0; d < d1; ++d)
-                        g.rel[o * g.Db + (d - d0)] =
-                            S[((size_t)gi * g.ndms + d) * g.nchans + c] - lo;
-                }
-            }
+        const int maxspan = tile_tables(g, S);
         g.max_span = maxspan;
         const long long bytes = (long long)(g.T + maxspan) * SZ + 32;
         g.rowcap = (int)(((bytes + 15) / 16) * 16 / SZ);
@@ -335,7 +584,8 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
         return fail(MDSM_EINVAL, "input row pitch must be a multiple of 16 bytes");
     if ((in_group_stride * SZ) % 16 != 0)
         return fail(MDSM_EINVAL, "input group pitch must be a multiple of 16 bytes");
-    void *fn = select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
+    void *fn = g.kernel == 2 ? reinterpret_cast<void *>(&k_shift_sum_u8x4)
+                             : select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
     MDSM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)g.smem_bytes));
     KArgs a;
@@ -354,13 +604,15 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     a.rowcap = g.rowcap;
     a.nst = g.nst;
     a.out_i32 = g.out_i32;
+    a.ps = g.ps;
     a.err = d_err;
     const long long ntiles = (g.nsamp + g.T - 1) / g.T;
     if (ntiles > 65535 || g.ngroups > 65535)
         return fail(MDSM_EINVAL, "block too long for one launch");
     dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);
     void *args[] = {&a};
-    MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kNW * 32), args, g.smem_bytes, st));
+    const unsigned threads = g.kernel == 2 ? kPNW * 32 : kNW * 32;
+    MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, g.smem_bytes, st));
     if (launches) *launches += 1;
     return MDSM_OK;
 }

@@ -64,7 +64,8 @@ struct StageGeom {
     int32_t *d_rel = nullptr;
     int32_t *d_sminspan = nullptr;
     size_t smem_bytes = 0;
-    int kernel = 1;       // 1 generic, 2 packed u8
+    int ps = 0;           // packed kernel: bytes per phase copy of a staged row
+    int kernel = 0;       // requested (0 choose, 1 generic); after tiling: 1 generic, 2 packed u8
 };
 
 // Build the blocked tables of a stage from a full shift table S[g][d][c] (row-major).  Picks

@@ -176,6 +176,7 @@ mdsm_status plan_create_brute(const mdsm_brute_desc &d, Plan &p)
     g.acc_int = ai;
     g.out_i32 = d.out_dtype == MDSM_OUT_I32;
     g.DPW = d.dm_block == 16 ? 2 : (d.dm_block == 8 ? 1 : 4);
+    g.kernel = d.kernel;
     MDSM_TRY(build_stage_tables(g, p.S));
     p.maxshift = g.max_shift;
     MDSM_TRY(upload_stage(g));

@@ -81,7 +81,7 @@ def host_fixtures():
     print("wrote ref_host.npz: %d detections" % len(det))
 
 
-def gpu_fixtures():
+def gpu_fixtures(out_dir=HERE):
     orc.build(reference=False)
     g = orc.RefGPU()
     out = {}
@@ -103,12 +103,13 @@ def gpu_fixtures():
     x2 = rng.standard_normal((nchans, nsamp2 + ms2), dtype=np.float32)
     y2, _ = g.brute(1, x2, nsamp2, ms2, lowdm, dmstep, tsamp, tdms, dms)
     out.update(opt_x=x2, opt_y=y2, opt_meta=np.array([nchans, nsamp2, ms2, tdms], np.int64))
-    np.savez_compressed(os.path.join(HERE, "ref_gpu.npz"), **out)
+    np.savez_compressed(os.path.join(out_dir, "ref_gpu.npz"), **out)
     print("wrote ref_gpu.npz")
 
 
 if __name__ == "__main__":
     if "--gpu" in sys.argv:
-        gpu_fixtures()
+        od = sys.argv[sys.argv.index("--out") + 1] if "--out" in sys.argv else HERE
+        gpu_fixtures(od)
     else:
         host_fixtures()

@@ -107,3 +107,43 @@ def test_cfg1_full_size_bitexact_and_fp64_error(lib, orc, cuda):
     scale = orc.dedisperse(np.abs(x), S, nsamp, out="f64")
     rel = np.abs(got.astype(np.float64) - y64) / scale
     assert rel.max() < 2e-6
+
+
+@pytest.mark.parametrize("nchans,nsamp,ndms", [(4096, 2000, 40), (257, 511, 33), (9, 4, 1),
+                                               (600, 3333, 100)])
+def test_packed_u8_matches_generic_and_oracle(lib, orc, cuda, nchans, nsamp, ndms):
+    """The packed 8-bit kernel (default for uint8) against the generic kernel and the oracle,
+    including all-255 input where every partial-sum stage is filled to its limit."""
+    import mdsm_gb300 as m
+    torch = cuda
+    segs = [(0.0, 600.0 / max(ndms, 1), ndms)]
+    packed = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs, in_dtype="u8",
+                         out_dtype="i32")
+    generic = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs, in_dtype="u8",
+                          out_dtype="i32", kernel=1)
+    assert packed.info.kernel == 2 and generic.info.kernel == 1
+    for fill in ("random", "max"):
+        nch, stride = packed.input_shape()
+        if fill == "max":
+            x = np.full((nch, stride), 255, np.uint8)
+        else:
+            x = np.random.default_rng(nchans).integers(0, 256, (nch, stride), dtype=np.uint8)
+        got = _run(packed, x, torch)
+        want = orc.dedisperse(x, packed.shift_table(), nsamp)
+        assert np.array_equal(got, want), fill
+        xg = np.zeros(generic.input_shape(), np.uint8)
+        w = min(xg.shape[1], x.shape[1])
+        xg[:, :w] = x[:, :w]
+        assert np.array_equal(_run(generic, xg, torch), want), fill
+
+
+def test_packed_u8_float_output(lib, orc, cuda):
+    import mdsm_gb300 as m
+    torch = cuda
+    plan = m.BrutePlan(512, 1500.0, -0.5, 64e-6, 1500, [(0.0, 1.0, 64)], in_dtype="u8",
+                       out_dtype="f32")
+    nch, stride = plan.input_shape()
+    x = np.random.default_rng(2).integers(0, 256, (nch, stride), dtype=np.uint8)
+    got = _run(plan, x, torch)
+    assert got.dtype == np.float32
+    assert np.array_equal(got, orc.dedisperse(x, plan.shift_table(), 1500).astype(np.float32))

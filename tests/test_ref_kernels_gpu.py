@@ -85,8 +85,10 @@ def test_reference_subband_bitexact(lib, orc, cuda, refgpu):
                                             orc.ctypes.c_float(p["highdm"]),
                                             orc.ctypes.c_float(tsamp))
     S1, S2 = plan.stage_tables()
-    # the reference reads stage-2 rows of nsamp + tempval; ours sizes by max(S2)
-    assert S2.max() <= tempval + 1
+    # The reference's stage-1 rows hold nsamp + tempval samples, but its fine DMs run past
+    # highdm (dm0 = subDM - calldms*dmstep/2 + k*dmstep), so some stage-2 shifts exceed tempval
+    # and the reference then reads the next subband's row.  Ours sizes rows by max(S2).
+    assert S2.max() >= tempval
     ms = max(plan.maxshift, tempval + int(S1.max())) + 2
     rng = np.random.default_rng(11)
     x = rng.standard_normal((nchans, nsamp + ms), dtype=np.float32)

@@ -206,14 +206,15 @@ __device__ __forceinline__ uint32_t hadd2_bits(uint32_t a, uint32_t b)
 __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    const int rawcap = a.rowcap;  // bytes per raw row
-    const int ps = a.ps;          // bytes per phase copy
+    const int rawcap = a.rowcap;  // bytes per raw row (multiple of 16)
+    const int ps = a.ps;          // bytes per phase copy (multiple of 16)
     const int nwp = ps >> 2;      // words per phase copy
+    const int nq = nwp >> 2;      // 16-byte quads per phase copy
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     unsigned char *raw = smem + 128;
     int32_t *offsm = reinterpret_cast<int32_t *>(raw + (size_t)kPNR * kPCC * rawcap);
-    int32_t *offcur = offsm + kPNR * kPCC * kPDB;
-    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + kPCC * kPDB);
+    int32_t *offcur = offsm + kPNR * kPCC * kPDB;                 // 2 x kPCC x kPDB
+    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + 2 * kPCC * kPDB);  // 2 x kPCC x 4 x nwp
 
     const int blk = blockIdx.x, g = blockIdx.z;
     const long long t0 = (long long)blockIdx.y * kPT;
@@ -273,24 +274,33 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
     bool aborted = false;
     for (; k < nchunks; ++k) {
         const int s = k % kPNR;
+        const int pb = k & 1;  // phase buffer of this chunk
         const unsigned par = (unsigned)(k / kPNR) & 1u;
         const int nc = min(kPCC, a.nchans - k * kPCC);
         const bool ok = mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
         if (ok) {
-            // expand the staged rows into their four phase copies; take the offsets
-            for (int ci = 0; ci < nc; ++ci) {
+            // Expand staged row `warp` into its four phase copies (16-byte loads and stores).
+            // P[pb] was last read by chunk k-2, before the barrier of iteration k-1.
+            if (warp < nc) {
                 const uint32_t *W =
-                    reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + ci) * rawcap);
-                uint32_t *Pr = P + (size_t)ci * 4 * nwp;
-                for (int j = tid; j < nwp; j += kPNW * 32) {
-                    const uint32_t w0 = W[j], w1 = W[j + 1];
-                    Pr[j] = w0;
-                    Pr[nwp + j] = __funnelshift_r(w0, w1, 8);
-                    Pr[2 * nwp + j] = __funnelshift_r(w0, w1, 16);
-                    Pr[3 * nwp + j] = __funnelshift_r(w0, w1, 24);
+                    reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + warp) * rawcap);
+                uint32_t *Pr = P + ((size_t)pb * kPCC + warp) * 4 * nwp;
+                for (int i = lane; i < nq; i += 32) {
+                    const uint4 w = reinterpret_cast<const uint4 *>(W)[i];
+                    const uint32_t w4 = W[4 * i + 4];
+                    reinterpret_cast<uint4 *>(Pr)[i] = w;
+                    reinterpret_cast<uint4 *>(Pr + nwp)[i] =
+                        make_uint4(__funnelshift_r(w.x, w.y, 8), __funnelshift_r(w.y, w.z, 8),
+                                   __funnelshift_r(w.z, w.w, 8), __funnelshift_r(w.w, w4, 8));
+                    reinterpret_cast<uint4 *>(Pr + 2 * nwp)[i] =
+                        make_uint4(__funnelshift_r(w.x, w.y, 16), __funnelshift_r(w.y, w.z, 16),
+                                   __funnelshift_r(w.z, w.w, 16), __funnelshift_r(w.w, w4, 16));
+                    reinterpret_cast<uint4 *>(Pr + 3 * nwp)[i] =
+                        make_uint4(__funnelshift_r(w.x, w.y, 24), __funnelshift_r(w.y, w.z, 24),
+                                   __funnelshift_r(w.z, w.w, 24), __funnelshift_r(w.w, w4, 24));
                 }
             }
-            for (int i = tid; i < nc * kPDB; i += kPNW * 32) offcur[i] = offsm[s * kPCC * kPDB + i];
+            offcur[pb * kPCC * kPDB + tid] = offsm[s * kPCC * kPDB + tid];  // 512 entries
         }
         if (__syncthreads_or(!ok)) {
             aborted = true;
@@ -300,32 +310,34 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
             fence_proxy_async_smem();
             fill(s, k + kPNR);
         }
-        // accumulate this chunk
-        const unsigned char *pbase = reinterpret_cast<const unsigned char *>(P) + lane * 4;
-        const int32_t *oc = offcur + warp * kPDPW;
-#pragma unroll 1
-        for (int ci = 0; ci < nc; ++ci) {
-            const unsigned char *prow = pbase + (size_t)ci * 4 * ps;
-#pragma unroll
-            for (int j = 0; j < kPDPW; ++j) {
-                const uint32_t *p = reinterpret_cast<const uint32_t *>(prow + oc[ci * kPDB + j]);
+        const unsigned char *pbase =
+            reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * 4 * nwp) + lane * 4;
+        const int32_t *oc = offcur + pb * kPCC * kPDB + warp * kPDPW;
+        for (int c8 = 0; c8 < nc; c8 += 8) {
+            const int ce = min(c8 + 8, nc);
+#pragma unroll 2
+            for (int ci = c8; ci < ce; ++ci) {
+                const unsigned char *prow = pbase + (size_t)ci * 4 * ps;
+                const int2 o2 = *reinterpret_cast<const int2 *>(oc + ci * kPDB);
+                const uint32_t *p0 = reinterpret_cast<const uint32_t *>(prow + o2.x);
+                const uint32_t *p1 = reinterpret_cast<const uint32_t *>(prow + o2.y);
 #pragma unroll
                 for (int r = 0; r < kPR4; ++r) {
-                    const uint32_t w = p[32 * r];
-                    hl[j][r] = hadd2_bits(hl[j][r], __byte_perm(w, 0u, 0x4240));
-                    hh[j][r] = hadd2_bits(hh[j][r], __byte_perm(w, 0u, 0x4341));
+                    const uint32_t w0 = p0[32 * r], w1 = p1[32 * r];
+                    hl[0][r] = hadd2_bits(hl[0][r], __byte_perm(w0, 0u, 0x4240));
+                    hh[0][r] = hadd2_bits(hh[0][r], __byte_perm(w0, 0u, 0x4341));
+                    hl[1][r] = hadd2_bits(hl[1][r], __byte_perm(w1, 0u, 0x4240));
+                    hh[1][r] = hadd2_bits(hh[1][r], __byte_perm(w1, 0u, 0x4341));
                 }
             }
-            if ((ci & 7) == 7 || ci == nc - 1) {
 #pragma unroll
-                for (int j = 0; j < kPDPW; ++j)
+            for (int j = 0; j < kPDPW; ++j)
 #pragma unroll
-                    for (int r = 0; r < kPR4; ++r) {
-                        il[j][r] += hl[j][r];
-                        ih[j][r] += hh[j][r];
-                        hl[j][r] = hh[j][r] = 0u;
-                    }
-            }
+                for (int r = 0; r < kPR4; ++r) {
+                    il[j][r] += hl[j][r];
+                    ih[j][r] += hh[j][r];
+                    hl[j][r] = hh[j][r] = 0u;
+                }
         }
         if (((k + 1) & 15) == 0 || k == nchunks - 1) {
 #pragma unroll
@@ -339,7 +351,6 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
                     il[j][r] = ih[j][r] = 0u;
                 }
         }
-        __syncthreads();  // P and offcur are rewritten by the next chunk
     }
 
     if (aborted) {
@@ -470,7 +481,7 @@ int tile_tables(StageGeom &g, const std::vector<int32_t> &S)
 size_t packed_smem(int rawcap, int ps)
 {
     return 128 + (size_t)kPNR * kPCC * rawcap + (size_t)kPNR * kPCC * kPDB * 4 +
-           (size_t)kPCC * kPDB * 4 + (size_t)kPCC * 4 * ps;
+           (size_t)2 * kPCC * kPDB * 4 + (size_t)2 * kPCC * 4 * ps;
 }
 
 }  // namespace
@@ -500,7 +511,7 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
         g.nst = kPNR;
         const int maxspan = tile_tables(g, S);
         const int rawcap = (int)(((long long)kPT + maxspan + 32 + 15) / 16 * 16) + 16;
-        const int ps = rawcap - 16;  // nwp = ps/4 words; the conversion reads word nwp too
+        const int ps = rawcap - 16;  // nwp = ps/4 words; the expansion reads word nwp too
         if (packed_smem(rawcap, ps) <= 220 * 1024) {
             g.max_span = maxspan;
             g.rowcap = rawcap;

@@ -116,7 +116,7 @@ def test_packed_u8_matches_generic_and_oracle(lib, orc, cuda, nchans, nsamp, ndm
     including all-255 input where every partial-sum stage is filled to its limit."""
     import mdsm_gb300 as m
     torch = cuda
-    segs = [(0.0, 600.0 / max(ndms, 1), ndms)]
+    segs = [(0.0, 0.5, ndms)]
     packed = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs, in_dtype="u8",
                          out_dtype="i32")
     generic = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs, in_dtype="u8",
@@ -135,6 +135,19 @@ def test_packed_u8_matches_generic_and_oracle(lib, orc, cuda, nchans, nsamp, ndm
         w = min(xg.shape[1], x.shape[1])
         xg[:, :w] = x[:, :w]
         assert np.array_equal(_run(generic, xg, torch), want), fill
+
+
+def test_packed_falls_back_for_wide_plans(lib, orc, cuda):
+    """A DM block whose shift span does not fit the packed kernel's staging runs on the
+    generic kernel, with the same exact result."""
+    import mdsm_gb300 as m
+    torch = cuda
+    plan = m.BrutePlan(1024, 1500.0, -300.0 / 1024, 64e-6, 1000, [(0.0, 20.0, 40)],
+                       in_dtype="u8", out_dtype="i32")
+    assert plan.info.kernel == 1
+    nch, stride = plan.input_shape()
+    x = np.random.default_rng(9).integers(0, 256, (nch, stride), dtype=np.uint8)
+    assert np.array_equal(_run(plan, x, torch), orc.dedisperse(x, plan.shift_table(), 1000))
 
 
 def test_packed_u8_float_output(lib, orc, cuda):

@@ -185,6 +185,23 @@ mdsm_status mdsm_ref_detect_device(const float *d_series, int ndms, int nsamp, f
                                    long long cap, long long *ncand, float *mean, float *rms,
                                    void *stream);
 
+/* The reference detector above, for callers that cannot allocate device memory: a real-time
+ * stage that must not stall on the device allocator between blocks, a host that hands out all
+ * device memory once at start-up, or a plugin where allocation is not permitted.  This entry
+ * point has no counterpart in the reference.  It calls no cudaMalloc/cudaFree and no allocating
+ * library routine: its work arrays live in one fixed device array of about 2 MiB that every GPU
+ * loading the library holds until exit.  Limits: ndms*nsamp <= 2^31 values (at most 65536
+ * statistics chunks) and cap <= 65536 candidates; larger requests return MDSM_ERANGE.  The
+ * first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls share the array
+ * and leave its contents behind (the candidate counter is cleared at each call), so calls that
+ * overlap on the GPU race.  Results equal mdsm_ref_detect_device's. */
+mdsm_status mdsm_ref_detect_device_noalloc(const float *d_series, int ndms, int nsamp,
+                                           float lowdm, float dmstep, float threshold,
+                                           mdsm_candidate *h_cands, long long cap,
+                                           long long *ncand, float *mean, float *rms,
+                                           void *stream);
+
 /* Boxcar single-pulse search (src/prototypes/singlepulse.cpp:41-146, restated): widths
  * 1,2,4..2^(nwidths-1); per-DM mean/sigma; SNR = (sum - w*mean)/(sigma*sqrt(w)); per-sample
  * best width; non-maximum suppression with radius max(w/2,1).  d_series is [ndms][nsamp] of

@@ -120,6 +120,9 @@ SIGNATURES = {
     "mdsm_ref_detect_device": (_st, [_vp, _i, _i, _f, _f, _f, ctypes.POINTER(Candidate), _ll,
                                      ctypes.POINTER(_ll), ctypes.POINTER(_f),
                                      ctypes.POINTER(_f), _vp]),
+    "mdsm_ref_detect_device_noalloc": (_st, [_vp, _i, _i, _f, _f, _f, ctypes.POINTER(Candidate),
+                                             _ll, ctypes.POINTER(_ll), ctypes.POINTER(_f),
+                                             ctypes.POINTER(_f), _vp]),
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
     "mdsm_processSurveyParameters": (ctypes.POINTER(SURVEY), [ctypes.c_char_p]),

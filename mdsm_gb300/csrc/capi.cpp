@@ -252,6 +252,18 @@ mdsm_status mdsm_ref_detect_device(const float *d_series, int ndms, int nsamp, f
                       mean, rms, static_cast<cudaStream_t>(stream));
 }
 
+mdsm_status mdsm_ref_detect_device_noalloc(const float *d_series, int ndms, int nsamp,
+                                           float lowdm, float dmstep, float threshold,
+                                           mdsm_candidate *h_cands, long long cap,
+                                           long long *ncand, float *mean, float *rms,
+                                           void *stream)
+{
+    if (!d_series || ndms <= 0 || nsamp < 5 || !ncand)
+        return fail(MDSM_EINVAL, "reference detector: bad arguments");
+    return ref_detect_noalloc(d_series, ndms, nsamp, lowdm, dmstep, threshold, h_cands, cap,
+                              ncand, mean, rms, static_cast<cudaStream_t>(stream));
+}
+
 mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, int ndms,
                                       int nsamp, int nwidths, double threshold,
                                       mdsm_candidate *h_cands, long long cap, long long *ncand,

@@ -12,7 +12,9 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstring>
 #include <mutex>
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -180,6 +182,120 @@ mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, 
     float hs[2];
     MDSM_CUDA_TRY(cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
     MDSM_TRY(fetch_cands(d_c, d_count, cap, h_cands, ncand, st));
+    if (mean) *mean = hs[0];
+    if (rms) *rms = hs[1];
+    return MDSM_OK;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Reference detector without allocation.
+//
+// Some callers cannot call cudaMalloc: a real-time pipeline stage that must not stall on the
+// device allocator between blocks, a host that hands all device memory out once at start-up
+// (an HBM-budget admission loop does this), or a plugin running where allocation is not
+// permitted.  This variant keeps its work arrays (per-chunk sums, the statistics, the candidate
+// counter and the candidate records) in one fixed array in device global memory instead of
+// the library's allocated scratch buffer.  The array is defined at file scope, so every GPU
+// that loads the library holds it (kNoAllocBytes, about 2 MiB) until the process exits.
+//
+// Limits: at most kNoAllocChunks 32K-value chunks (ndms*nsamp <= 2^31 values) and at most
+// kNoAllocCands stored candidates (cap); larger requests are rejected with MDSM_ERANGE.
+// Every call uses the same array and leaves its contents behind; the candidate counter is
+// cleared at the start of each call.  Calls whose work overlaps on the GPU (different streams
+// or threads without ordering between them) race on the array.
+// ---------------------------------------------------------------------------------------------
+constexpr unsigned kNoAllocChunks = 65536u;
+constexpr long long kNoAllocCands = 65536;
+constexpr size_t kNoAllocHeader = 256;  // counter at 0, statistics at 16
+constexpr size_t kNoAllocBytes =
+    kNoAllocHeader + (size_t)kNoAllocChunks * sizeof(double2) + (size_t)kNoAllocCands * 16;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+namespace {
+std::mutex g_noalloc_mu;
+constexpr int kMaxDevices = 64;
+void *g_noalloc_ptr[kMaxDevices];
+}  // namespace
+
+// The device address of g_noalloc_scratch on the current device.  Host code may not use the
+// symbol's name as a pointer (on the host it names a stand-in, not device memory), so the
+// address is looked up once per device, with that device current, and cached.
+static mdsm_status noalloc_scratch(char **out)
+{
+    int dev = 0;
+    MDSM_CUDA_TRY(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return fail(MDSM_EINVAL, "device index out of range");
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_ptr[dev]) {
+        void *ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_ptr[dev] = ptr;
+    }
+    *out = static_cast<char *>(g_noalloc_ptr[dev]);
+    return MDSM_OK;
+}
+
+mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float lowdm,
+                               float dmstep, float threshold, mdsm_candidate *h_cands,
+                               long long cap, long long *ncand, float *mean, float *rms,
+                               cudaStream_t st)
+{
+    const unsigned long long vals64 = (unsigned long long)ndms * (unsigned long long)nsamp;
+    if (vals64 > 0xFFFFFFFFull / 2)
+        return fail(MDSM_ERANGE, "reference detector counts values in 32 bits");
+    const unsigned vals = (unsigned)vals64;
+    const unsigned mod = vals < 32768u ? vals : 32768u;
+    unsigned nchunks = 1;
+    while ((unsigned long long)(nchunks + 1) * mod < vals) ++nchunks;
+    if (nchunks > kNoAllocChunks)
+        return fail(MDSM_ERANGE, "no-allocation detector: block needs " + std::to_string(nchunks) +
+                                     " statistics chunks, the fixed array holds " +
+                                     std::to_string(kNoAllocChunks));
+    if (cap < 0) cap = 0;
+    if (cap > kNoAllocCands)
+        return fail(MDSM_ERANGE, "no-allocation detector: cap " + std::to_string(cap) +
+                                     " exceeds the fixed array's " +
+                                     std::to_string(kNoAllocCands) + " candidates");
+    char *base = nullptr;
+    MDSM_TRY(noalloc_scratch(&base));
+    auto *d_count = reinterpret_cast<unsigned long long *>(base);
+    auto *d_stats = reinterpret_cast<float *>(base + 16);
+    auto *d_sums = reinterpret_cast<double2 *>(base + kNoAllocHeader);
+    auto *d_c = reinterpret_cast<DevCand *>(base + kNoAllocHeader +
+                                            (size_t)kNoAllocChunks * sizeof(double2));
+    MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
+    k_ref_chunk_sums<<<(nchunks + 127) / 128, 128, 0, st>>>(d_series, mod, nchunks, d_sums);
+    k_ref_finish<<<1, 1, 0, st>>>(d_sums, mod, nchunks, d_stats);
+    dim3 grid((unsigned)std::min<long long>((nsamp + 255) / 256, 64), (unsigned)ndms);
+    k_ref_detect<<<grid, 256, 0, st>>>(d_series, ndms, nsamp, lowdm, dmstep, threshold, d_stats,
+                                       d_c, d_count, cap);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    float hs[2];
+    unsigned long long n = 0;
+    MDSM_CUDA_TRY(cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
+    MDSM_CUDA_TRY(cudaMemcpyAsync(&n, d_count, sizeof(n), cudaMemcpyDeviceToHost, st));
+    MDSM_CUDA_TRY(cudaStreamSynchronize(st));
+    const long long got = std::min<long long>((long long)n, cap);
+    if (got > 0 && h_cands) {
+        // the device records (dm, sample, width, snr) land in the caller's array as they are,
+        // then are put in mdsm_candidate order in place
+        static_assert(sizeof(DevCand) == sizeof(mdsm_candidate), "record sizes differ");
+        MDSM_CUDA_TRY(cudaMemcpyAsync(h_cands, d_c, (size_t)got * sizeof(DevCand),
+                                      cudaMemcpyDeviceToHost, st));
+        MDSM_CUDA_TRY(cudaStreamSynchronize(st));
+        for (long long i = 0; i < got; ++i) {
+            DevCand dc;
+            std::memcpy(&dc, &h_cands[i], sizeof dc);
+            h_cands[i].dm_idx = dc.dm_idx;
+            h_cands[i].sample = dc.sample;
+            h_cands[i].snr = dc.snr;
+            h_cands[i].width = dc.width;
+        }
+        sort_cands(h_cands, got);
+    }
+    *ncand = (long long)n;
     if (mean) *mean = hs[0];
     if (rms) *rms = hs[1];
     return MDSM_OK;

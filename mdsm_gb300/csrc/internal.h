@@ -125,6 +125,10 @@ int32_t shift_of(float dms, double delay64, float lowdm, float dmstep, int idx, 
 mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, float dmstep,
                        float threshold, mdsm_candidate *h_cands, long long cap,
                        long long *ncand, float *mean, float *rms, cudaStream_t st);
+mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float lowdm,
+                               float dmstep, float threshold, mdsm_candidate *h_cands,
+                               long long cap, long long *ncand, float *mean, float *rms,
+                               cudaStream_t st);
 mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
                           double threshold, mdsm_candidate *h_cands, long long cap,
                           long long *ncand, cudaStream_t st);

@@ -313,14 +313,31 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
         const unsigned char *pbase =
             reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * 4 * nwp) + lane * 4;
         const int32_t *oc = offcur + pb * kPCC * kPDB + warp * kPDPW;
+        static_assert(kPDPW == 2, "the channel loop below handles two DM trials per warp");
+        // groups of 8 channels: the first channel of a group sets the fp16 partials, the
+        // others add to them, then the group is added into the int16x2 partials
         for (int c8 = 0; c8 < nc; c8 += 8) {
-            const int ce = min(c8 + 8, nc);
-#pragma unroll 2
-            for (int ci = c8; ci < ce; ++ci) {
-                const unsigned char *prow = pbase + (size_t)ci * 4 * ps;
-                const int2 o2 = *reinterpret_cast<const int2 *>(oc + ci * kPDB);
+            const int ng = min(8, nc - c8);
+            const unsigned char *prow = pbase + (size_t)c8 * 4 * ps;
+            const int32_t *oco = oc + c8 * kPDB;
+            {
+                const int2 o2 = *reinterpret_cast<const int2 *>(oco);
                 const uint32_t *p0 = reinterpret_cast<const uint32_t *>(prow + o2.x);
                 const uint32_t *p1 = reinterpret_cast<const uint32_t *>(prow + o2.y);
+#pragma unroll
+                for (int r = 0; r < kPR4; ++r) {
+                    const uint32_t w0 = p0[32 * r], w1 = p1[32 * r];
+                    hl[0][r] = __byte_perm(w0, 0u, 0x4240);
+                    hh[0][r] = __byte_perm(w0, 0u, 0x4341);
+                    hl[1][r] = __byte_perm(w1, 0u, 0x4240);
+                    hh[1][r] = __byte_perm(w1, 0u, 0x4341);
+                }
+            }
+            auto step = [&](int ci) {
+                const unsigned char *pr = prow + (size_t)ci * 4 * ps;
+                const int2 o2 = *reinterpret_cast<const int2 *>(oco + ci * kPDB);
+                const uint32_t *p0 = reinterpret_cast<const uint32_t *>(pr + o2.x);
+                const uint32_t *p1 = reinterpret_cast<const uint32_t *>(pr + o2.y);
 #pragma unroll
                 for (int r = 0; r < kPR4; ++r) {
                     const uint32_t w0 = p0[32 * r], w1 = p1[32 * r];
@@ -329,6 +346,13 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
                     hl[1][r] = hadd2_bits(hl[1][r], __byte_perm(w1, 0u, 0x4240));
                     hh[1][r] = hadd2_bits(hh[1][r], __byte_perm(w1, 0u, 0x4341));
                 }
+            };
+            if (ng == 8) {
+#pragma unroll
+                for (int ci = 1; ci < 8; ++ci) step(ci);
+            } else {
+#pragma unroll 1
+                for (int ci = 1; ci < ng; ++ci) step(ci);
             }
 #pragma unroll
             for (int j = 0; j < kPDPW; ++j)
@@ -336,7 +360,6 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
                 for (int r = 0; r < kPR4; ++r) {
                     il[j][r] += hl[j][r];
                     ih[j][r] += hh[j][r];
-                    hl[j][r] = hh[j][r] = 0u;
                 }
         }
         if (((k + 1) & 15) == 0 || k == nchunks - 1) {

@@ -168,6 +168,103 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def serve_passes(nchans):
+    """Subband passes over the 4096-trial plan: 16 fine DM trials per sub-DM call."""
+    out = []
+    for lo, st, n in SEGMENTS:
+        out.append(dict(lowdm=lo, highdm=lo + n * st, dmstep=st, sub_dmstep=16 * st,
+                        ncalls=n // 16, calldms=16))
+    return out
+
+
+def run_serve(args):
+    """Serving form: 64 beams (10% at 1024 channels), blocks of 2^16 uint8 samples arriving per
+    beam as Poisson streams at 1.0-1.5x real time, continuous batching on one GPU."""
+    import threading
+    import torch
+
+    from mdsm_gb300.serving import Server
+    nbeams, nsamp = args.serve_beams, 1 << 16
+    block_s = nsamp * TSAMP
+    srv = Server(hbm_budget_bytes=200 << 30, host_stage_bytes=24 << 30,
+                 max_inflight=args.serve_slots, nwidths=9, threshold=6.0, cand_cap=4096)
+    rng = np.random.default_rng(11)
+    beams, pools = [], {}
+    for b in range(nbeams):
+        nch = 1024 if b % 10 == 9 else 4096
+        if args.algo == "subband":
+            bid = srv.add_beam_subband(nch, FCH1, -BW / nch, TSAMP, nsamp, 64 if nch == 4096 else 32,
+                                       serve_passes(nch))
+        else:
+            bid = srv.add_beam(nch, FCH1, -BW / nch, TSAMP, nsamp, SEGMENTS)
+        info = srv.beam_info(bid)
+        if nch not in pools:
+            pools[nch] = (rng.integers(96, 160, (nch, nsamp + info.maxshift), dtype=np.uint8),
+                          [rng.integers(96, 160, (nch, nsamp), dtype=np.uint8) for _ in range(2)])
+        beams.append((bid, nch, info))
+    speed = rng.uniform(1.0, 1.5, nbeams) * args.serve_speed
+    events = []
+    for b in range(nbeams):
+        t = rng.exponential(block_s / speed[b]) * 0.1
+        for k in range(args.serve_blocks):
+            events.append((t, b, k))
+            t += rng.exponential(block_s / speed[b]) if np.isfinite(speed[b]) else 0.0
+    events.sort()
+    # arrivals must respect each beam's block order
+    nexts = [0] * nbeams
+    queue = {b: [] for b in range(nbeams)}
+    for t, b, k in events:
+        queue[b].append(t)
+    order = []
+    for b in range(nbeams):
+        for k, t in enumerate(sorted(queue[b])):
+            order.append((t, b, k))
+    order.sort()
+    got = []
+
+    def consumer():
+        while len(got) < len(order):
+            r = srv.poll(wait_ms=50)
+            if r is not None:
+                got.append(r)
+
+    th = threading.Thread(target=consumer)
+    th.start()
+    t0 = time.perf_counter()
+    delayed = 0
+    for t, b, k in order:
+        now = time.perf_counter() - t0
+        if np.isfinite(t) and t > now:
+            time.sleep(t - now)
+        bid, nch, info = beams[b]
+        init, regs = pools[nch]
+        blk = init if k == 0 else regs[k % 2]
+        while srv.submit(bid, blk) is None:
+            delayed += 1
+            time.sleep(0.002)
+    th.join()
+    wall = time.perf_counter() - t0
+    st = srv.stats()
+    srv.close()
+    units = sum(beams[b][2].ndms * nsamp for _, b, _ in order)
+    data_s = len(order) * block_s
+    line = {"metric": METRIC, "value": units / wall, "unit": METRIC, "n_gpus": 1,
+            "steps": len(order), "warmup": 0, "ms_per_step": wall * 1e3 / len(order),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic uint8 blocks (uniform 96-159), Poisson arrivals",
+            "config": {"workload": "serving: %d beams (10%% at 1024 ch) x 2^16-sample blocks x "
+                                   "4096 DM trials 0-2000, %s, arrivals %.1f-%.1fx real time"
+                                   % (nbeams, args.algo, args.serve_speed,
+                                      1.5 * args.serve_speed),
+                       "slots": args.serve_slots, "blocks_per_beam": args.serve_blocks},
+            "real_time_factor": data_s / wall,
+            "latency": {"p50_s": st["p50_latency_s"], "p99_s": st["p99_latency_s"],
+                        "max_s": st["max_latency_s"]},
+            "admission": {"admitted": st["admitted"], "deferred_submits": delayed},
+            "candidates": int(sum(r["ncand"] for r in got))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -176,10 +273,19 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--case", default="full", choices=["full", "small"],
-                    help="small: 2048 ch x 2^16 samples x 512 DM trials (profiling case)")
+    ap.add_argument("--case", default="full", choices=["full", "small", "serve"],
+                    help="small: 2048 ch x 2^16 samples x 512 DM trials (profiling case); "
+                         "serve: the multi-beam serving form")
+    ap.add_argument("--algo", default="subband", choices=["subband", "brute"])
+    ap.add_argument("--serve-beams", type=int, default=64)
+    ap.add_argument("--serve-blocks", type=int, default=3)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-speed", type=float, default=1.0,
+                    help="arrival speed factor over real time (inf: all at once)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.case == "serve":
+        return run_serve(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

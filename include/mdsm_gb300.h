@@ -212,6 +212,58 @@ mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, in
                                       void *stream);
 
 /* ---------------------------------------------------------------------------------------- */
+/* Serving form: a continuous-batching search server over many beams on one GPU.  Each beam   */
+/* keeps its overlap tail resident in HBM; blocks from any beam are admitted into a bounded   */
+/* set of in-flight slots (CUDA streams) as they arrive, subject to an HBM budget and a host */
+/* staging budget, and overlap on the device; each block is dedispersed and boxcar-searched */
+/* and only its candidates are copied back.  Replaces the one-stream block loop of           */
+/* src/mdsm/dedispersion_thread.cu:246-401 and the host detector thread of                   */
+/* src/mdsm/dedispersion_output.cpp:216-356.  Add every beam before the first submit.        */
+typedef struct {
+    long long hbm_budget_bytes;  /* device bytes beams and slots may hold                    */
+    long long host_stage_bytes;  /* pinned bytes of blocks waiting for a slot                */
+    int max_inflight;            /* slots (blocks on the device at once)                     */
+    int detector;                /* 1 boxcar search, 0 none                                  */
+    int nwidths;                 /* boxcar widths 1..2^(nwidths-1)                           */
+    double threshold;            /* boxcar SNR threshold                                     */
+    long long cand_cap;          /* candidates kept per block                                */
+} mdsm_server_desc;
+
+typedef struct {
+    int beam;
+    long long block;             /* block index within its beam                              */
+    long long ticket;            /* submission order over all beams                          */
+    double submit_time, done_time;  /* seconds, steady clock                                 */
+    long long ncand;             /* candidates found (may exceed cand_cap)                   */
+    int status;
+} mdsm_block_result;
+
+typedef struct {
+    long long admitted, refused, completed, held_bytes, dm_trial_samples;
+    double wall_s, p50_latency_s, p99_latency_s, max_latency_s;
+} mdsm_server_stats;
+
+typedef struct mdsm_server_s mdsm_server;
+
+mdsm_status mdsm_server_create(const mdsm_server_desc *desc, mdsm_server **out);
+mdsm_status mdsm_server_add_beam_brute(mdsm_server *sv, const mdsm_brute_desc *desc, int *beam);
+mdsm_status mdsm_server_add_beam_subband(mdsm_server *sv, const mdsm_subband_desc *desc,
+                                         int *beam);
+mdsm_status mdsm_server_beam_info(mdsm_server *sv, int beam, mdsm_plan_info *info);
+/* Block 0 of a beam holds nsamp + maxshift samples per channel, later blocks nsamp new samples
+ * (row pitch h_stride elements).  The data are copied before return.  MDSM_EBUDGET: not
+ * admitted now (staging budget full); retry after results are polled. */
+mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
+                               long long h_stride, long long *ticket);
+/* One finished block (completion order), its candidates sorted by dm then sample.
+ * MDSM_EAGAIN when none is ready within wait_ms. */
+mdsm_status mdsm_server_poll(mdsm_server *sv, mdsm_block_result *res, mdsm_candidate *cands,
+                             long long cap, int wait_ms);
+mdsm_status mdsm_server_drain(mdsm_server *sv);
+mdsm_status mdsm_server_get_stats(mdsm_server *sv, mdsm_server_stats *out);
+void mdsm_server_destroy(mdsm_server *sv);
+
+/* ---------------------------------------------------------------------------------------- */
 /* Compatibility layer: the reference stage interface (src/mdsm/dedispersion_manager.h:7-12) */
 /* with C linkage.  include/dedispersion_manager.h wraps these under the reference's C++      */
 /* names and default arguments.  Same buffer ownership, one-block latency and stop protocol.  */

@@ -137,6 +137,12 @@ SIGNATURES = {
 
 _LIB = None
 
+# serving-form entry points are bound by mdsm_gb300/serving.py
+SERVER_SYMBOLS = ("mdsm_server_create", "mdsm_server_add_beam_brute",
+                  "mdsm_server_add_beam_subband", "mdsm_server_beam_info", "mdsm_server_submit",
+                  "mdsm_server_poll", "mdsm_server_drain", "mdsm_server_get_stats",
+                  "mdsm_server_destroy")
+
 
 def load(path=None):
     """Load the library (once).  Raises if it has not been built."""

@@ -478,4 +478,78 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
     return fetch_cands(d_c, d_count, cap, h_cands, ncand, st);
 }
 
+// Bytes of device work area boxcar_launch needs.
+size_t boxcar_work_bytes(int ndms, int nsamp, long long cap)
+{
+    const int nch = (nsamp + 1023) / 1024;
+    return 256 + ((size_t)ndms * nch * sizeof(double2) + 255) / 256 * 256 +
+           ((size_t)ndms * sizeof(double2) + 255) / 256 * 256 +
+           (size_t)std::max<long long>(cap, 1) * sizeof(DevCand);
+}
+
+// The boxcar search launched on `st` without waiting: statistics, search, then asynchronous
+// copies of the candidate count and up to `cap` records into pinned host memory (h_cands holds
+// the device record layout until devcand_to_candidate() puts it in mdsm_candidate order).
+mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
+                          double threshold, void *d_work, size_t work_bytes, long long cap,
+                          mdsm_candidate *h_cands, long long *h_count, cudaStream_t st)
+{
+    if (dtype != MDSM_OUT_F32 && dtype != MDSM_OUT_I32)
+        return fail(MDSM_EINVAL, "boxcar detector: series must be float32 or int32");
+    if (nwidths < 1 || nwidths > 9) return fail(MDSM_EINVAL, "boxcar detector: widths up to 256");
+    if (work_bytes < boxcar_work_bytes(ndms, nsamp, cap))
+        return fail(MDSM_ERANGE, "boxcar detector: work area too small");
+    if (cap < 1) cap = 1;
+    const int nch = (nsamp + 1023) / 1024;
+    char *base = static_cast<char *>(d_work);
+    auto *d_count = reinterpret_cast<unsigned long long *>(base);
+    auto *d_part = reinterpret_cast<double2 *>(base + 256);
+    const size_t off_ms = 256 + ((size_t)ndms * nch * sizeof(double2) + 255) / 256 * 256;
+    auto *d_ms = reinterpret_cast<double2 *>(base + off_ms);
+    auto *d_c = reinterpret_cast<DevCand *>(base + off_ms +
+                                            ((size_t)ndms * sizeof(double2) + 255) / 256 * 256);
+    MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
+    dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
+    const int wmax = 1 << (nwidths - 1);
+    const int hl = std::max(wmax / 2, 1);
+    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 12;
+    dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
+    if (dtype == MDSM_OUT_F32) {
+        const float *y = static_cast<const float *>(d_series);
+        k_series_chunk_sums<float><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
+        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
+        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<float>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_boxcar<float><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
+                                                       d_count, cap);
+    } else {
+        const int32_t *y = static_cast<const int32_t *>(d_series);
+        k_series_chunk_sums<int32_t><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
+        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
+        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<int32_t>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        k_boxcar<int32_t><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
+                                                         d_count, cap);
+    }
+    MDSM_CUDA_TRY(cudaGetLastError());
+    MDSM_CUDA_TRY(cudaMemcpyAsync(h_count, d_count, sizeof(long long), cudaMemcpyDeviceToHost, st));
+    static_assert(sizeof(DevCand) == sizeof(mdsm_candidate), "record sizes differ");
+    MDSM_CUDA_TRY(cudaMemcpyAsync(h_cands, d_c, (size_t)cap * sizeof(DevCand),
+                                  cudaMemcpyDeviceToHost, st));
+    return MDSM_OK;
+}
+
+// Put n device-layout records (dm, sample, width, snr) into mdsm_candidate order, in place.
+void devcand_to_candidate(mdsm_candidate *c, long long n)
+{
+    for (long long i = 0; i < n; ++i) {
+        DevCand dc;
+        std::memcpy(&dc, &c[i], sizeof dc);
+        c[i].dm_idx = dc.dm_idx;
+        c[i].sample = dc.sample;
+        c[i].snr = dc.snr;
+        c[i].width = dc.width;
+    }
+}
+
 }  // namespace mdsm

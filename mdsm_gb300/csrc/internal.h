@@ -132,6 +132,11 @@ mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float
 mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
                           double threshold, mdsm_candidate *h_cands, long long cap,
                           long long *ncand, cudaStream_t st);
+size_t boxcar_work_bytes(int ndms, int nsamp, long long cap);
+mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
+                          double threshold, void *d_work, size_t work_bytes, long long cap,
+                          mdsm_candidate *h_cands, long long *h_count, cudaStream_t st);
+void devcand_to_candidate(mdsm_candidate *c, long long n);
 mdsm_status rfi_clip(void *d_x, int dtype, int nchans, long long stride, long long len,
                      double k_chan, double k_spec, cudaStream_t st);
 

@@ -1,0 +1,483 @@
+// serve.cpp -- continuous-batching search server over many beams on one GPU.
+//
+// The reference processes one stream of blocks with one worker pthread per GPU and barriers
+// (src/mdsm/dedispersion_manager.cpp:269-501, src/mdsm/dedispersion_thread.cu:246-401): block
+// k+1 is copied in only after block k's output has been copied out, the overlap tail goes
+// through host memory, and detection runs on one host thread.  Here many beams share the GPU:
+//  * each beam keeps its last maxshift samples resident in HBM (two device block buffers used
+//    in turn; the tail moves with one device-to-device copy), so only new samples cross the
+//    host link;
+//  * blocks from any beam are admitted as they arrive into a bounded set of slots (one CUDA
+//    stream each, with the slot's output and candidate buffers), subject to an HBM budget;
+//    blocks admitted while others run overlap with them on the device (copies and kernels
+//    of different slots run concurrently);
+//  * a block's pipeline is H2D of the new samples -> tail copy -> dedispersion -> boxcar
+//    search -> D2H of the candidates only (the dedispersed block stays on the device);
+//  * one dispatcher thread admits, one completion step records per-block latency (submit to
+//    candidates on the host) and returns results in completion order.
+// A beam's blocks are processed in order; different beams are independent, so a beam's
+// results are the same whether it runs alone or mixed with others.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include "internal.h"
+
+namespace mdsm {
+
+mdsm_status plan_create_brute(const mdsm_brute_desc &d, Plan &p);
+mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p);
+
+namespace {
+
+double now_s()
+{
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+        .count();
+}
+
+struct Beam {
+    mdsm_plan *plan = nullptr;
+    void *d_buf[2] = {nullptr, nullptr};
+    size_t buf_bytes = 0;
+    long long stride = 0;      // device row pitch (elements)
+    long long next_block = 0;  // blocks submitted
+    cudaEvent_t in_ready = nullptr;     // the last launched block's input (and tail) complete
+    cudaEvent_t buf_free[2] = {nullptr, nullptr};  // last reader of each block buffer done
+    size_t elem = 1;
+};
+
+struct Pending {
+    int beam;
+    long long block;
+    long long ticket;
+    double t_submit;
+    void *h_stage;  // pinned copy of the new samples [nchans][cols]
+    size_t stage_bytes;
+    long long cols;
+};
+
+struct Slot {
+    cudaStream_t st = nullptr;
+    cudaEvent_t done = nullptr;
+    void *d_out = nullptr;
+    size_t out_bytes = 0;
+    void *d_det = nullptr;  // detector work arrays + device candidates
+    size_t det_bytes = 0;
+    mdsm_candidate *h_cands = nullptr;  // pinned
+    long long *h_count = nullptr;       // pinned
+    bool busy = false;
+    Pending job{};
+};
+
+}  // namespace
+
+struct Server {
+    mdsm_server_desc desc{};
+    int device = 0;
+    std::deque<Beam> beams;  // stable addresses while beams are added
+    std::vector<Slot> slots;
+    std::deque<Pending> queue;
+    std::deque<std::pair<mdsm_block_result, std::vector<mdsm_candidate>>> results;
+    std::mutex mu;
+    std::condition_variable cv;
+    std::thread worker;
+    bool stop = false;
+    long long tickets = 0;
+    long long held_bytes = 0;     // device bytes held (beams + slots)
+    long long staged_bytes = 0;   // pinned bytes of queued blocks
+    std::vector<double> latencies;
+    long long admitted = 0, refused = 0, completed = 0, units = 0;
+    double t_first = 0, t_last = 0;
+    mdsm_status fault = MDSM_OK;
+    std::string fault_msg;
+
+    void run();
+    bool launch(Slot &s, Pending &p);
+    void harvest(Slot &s);
+};
+
+void Server::harvest(Slot &s)
+{
+    mdsm_block_result r{};
+    r.beam = s.job.beam;
+    r.block = s.job.block;
+    r.ticket = s.job.ticket;
+    r.submit_time = s.job.t_submit;
+    r.done_time = now_s();
+    r.ncand = *s.h_count;
+    r.status = MDSM_OK;
+    const long long got = std::max<long long>(0, std::min<long long>(r.ncand, desc.cand_cap));
+    devcand_to_candidate(s.h_cands, got);
+    std::vector<mdsm_candidate> c(s.h_cands, s.h_cands + got);
+    std::sort(c.begin(), c.end(), [](const mdsm_candidate &a, const mdsm_candidate &b) {
+        return a.dm_idx != b.dm_idx ? a.dm_idx < b.dm_idx : a.sample < b.sample;
+    });
+    const Plan &p = beams[r.beam].plan->p;
+    std::lock_guard<std::mutex> lk(mu);
+    latencies.push_back(r.done_time - r.submit_time);
+    completed++;
+    units += (long long)p.ndms * p.nsamp;
+    t_last = r.done_time;
+    results.emplace_back(r, std::move(c));
+    cudaFreeHost(s.job.h_stage);
+    staged_bytes -= (long long)s.job.stage_bytes;
+    s.busy = false;
+    cv.notify_all();
+}
+
+bool Server::launch(Slot &s, Pending &job)
+{
+    Beam &b = beams[job.beam];
+    Plan &p = b.plan->p;
+    const int cur = (int)(job.block & 1), prv = cur ^ 1;
+    const long long ms = p.maxshift, ns = p.nsamp;
+    const size_t E = b.elem;
+    cudaStream_t st = s.st;
+    // A beam's blocks run one after another: the previous block's input holds this block's
+    // tail, and its dedispersion must be done (the plan's intermediate buffers are per beam,
+    // and the block before it read the buffer this block overwrites).  Other beams overlap.
+    if (job.block > 0) cudaStreamWaitEvent(st, b.in_ready, 0);
+    if (job.block > 0) cudaStreamWaitEvent(st, b.buf_free[prv], 0);
+    cudaError_t e = cudaSuccess;
+    if (job.block == 0) {
+        e = cudaMemcpy2DAsync(b.d_buf[cur], b.stride * E, job.h_stage, (size_t)job.cols * E,
+                              (size_t)(ns + ms) * E, p.nchans, cudaMemcpyHostToDevice, st);
+    } else {
+        if (ms > 0)
+            e = cudaMemcpy2DAsync(b.d_buf[cur], b.stride * E,
+                                  static_cast<char *>(b.d_buf[prv]) + ns * E, b.stride * E,
+                                  (size_t)ms * E, p.nchans, cudaMemcpyDeviceToDevice, st);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(static_cast<char *>(b.d_buf[cur]) + ms * E, b.stride * E,
+                                  job.h_stage, (size_t)job.cols * E, (size_t)ns * E, p.nchans,
+                                  cudaMemcpyHostToDevice, st);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(b.in_ready, st);
+    if (e != cudaSuccess) {
+        fault = cuda_fail(e, "serving: input copy");
+        return false;
+    }
+    mdsm_status rc = plan_run_device(p, b.d_buf[cur], b.stride, b.buf_bytes, s.d_out, ns, st);
+    if (rc == MDSM_OK && cudaEventRecord(b.buf_free[cur], st) != cudaSuccess)
+        rc = fail(MDSM_ECUDA, "serving: event record");
+    if (rc == MDSM_OK && desc.detector == 1)
+        rc = boxcar_launch(s.d_out, p.out_dtype, p.ndms, (int)ns, desc.nwidths, desc.threshold,
+                           s.d_det, s.det_bytes, desc.cand_cap, s.h_cands, s.h_count, st);
+    if (rc == MDSM_OK && desc.detector != 1) {
+        *s.h_count = 0;
+    }
+    if (rc == MDSM_OK && cudaEventRecord(s.done, st) != cudaSuccess)
+        rc = fail(MDSM_ECUDA, "serving: event record");
+    if (rc != MDSM_OK) {
+        fault = rc;
+        return false;
+    }
+    s.job = job;
+    s.busy = true;
+    return true;
+}
+
+void Server::run()
+{
+    cudaSetDevice(device);
+    std::unique_lock<std::mutex> lk(mu);
+    for (;;) {
+        // completions
+        bool any_busy = false;
+        for (auto &s : slots) {
+            if (!s.busy) continue;
+            if (cudaEventQuery(s.done) == cudaSuccess) {
+                lk.unlock();
+                harvest(s);
+                lk.lock();
+            } else {
+                any_busy = true;
+            }
+        }
+        // admissions: first queued block whose beam has no earlier block still queued
+        for (auto &s : slots) {
+            if (s.busy || queue.empty() || fault != MDSM_OK) continue;
+            Pending job = queue.front();
+            queue.pop_front();
+            admitted++;
+            lk.unlock();
+            const bool ok = launch(s, job);
+            lk.lock();
+            if (!ok) {
+                fault_msg = mdsm_last_error();
+                cv.notify_all();
+            }
+        }
+        if (stop && queue.empty()) {
+            bool idle = true;
+            for (auto &s : slots) idle &= !s.busy;
+            if (idle) break;
+        }
+        if (any_busy || !queue.empty()) {
+            lk.unlock();
+            std::this_thread::sleep_for(std::chrono::microseconds(50));
+            lk.lock();
+        } else {
+            cv.wait_for(lk, std::chrono::milliseconds(5));
+        }
+    }
+}
+
+}  // namespace mdsm
+
+using namespace mdsm;
+
+struct mdsm_server_s {
+    Server s;
+};
+
+namespace {
+
+mdsm_status add_beam(mdsm_server *sv, mdsm_plan *plan, int *beam)
+{
+    Server &S = sv->s;
+    Plan &p = plan->p;
+    Beam b;
+    b.plan = plan;
+    b.elem = dtype_size(p.in_dtype);
+    b.stride = p.in_stride;
+    long long need = 0;
+    MDSM_TRY(plan_in_requirements(p, b.stride, &need));
+    b.buf_bytes = (size_t)need + 256;
+    const long long bytes = 2LL * (long long)b.buf_bytes + (long long)p.work_bytes;
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        if (S.held_bytes + bytes > S.desc.hbm_budget_bytes)
+            return fail(MDSM_EBUDGET, "HBM budget: beam needs " + std::to_string(bytes) +
+                                          " bytes, " +
+                                          std::to_string(S.desc.hbm_budget_bytes - S.held_bytes) +
+                                          " left");
+        S.held_bytes += bytes;
+    }
+    for (int i = 0; i < 2; ++i) {
+        MDSM_CUDA_TRY(cudaMalloc(&b.d_buf[i], b.buf_bytes));
+        MDSM_CUDA_TRY(cudaMemset(b.d_buf[i], 0, b.buf_bytes));
+    }
+    MDSM_CUDA_TRY(cudaEventCreateWithFlags(&b.in_ready, cudaEventDisableTiming));
+    for (int i = 0; i < 2; ++i)
+        MDSM_CUDA_TRY(cudaEventCreateWithFlags(&b.buf_free[i], cudaEventDisableTiming));
+    // slot buffers must hold this beam's output
+    const size_t out_bytes = (size_t)p.ndms * p.nsamp * 4;
+    for (auto &sl : S.slots) {
+        if (sl.out_bytes < out_bytes) {
+            if (sl.d_out) cudaFree(sl.d_out);
+            S.held_bytes += (long long)(out_bytes - sl.out_bytes);
+            MDSM_CUDA_TRY(cudaMalloc(&sl.d_out, out_bytes));
+            sl.out_bytes = out_bytes;
+        }
+        const size_t det = boxcar_work_bytes(p.ndms, p.nsamp, S.desc.cand_cap);
+        if (sl.det_bytes < det) {
+            if (sl.d_det) cudaFree(sl.d_det);
+            MDSM_CUDA_TRY(cudaMalloc(&sl.d_det, det));
+            sl.det_bytes = det;
+        }
+    }
+    std::lock_guard<std::mutex> lk(S.mu);
+    S.beams.push_back(b);
+    *beam = (int)S.beams.size() - 1;
+    return MDSM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+mdsm_status mdsm_server_create(const mdsm_server_desc *desc, mdsm_server **out)
+{
+    if (!desc || !out || desc->max_inflight <= 0 || desc->hbm_budget_bytes <= 0)
+        return fail(MDSM_EINVAL, "server: bad description");
+    if (desc->detector == 1 && (desc->nwidths < 1 || desc->nwidths > 9))
+        return fail(MDSM_EINVAL, "server: boxcar widths must be 1..9 levels");
+    mdsm_server *sv = new mdsm_server();
+    Server &S = sv->s;
+    S.desc = *desc;
+    if (S.desc.cand_cap <= 0) S.desc.cand_cap = 4096;
+    cudaGetDevice(&S.device);
+    S.slots.resize(desc->max_inflight);
+    for (auto &sl : S.slots) {
+        if (cudaStreamCreateWithFlags(&sl.st, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming) != cudaSuccess ||
+            cudaHostAlloc((void **)&sl.h_cands, (size_t)S.desc.cand_cap * sizeof(mdsm_candidate),
+                          0) != cudaSuccess ||
+            cudaHostAlloc((void **)&sl.h_count, sizeof(long long), 0) != cudaSuccess) {
+            mdsm_server_destroy(sv);
+            return fail(MDSM_ECUDA, "server: stream/event/pinned allocation failed");
+        }
+    }
+    S.worker = std::thread([&S] { S.run(); });
+    *out = sv;
+    return MDSM_OK;
+}
+
+mdsm_status mdsm_server_add_beam_brute(mdsm_server *sv, const mdsm_brute_desc *d, int *beam)
+{
+    if (!sv || !d || !beam) return fail(MDSM_EINVAL, "null argument");
+    mdsm_plan *plan = nullptr;
+    MDSM_TRY(mdsm_brute_plan_create(d, &plan));
+    mdsm_status st = add_beam(sv, plan, beam);
+    if (st != MDSM_OK) mdsm_plan_destroy(plan);
+    return st;
+}
+
+mdsm_status mdsm_server_add_beam_subband(mdsm_server *sv, const mdsm_subband_desc *d, int *beam)
+{
+    if (!sv || !d || !beam) return fail(MDSM_EINVAL, "null argument");
+    mdsm_plan *plan = nullptr;
+    MDSM_TRY(mdsm_subband_plan_create(d, &plan));
+    mdsm_status st = add_beam(sv, plan, beam);
+    if (st != MDSM_OK) mdsm_plan_destroy(plan);
+    return st;
+}
+
+mdsm_status mdsm_server_beam_info(mdsm_server *sv, int beam, mdsm_plan_info *info)
+{
+    if (!sv || beam < 0 || beam >= (int)sv->s.beams.size()) return fail(MDSM_EINVAL, "bad beam");
+    return mdsm_plan_get_info(sv->s.beams[beam].plan, info);
+}
+
+mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
+                               long long h_stride, long long *ticket)
+{
+    if (!sv || !h_block) return fail(MDSM_EINVAL, "null argument");
+    Server &S = sv->s;
+    if (beam < 0 || beam >= (int)S.beams.size()) return fail(MDSM_EINVAL, "bad beam");
+    Beam &b = S.beams[beam];
+    const Plan &p = b.plan->p;
+    const long long first = b.next_block == 0;
+    const long long cols = first ? (long long)p.nsamp + p.maxshift : p.nsamp;
+    if (h_stride < cols) return fail(MDSM_ERANGE, "block row pitch smaller than its samples");
+    const size_t bytes = (size_t)cols * p.nchans * b.elem;
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        if (S.fault != MDSM_OK) return fail(S.fault, "server stopped after a fault: " + S.fault_msg);
+        if (S.staged_bytes + (long long)bytes > S.desc.host_stage_bytes) {
+            S.refused++;
+            return fail(MDSM_EBUDGET, "admission: host staging budget full, retry later");
+        }
+        S.staged_bytes += (long long)bytes;
+    }
+    void *stage = nullptr;
+    if (cudaHostAlloc(&stage, bytes, 0) != cudaSuccess) {
+        std::lock_guard<std::mutex> lk(S.mu);
+        S.staged_bytes -= (long long)bytes;
+        return fail(MDSM_ENOMEM, "pinned staging allocation failed");
+    }
+    // copy the new samples (row pitch cols) so the caller's buffer is free on return
+    for (int c = 0; c < p.nchans; ++c)
+        std::memcpy(static_cast<char *>(stage) + (size_t)c * cols * b.elem,
+                    static_cast<const char *>(h_block) + (size_t)c * h_stride * b.elem,
+                    (size_t)cols * b.elem);
+    Pending job{beam, b.next_block, 0, now_s(), stage, bytes, cols};
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        job.ticket = S.tickets++;
+        if (S.t_first == 0) S.t_first = job.t_submit;
+        S.queue.push_back(job);
+        b.next_block++;
+    }
+    S.cv.notify_all();
+    if (ticket) *ticket = job.ticket;
+    return MDSM_OK;
+}
+
+mdsm_status mdsm_server_poll(mdsm_server *sv, mdsm_block_result *res, mdsm_candidate *cands,
+                             long long cap, int wait_ms)
+{
+    if (!sv || !res) return fail(MDSM_EINVAL, "null argument");
+    Server &S = sv->s;
+    std::unique_lock<std::mutex> lk(S.mu);
+    if (S.results.empty() && wait_ms > 0)
+        S.cv.wait_for(lk, std::chrono::milliseconds(wait_ms), [&] { return !S.results.empty(); });
+    if (S.results.empty()) {
+        if (S.fault != MDSM_OK) return fail(S.fault, "server stopped after a fault: " + S.fault_msg);
+        return MDSM_EAGAIN;
+    }
+    auto item = std::move(S.results.front());
+    S.results.pop_front();
+    *res = item.first;
+    if (cands)
+        for (long long i = 0; i < (long long)item.second.size() && i < cap; ++i)
+            cands[i] = item.second[(size_t)i];
+    return MDSM_OK;
+}
+
+mdsm_status mdsm_server_drain(mdsm_server *sv)
+{
+    if (!sv) return fail(MDSM_EINVAL, "null argument");
+    Server &S = sv->s;
+    std::unique_lock<std::mutex> lk(S.mu);
+    for (;;) {
+        bool idle = S.queue.empty();
+        for (auto &sl : S.slots) idle &= !sl.busy;
+        if (idle || S.fault != MDSM_OK) break;
+        S.cv.wait_for(lk, std::chrono::milliseconds(2));
+    }
+    return S.fault == MDSM_OK ? MDSM_OK : fail(S.fault, "server fault: " + S.fault_msg);
+}
+
+mdsm_status mdsm_server_get_stats(mdsm_server *sv, mdsm_server_stats *out)
+{
+    if (!sv || !out) return fail(MDSM_EINVAL, "null argument");
+    Server &S = sv->s;
+    std::lock_guard<std::mutex> lk(S.mu);
+    std::memset(out, 0, sizeof(*out));
+    out->admitted = S.admitted;
+    out->refused = S.refused;
+    out->completed = S.completed;
+    out->held_bytes = S.held_bytes;
+    out->dm_trial_samples = S.units;
+    out->wall_s = S.t_last > S.t_first ? S.t_last - S.t_first : 0;
+    if (!S.latencies.empty()) {
+        std::vector<double> v = S.latencies;
+        std::sort(v.begin(), v.end());
+        auto q = [&](double f) { return v[(size_t)std::min<double>(v.size() - 1, f * (v.size() - 1) + 0.5)]; };
+        out->p50_latency_s = q(0.50);
+        out->p99_latency_s = q(0.99);
+        out->max_latency_s = v.back();
+    }
+    return MDSM_OK;
+}
+
+void mdsm_server_destroy(mdsm_server *sv)
+{
+    if (!sv) return;
+    Server &S = sv->s;
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        S.stop = true;
+    }
+    S.cv.notify_all();
+    if (S.worker.joinable()) S.worker.join();
+    for (auto &sl : S.slots) {
+        if (sl.st) cudaStreamSynchronize(sl.st);
+        if (sl.st) cudaStreamDestroy(sl.st);
+        if (sl.done) cudaEventDestroy(sl.done);
+        if (sl.d_out) cudaFree(sl.d_out);
+        if (sl.d_det) cudaFree(sl.d_det);
+        if (sl.h_cands) cudaFreeHost(sl.h_cands);
+        if (sl.h_count) cudaFreeHost(sl.h_count);
+    }
+    for (auto &b : S.beams) {
+        for (int i = 0; i < 2; ++i)
+            if (b.d_buf[i]) cudaFree(b.d_buf[i]);
+        if (b.in_ready) cudaEventDestroy(b.in_ready);
+        for (int i = 0; i < 2; ++i)
+            if (b.buf_free[i]) cudaEventDestroy(b.buf_free[i]);
+        mdsm_plan_destroy(b.plan);
+    }
+    for (auto &q : S.queue) cudaFreeHost(q.h_stage);
+    delete sv;
+}
+
+}  // extern "C"

@@ -32,7 +32,8 @@ def test_every_declared_symbol_is_exported(lib):
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
     from mdsm_gb300 import _lib
-    assert set(names) <= set(_lib.SIGNATURES), set(names) - set(_lib.SIGNATURES)
+    bound = set(_lib.SIGNATURES) | set(_lib.SERVER_SYMBOLS)
+    assert set(names) <= bound, set(names) - bound
 
 
 def test_library_has_no_oracle_dependency():

@@ -203,13 +203,39 @@ mdsm_status mdsm_ref_detect_device_noalloc(const float *d_series, int ndms, int 
                                            void *stream);
 
 /* Boxcar single-pulse search (src/prototypes/singlepulse.cpp:41-146, restated): widths
- * 1,2,4..2^(nwidths-1); per-DM mean/sigma; SNR = (sum - w*mean)/(sigma*sqrt(w)); per-sample
+ * 1,2,4..2^(nwidths-1); per-DM mean/sigma in FP64; boxcar sums and SNR = (sum - w*mean) /
+ * (sigma*sqrt(w)) in FP32, explicitly rounded in a fixed order; per-sample
  * best width; non-maximum suppression with radius max(w/2,1).  d_series is [ndms][nsamp] of
  * dtype MDSM_OUT_F32 or MDSM_OUT_I32.  Candidates sorted by dm then sample. */
 mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, int ndms,
                                       int nsamp, int nwidths, double threshold,
                                       mdsm_candidate *h_cands, long long cap, long long *ncand,
                                       void *stream);
+
+/* ---------------------------------------------------------------------------------------- */
+/* Batched form: several brute-force plans (beams of uneven block length, channel count and  */
+/* DM plan) dedispersed by one persistent launch over all their (DM block, time tile) items,  */
+/* optionally with RFI clipping before and a boxcar search after; the pass can be captured  */
+/* once in a CUDA graph and replayed.  mdsm_batch_autotune times the launch shapes (one     */
+/* persistent launch walking tiles or DM blocks first, or one launch per beam) on the        */
+/* registered buffers and keeps the fastest; with MDSM_AUTOTUNE_CACHE set to a file path the */
+/* choice is cached per beam geometry.  Replaces the one-beam, one-launch-per-segment loop   */
+/* of src/mdsm/dedispersion_thread.cu:64-94,220-243.  The plans must outlive the batch.      */
+typedef struct mdsm_batch_s mdsm_batch;
+mdsm_status mdsm_batch_create(mdsm_plan *const *plans, int nbeams, mdsm_batch **out);
+mdsm_status mdsm_batch_set_buffers(mdsm_batch *b, const void *const *d_in,
+                                   const long long *in_stride, void *const *d_out,
+                                   const long long *out_stride);
+/* In-place clip of every beam's input before dedispersion (as mdsm_rfi_clip_device). */
+mdsm_status mdsm_batch_enable_clip(mdsm_batch *b, double k_chan, double k_spec);
+mdsm_status mdsm_batch_enable_detect(mdsm_batch *b, int nwidths, double threshold,
+                                     long long cap);
+mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice);
+mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream);
+int mdsm_batch_last_launches(const mdsm_batch *b);
+mdsm_status mdsm_batch_candidates(mdsm_batch *b, int beam, mdsm_candidate *out, long long cap,
+                                  long long *ncand, void *stream);
+void mdsm_batch_destroy(mdsm_batch *b);
 
 /* ---------------------------------------------------------------------------------------- */
 /* Serving form: a continuous-batching search server over many beams on one GPU.  Each beam   */

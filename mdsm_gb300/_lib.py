@@ -125,6 +125,17 @@ SIGNATURES = {
                                              ctypes.POINTER(_f), _vp]),
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
+    "mdsm_batch_create": (_st, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]),
+    "mdsm_batch_set_buffers": (_st, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_ll),
+                                     ctypes.POINTER(_vp), ctypes.POINTER(_ll)]),
+    "mdsm_batch_enable_clip": (_st, [_vp, _d, _d]),
+    "mdsm_batch_enable_detect": (_st, [_vp, _i, _d, _ll]),
+    "mdsm_batch_autotune": (_st, [_vp, _vp, ctypes.POINTER(_i)]),
+    "mdsm_batch_run": (_st, [_vp, _i, _vp]),
+    "mdsm_batch_last_launches": (_i, [_vp]),
+    "mdsm_batch_candidates": (_st, [_vp, _i, ctypes.POINTER(Candidate), _ll,
+                                    ctypes.POINTER(_ll), _vp]),
+    "mdsm_batch_destroy": (None, [_vp]),
     "mdsm_processSurveyParameters": (ctypes.POINTER(SURVEY), [ctypes.c_char_p]),
     "mdsm_initialiseMDSM": (ctypes.POINTER(_f), [ctypes.POINTER(SURVEY)]),
     "mdsm_next_chunk": (ctypes.POINTER(_f), [ctypes.c_uint, ctypes.POINTER(ctypes.c_uint), _d,

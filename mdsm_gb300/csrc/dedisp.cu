@@ -203,9 +203,12 @@ __device__ __forceinline__ uint32_t hadd2_bits(uint32_t a, uint32_t b)
     return d;
 }
 
-__global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
+// One (DM block, time tile, group) item of the packed kernel.  `kc` counts the chunks this CTA
+// has staged so far: it selects the mbarrier stage, phase parity and phase buffer, so a CTA can
+// process any number of items in a row.  Returns false if a bounded wait ran out.
+__device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long tile, int g,
+                                            unsigned char *smem, unsigned &kc)
 {
-    extern __shared__ __align__(128) unsigned char smem[];
     const int rawcap = a.rowcap;  // bytes per raw row (multiple of 16)
     const int ps = a.ps;          // bytes per phase copy (multiple of 16)
     const int nwp = ps >> 2;      // words per phase copy
@@ -216,20 +219,13 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
     int32_t *offcur = offsm + kPNR * kPCC * kPDB;                 // 2 x kPCC x kPDB
     uint32_t *P = reinterpret_cast<uint32_t *>(offcur + 2 * kPCC * kPDB);  // 2 x kPCC x 4 x nwp
 
-    const int blk = blockIdx.x, g = blockIdx.z;
-    const long long t0 = (long long)blockIdx.y * kPT;
+    const long long t0 = tile * kPT;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const unsigned char *in_g = a.in + (size_t)(g * a.in_group_stride);
     const size_t bofs = (size_t)(g * a.nblk + blk) * a.nchans;
     const int32_t *off_b = a.rel + bofs * kPDB;
     const int32_t *ss_b = a.sminspan + bofs * 2;
     const int nchunks = (a.nchans + kPCC - 1) / kPCC;
-
-    if (tid == 0) {
-        for (int s = 0; s < kPNR; ++s) mbar_init(&bars[s], 1);
-        fence_mbar_init();
-    }
-    __syncthreads();
 
     auto fill = [&](int s, int k) {
         const int c0 = k * kPCC;
@@ -256,7 +252,7 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
     };
 
     if (warp == 0)
-        for (int s = 0; s < kPNR && s < nchunks; ++s) fill(s, s);
+        for (int i = 0; i < kPNR && i < nchunks; ++i) fill((int)((kc + i) % kPNR), i);
 
     uint32_t hl[kPDPW][kPR4], hh[kPDPW][kPR4];  // fp16x2 partials (<= 8 channels)
     uint32_t il[kPDPW][kPR4], ih[kPDPW][kPR4];  // int16x2 partials (<= 256 channels)
@@ -273,9 +269,10 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
     int k = 0;
     bool aborted = false;
     for (; k < nchunks; ++k) {
-        const int s = k % kPNR;
-        const int pb = k & 1;  // phase buffer of this chunk
-        const unsigned par = (unsigned)(k / kPNR) & 1u;
+        const unsigned kk = kc + (unsigned)k;  // chunks staged by this CTA before this one
+        const int s = (int)(kk % kPNR);
+        const int pb = (int)(kk & 1u);  // phase buffer of this chunk
+        const unsigned par = (kk / kPNR) & 1u;
         const int nc = min(kPCC, a.nchans - k * kPCC);
         const bool ok = mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
         if (ok) {
@@ -377,10 +374,13 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
     }
 
     if (aborted) {
-        for (int kk = k; kk < nchunks && kk < k + kPNR; ++kk)
-            mbar_wait_bounded(&bars[kk % kPNR], (unsigned)(kk / kPNR) & 1u, nullptr, 0);
-        return;
+        for (int q = k; q < nchunks && q < k + kPNR; ++q) {
+            const unsigned qq = kc + (unsigned)q;
+            mbar_wait_bounded(&bars[qq % kPNR], (qq / kPNR) & 1u, nullptr, 0);
+        }
+        return false;
     }
+    kc += (unsigned)nchunks;
 
 #pragma unroll
     for (int j = 0; j < kPDPW; ++j) {
@@ -405,6 +405,48 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
                     if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
             }
         }
+    }
+    return true;
+}
+
+__global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    if (threadIdx.x == 0) {
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+        for (int s = 0; s < kPNR; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    unsigned kc = 0;
+    packed_tile(a, blockIdx.x, blockIdx.y, blockIdx.z, smem, kc);
+}
+
+// Persistent form over a work list: every CTA takes (beam, DM block, time tile, group) items
+// from a global counter until the list is exhausted.  Beams may differ in channels, samples
+// and DM plan; they share one staging geometry (rowcap, ps) so the shared-memory layout stays
+// fixed across items.
+__global__ void __launch_bounds__(kPNW * 32, 1)
+    k_shift_sum_u8x4_batch(const KArgs *__restrict__ beams, const int4 *__restrict__ items,
+                           int nitems, unsigned *__restrict__ counter)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int s_item;
+    if (threadIdx.x == 0) {
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+        for (int s = 0; s < kPNR; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    unsigned kc = 0;
+    for (;;) {
+        __syncthreads();  // previous item done with s_item; barriers initialised
+        if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= nitems) break;
+        const int4 w = items[it];
+        const KArgs a = beams[w.x];
+        if (!packed_tile(a, w.y, (long long)w.z, w.w, smem, kc)) break;
     }
 }
 
@@ -649,6 +691,157 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, g.smem_bytes, st));
     if (launches) *launches += 1;
     return MDSM_OK;
+}
+
+// ------------------------------------------------------------------------------------------
+// batched persistent launch over several brute-force plans
+// ------------------------------------------------------------------------------------------
+
+mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams)
+{
+    batch_release(b);
+    b.beams = beams;
+    int rawcap = 0, ps = 0;
+    for (const BatchBeam &bb : beams)
+        if (bb.g->kernel == 2) {
+            rawcap = std::max(rawcap, bb.g->rowcap);
+            ps = std::max(ps, bb.g->ps);
+        }
+    b.rawcap = rawcap;
+    b.ps = ps;
+    b.smem = rawcap ? packed_smem(rawcap, ps) : 0;
+    if (b.smem > 220 * 1024) return fail(MDSM_EINVAL, "batch: common staging does not fit");
+    // per packed beam: offsets re-expressed with the common phase stride
+    b.d_rel.assign(beams.size(), nullptr);
+    for (size_t i = 0; i < beams.size(); ++i) {
+        const StageGeom &g = *beams[i].g;
+        if (g.kernel != 2) continue;
+        std::vector<int32_t> rel(g.rel.size());
+        for (size_t j = 0; j < rel.size(); ++j) {
+            const int a = g.rel[j] / g.ps, q4 = g.rel[j] % g.ps;
+            rel[j] = a * ps + q4;
+        }
+        MDSM_CUDA_TRY(cudaMalloc(&b.d_rel[i], rel.size() * sizeof(int32_t)));
+        MDSM_CUDA_TRY(cudaMemcpy(b.d_rel[i], rel.data(), rel.size() * sizeof(int32_t),
+                                 cudaMemcpyHostToDevice));
+    }
+    MDSM_CUDA_TRY(cudaMalloc(&b.d_counter, sizeof(unsigned)));
+    MDSM_CUDA_TRY(cudaMalloc(&b.d_kargs, std::max<size_t>(1, beams.size()) * sizeof(KArgs)));
+    return MDSM_OK;
+}
+
+// Items of the packed beams, largest channel count first; within a beam all DM blocks of a
+// time tile are adjacent (tile_major) so the tile's rows are reused from L2, or all tiles of a
+// DM block are adjacent (!tile_major).
+mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in,
+                              const std::vector<long long> &in_stride,
+                              const std::vector<void *> &out,
+                              const std::vector<long long> &out_stride, unsigned *d_err,
+                              int tile_major)
+{
+    if (in.size() != b.beams.size() || out.size() != b.beams.size())
+        return fail(MDSM_EINVAL, "batch: one input and one output per beam");
+    std::vector<KArgs> ka(b.beams.size());
+    std::vector<int> order(b.beams.size());
+    for (size_t i = 0; i < order.size(); ++i) order[i] = (int)i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return b.beams[x].g->nchans > b.beams[y].g->nchans;
+    });
+    std::vector<int4> items;
+    for (size_t i = 0; i < b.beams.size(); ++i) {
+        const StageGeom &g = *b.beams[i].g;
+        b.beams[i].in = in[i];
+        b.beams[i].in_stride = in_stride[i];
+        b.beams[i].out = out[i];
+        b.beams[i].out_stride = out_stride[i];
+        if (((uintptr_t)in[i] & 15) != 0 || (in_stride[i] * (long long)dtype_size(g.in_dtype)) % 16)
+            return fail(MDSM_EINVAL, "batch: inputs must be 16-byte aligned with 16-byte pitches");
+        KArgs &a = ka[i];
+        std::memset(&a, 0, sizeof a);
+        a.in = static_cast<const unsigned char *>(in[i]);
+        a.in_stride = in_stride[i];
+        a.in_group_stride = 0;
+        a.out = static_cast<unsigned char *>(out[i]);
+        a.out_stride = out_stride[i];
+        a.out_group_stride = 0;
+        a.rel = g.kernel == 2 ? static_cast<const int32_t *>(b.d_rel[i]) : g.d_rel;
+        a.sminspan = g.d_sminspan;
+        a.nchans = g.nchans;
+        a.ndms = g.ndms;
+        a.nsamp = g.nsamp;
+        a.nblk = g.nblk;
+        a.rowcap = g.kernel == 2 ? b.rawcap : g.rowcap;
+        a.nst = g.nst;
+        a.out_i32 = g.out_i32;
+        a.ps = g.kernel == 2 ? b.ps : g.ps;
+        a.err = d_err;
+    }
+    for (int i : order) {
+        const StageGeom &g = *b.beams[i].g;
+        if (g.kernel != 2) continue;
+        const int ntiles = (g.nsamp + g.T - 1) / g.T;
+        if (tile_major) {
+            for (int t = 0; t < ntiles; ++t)
+                for (int k = 0; k < g.nblk; ++k) items.push_back(make_int4(i, k, t, 0));
+        } else {
+            for (int k = 0; k < g.nblk; ++k)
+                for (int t = 0; t < ntiles; ++t) items.push_back(make_int4(i, k, t, 0));
+        }
+    }
+    b.tile_major = tile_major;
+    b.nitems = (int)items.size();
+    if (b.d_items) cudaFree(b.d_items);
+    b.d_items = nullptr;
+    if (!items.empty()) {
+        MDSM_CUDA_TRY(cudaMalloc(&b.d_items, items.size() * sizeof(int4)));
+        MDSM_CUDA_TRY(cudaMemcpy(b.d_items, items.data(), items.size() * sizeof(int4),
+                                 cudaMemcpyHostToDevice));
+    }
+    MDSM_CUDA_TRY(cudaMemcpy(b.d_kargs, ka.data(), ka.size() * sizeof(KArgs),
+                             cudaMemcpyHostToDevice));
+    b.d_err = d_err;
+    return MDSM_OK;
+}
+
+// mode 0: one persistent launch for the packed beams (plus separate launches for the others);
+// mode 1: every beam its own launch.
+mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches)
+{
+    if (mode == 0 && b.nitems > 0) {
+        MDSM_CUDA_TRY(cudaMemsetAsync(b.d_counter, 0, sizeof(unsigned), st));
+        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_shift_sum_u8x4_batch,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)b.smem));
+        int dev = 0, sms = 0;
+        MDSM_CUDA_TRY(cudaGetDevice(&dev));
+        MDSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        const int grid = std::min(sms, b.nitems);
+        k_shift_sum_u8x4_batch<<<grid, kPNW * 32, b.smem, st>>>(
+            reinterpret_cast<const KArgs *>(b.d_kargs), reinterpret_cast<const int4 *>(b.d_items),
+            b.nitems, b.d_counter);
+        MDSM_CUDA_TRY(cudaGetLastError());
+        if (launches) *launches += 1;
+    }
+    for (const BatchBeam &bb : b.beams) {
+        if (mode == 0 && bb.g->kernel == 2) continue;
+        MDSM_TRY(launch_stage(*bb.g, bb.in, bb.in_stride, 0, bb.out, bb.out_stride, 0, b.d_err, st,
+                              launches));
+    }
+    return MDSM_OK;
+}
+
+void batch_release(BatchState &b)
+{
+    for (void *p : b.d_rel)
+        if (p) cudaFree(p);
+    b.d_rel.clear();
+    if (b.d_items) cudaFree(b.d_items);
+    if (b.d_counter) cudaFree(b.d_counter);
+    if (b.d_kargs) cudaFree(b.d_kargs);
+    b.d_items = nullptr;
+    b.d_counter = nullptr;
+    b.d_kargs = nullptr;
+    b.nitems = 0;
 }
 
 }  // namespace mdsm

@@ -350,7 +350,9 @@ constexpr int kBoxTile = 2048;   // output samples per CTA
 constexpr int kBoxHaloL = 128;   // NMS radius for the widest boxcar (256/2)
 constexpr int kBoxThreads = 256;
 
-// One CTA per (DM, tile).  Region [t0 - HL, t0 + TILE + HL + wmax - 1) is staged as doubles.
+// One CTA per (DM, tile).  Region [t0 - HL, t0 + TILE + HL + wmax - 1) is staged in float.
+// Arithmetic per sample and width is FP32 (explicitly rounded, same order as the oracle); only
+// the per-DM statistics are FP64.
 template <typename T>
 __global__ void __launch_bounds__(kBoxThreads)
     k_boxcar(const T *__restrict__ y, long long n, int nw, double threshold,
@@ -362,19 +364,21 @@ __global__ void __launch_bounds__(kBoxThreads)
     const int hl = max(wmax / 2, 1);
     const int span = kBoxTile + 2 * hl + wmax;  // staged samples
     const int nbest = kBoxTile + 2 * hl;        // positions with a best value
-    double *B = reinterpret_cast<double *>(sm);
-    double *best = B + span;
+    float *B = reinterpret_cast<float *>(sm);
+    float *best = B + span;
     int *bw = reinterpret_cast<int *>(best + nbest);
 
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
     if (!(sig > 0.0)) return;
+    const float mu_f = __double2float_rn(mu);
+    const float thr = __double2float_rn(threshold);
     const long long t0 = (long long)blockIdx.x * kBoxTile;
     const long long r0 = t0 - hl;  // series index of B[0] and best[0]
     const T *r = y + (size_t)d * n;
     for (int i = threadIdx.x; i < span; i += blockDim.x) {
         const long long t = r0 + i;
-        B[i] = (t >= 0 && t < n) ? ld_d(r, t) : 0.0;
+        B[i] = (t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
     }
     for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
         best[i] = -INFINITY;
@@ -386,11 +390,11 @@ __global__ void __launch_bounds__(kBoxThreads)
         const int w = 1 << l;
         if (l > 0) {
             const int h = w >> 1;
-            double nv[PER];
+            float nv[PER];
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
                 const int i = threadIdx.x + q * kBoxThreads;
-                nv[q] = (i + h < span) ? __dadd_rn(B[i], B[i + h]) : 0.0;
+                nv[q] = (i + h < span) ? __fadd_rn(B[i], B[i + h]) : 0.0f;
             }
             __syncthreads();
 #pragma unroll
@@ -400,12 +404,12 @@ __global__ void __launch_bounds__(kBoxThreads)
             }
             __syncthreads();
         }
-        const double wm = __dmul_rn((double)w, mu);
-        const double den = __dmul_rn(sig, __dsqrt_rn((double)w));
+        const float wm = __fmul_rn((float)w, mu_f);
+        const float den = __double2float_rn(__dmul_rn(sig, __dsqrt_rn((double)w)));
         for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
             const long long t = r0 + i;
             if (t < 0 || t + w > n) continue;
-            const double s = __ddiv_rn(__dadd_rn(B[i], -wm), den);
+            const float s = __fdiv_rn(__fsub_rn(B[i], wm), den);
             if (s > best[i]) {
                 best[i] = s;
                 bw[i] = w;
@@ -417,8 +421,8 @@ __global__ void __launch_bounds__(kBoxThreads)
         const long long t = t0 + q;
         if (t >= n) break;
         const int i = q + hl;
-        const double b = best[i];
-        if (!(b >= threshold)) continue;
+        const float b = best[i];
+        if (!(b >= thr)) continue;
         const int h = max(bw[i] / 2, 1);
         bool keep = true;
         for (int u = 1; u <= h && keep; ++u)
@@ -427,7 +431,7 @@ __global__ void __launch_bounds__(kBoxThreads)
             if (t + u <= n - 1 && !(best[i + u] <= b)) keep = false;
         if (!keep) continue;
         const unsigned long long at = atomicAdd(count, 1ull);
-        if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw[i], __double2float_rn(b)};
+        if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw[i], b};
     }
 }
 
@@ -455,7 +459,7 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
     dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
     const int wmax = 1 << (nwidths - 1);
     const int hl = std::max(wmax / 2, 1);
-    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 12;
+    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 4 + (size_t)(kBoxTile + 2 * hl) * 8;
     dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
     if (dtype == MDSM_OUT_F32) {
         const float *y = static_cast<const float *>(d_series);
@@ -512,7 +516,7 @@ mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, 
     dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
     const int wmax = 1 << (nwidths - 1);
     const int hl = std::max(wmax / 2, 1);
-    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 12;
+    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 4 + (size_t)(kBoxTile + 2 * hl) * 8;
     dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
     if (dtype == MDSM_OUT_F32) {
         const float *y = static_cast<const float *>(d_series);

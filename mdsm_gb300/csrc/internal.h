@@ -83,6 +83,37 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
                          int *launches);
 
 // ----------------------------------------------------------------------------------------
+// batched persistent launch (dedisp.cu)
+// ----------------------------------------------------------------------------------------
+struct BatchBeam {
+    const StageGeom *g = nullptr;
+    const void *in = nullptr;
+    long long in_stride = 0;
+    void *out = nullptr;
+    long long out_stride = 0;
+};
+
+struct BatchState {
+    std::vector<BatchBeam> beams;
+    std::vector<void *> d_rel;  // per packed beam: offsets with the common phase stride
+    void *d_items = nullptr;    // int4 (beam, DM block, tile, group)
+    void *d_kargs = nullptr;    // per-beam kernel arguments
+    unsigned *d_counter = nullptr;
+    unsigned *d_err = nullptr;
+    int nitems = 0, rawcap = 0, ps = 0, tile_major = 1;
+    size_t smem = 0;
+};
+
+mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams);
+mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in,
+                              const std::vector<long long> &in_stride,
+                              const std::vector<void *> &out,
+                              const std::vector<long long> &out_stride, unsigned *d_err,
+                              int tile_major);
+mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches);
+void batch_release(BatchState &b);
+
+// ----------------------------------------------------------------------------------------
 // plans
 // ----------------------------------------------------------------------------------------
 struct Plan {

@@ -320,7 +320,7 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         g2.in_dtype = zdtype;
         g2.acc_int = ai;
         g2.out_i32 = d.out_dtype == MDSM_OUT_I32;
-        g2.DPW = 4;
+        g2.DPW = calldms <= 8 ? 1 : (calldms <= 16 ? 2 : 4);  // DM block no wider than a call
         MDSM_TRY(build_stage_tables(g2, S2));
         g2.in_stride = n1p;
         g2.in_group_stride = (long long)nsubs * n1p;

@@ -439,15 +439,17 @@ long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double thresho
                        int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap)
 {
     long total = 0;
-    double *B = (double *)malloc(sizeof(double) * (size_t)n);
-    double *best = (double *)malloc(sizeof(double) * (size_t)n);
+    float *B = (float *)malloc(sizeof(float) * (size_t)n);
+    float *best = (float *)malloc(sizeof(float) * (size_t)n);
     int *bw = (int *)malloc(sizeof(int) * (size_t)n);
+    const float thr = (float)threshold;
     for (int d = 0; d < ndms; d++) {
         const double *yr = y + (long)d * n;
         double mu, sig;
         orc_series_stats(yr, n, &mu, &sig);
         if (!(sig > 0.0)) continue;
-        for (long t = 0; t < n; t++) B[t] = yr[t];
+        const float mu_f = (float)mu;
+        for (long t = 0; t < n; t++) B[t] = (float)yr[t];
         for (long t = 0; t < n; t++) { best[t] = -INFINITY; bw[t] = 0; }
         for (int l = 0; l < nw; l++) {
             long w = 1L << l;
@@ -455,15 +457,15 @@ long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double thresho
                 long h = w / 2;
                 for (long t = 0; t + w <= n; t++) B[t] = B[t] + B[t + h];
             }
-            double wm = (double)w * mu;
-            double den = sig * sqrt((double)w);
+            const float wm = (float)w * mu_f;
+            const float den = (float)(sig * sqrt((double)w));
             for (long t = 0; t + w <= n; t++) {
-                double s = (B[t] - wm) / den;
+                const float s = (B[t] - wm) / den;
                 if (s > best[t]) { best[t] = s; bw[t] = (int)w; }
             }
         }
         for (long t = 0; t < n; t++) {
-            if (!(best[t] >= threshold)) continue;
+            if (!(best[t] >= thr)) continue;
             long h = bw[t] / 2 > 1 ? bw[t] / 2 : 1;
             int keep = 1;
             long lo = t - h < 0 ? 0 : t - h, hi = t + h > n - 1 ? n - 1 : t + h;
@@ -474,7 +476,7 @@ long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double thresho
                 dm_idx[total] = d;
                 samp[total] = (int32_t)t;
                 width[total] = bw[t];
-                snr[total] = (float)best[t];
+                snr[total] = best[t];
             }
             total++;
         }

@@ -106,9 +106,11 @@ void orc_rfi_clip(void *x, int kind, int nchans, long stride, long len, double k
 /* ---- boxcar single-pulse detector (singlepulse.cpp:41-146, restated) ---- */
 /* Per-DM mean/sigma in double with a fixed chunked order (chunk = 1024 samples). */
 void orc_series_stats(const double *y, long n, double *mean, double *sigma);
-/* Widths 1,2,4..2^(nw-1); boxcar sums by pairwise doubling; SNR = (B - w*mu)/(sigma*sqrt(w));
- * per-sample best width; non-maximum suppression with radius max(w/2,1).  y is [ndms][n]
- * (double; exact copies of int32 or float series).  Returns candidates found. */
+/* Widths 1,2,4..2^(nw-1).  Per DM: mean and sigma in double (orc_series_stats); the series in
+ * float; boxcar sums by pairwise doubling in float; SNR = (B - w*mu)/den in float with
+ * den = (float)(sigma*sqrt(w)); per-sample best width (first of equals); non-maximum
+ * suppression with radius max(w/2,1).  y is [ndms][n] (double; exact copies of int32 or float
+ * series).  Returns candidates found. */
 long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double threshold,
                        int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap);
 

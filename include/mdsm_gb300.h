@@ -231,6 +231,7 @@ mdsm_status mdsm_batch_enable_clip(mdsm_batch *b, double k_chan, double k_spec);
 mdsm_status mdsm_batch_enable_detect(mdsm_batch *b, int nwidths, double threshold,
                                      long long cap);
 mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice);
+/* use_graph: the first call runs the pass and captures it; later calls replay the graph. */
 mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream);
 int mdsm_batch_last_launches(const mdsm_batch *b);
 mdsm_status mdsm_batch_candidates(mdsm_batch *b, int beam, mdsm_candidate *out, long long cap,

@@ -257,14 +257,16 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
     return MDSM_OK;
 }
 
-// One pass over all beams.  use_graph: the pass is captured into a CUDA graph on first use
-// (after one ordinary pass, which also sets kernel attributes) and replayed after that.
+// One pass over all beams.  use_graph: the first call runs the pass as ordinary launches and
+// captures it into a CUDA graph; later calls replay the graph.
 mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream)
 {
     if (!b || !b->buffers) return fail(MDSM_ESTATE, "batch: set buffers first");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (!use_graph) return pass(b, b->choice, st);
     if (!b->exec || b->graph_choice != b->choice) {
+        // This call's pass runs as ordinary launches (which also sets kernel attributes); the
+        // same pass is then captured, not executed, and replayed from the next call on.
         drop_graph(b);
         MDSM_TRY(pass(b, b->choice, st));
         MDSM_CUDA_TRY(cudaStreamSynchronize(st));
@@ -283,6 +285,7 @@ mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream)
         b->graph = g;
         MDSM_CUDA_TRY(cudaGraphInstantiate(&b->exec, b->graph, 0));
         b->graph_choice = b->choice;
+        return MDSM_OK;
     }
     MDSM_CUDA_TRY(cudaGraphLaunch(b->exec, st));
     return MDSM_OK;

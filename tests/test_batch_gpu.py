@@ -97,7 +97,13 @@ def test_batch_autotune_and_fused_clip_detect(lib, orc, cuda):
     # autotune does not clip; restore the inputs and run the fused pass once as a graph
     for x, t in zip(xs, d_in):
         t[: x.size].copy_(torch.from_numpy(x.ravel()))
-    b.run(graph=True)
+    b.run(graph=True)      # ordinary launches; the pass is captured for the next call
+    torch.cuda.synchronize()
+    for x, t in zip(xs, d_in):
+        t[: x.size].copy_(torch.from_numpy(x.ravel()))
+    for t in d_out:
+        t.zero_()
+    b.run(graph=True)      # the captured graph
     torch.cuda.synchronize()
     for k, (p, x) in enumerate(zip(plans, xs)):
         info = p.info

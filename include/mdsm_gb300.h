@@ -88,9 +88,11 @@ typedef struct {
     int kernel;      /* 0 = choose, 1 = generic smem kernel, 2 = packed 8-bit kernel */
 } mdsm_brute_desc;
 
-/* Two-stage subband plan, one or more passes with downsample 1.  Replaces the subband set-up
- * of initialiseMDSM and subband_dedispersion (src/mdsm/dedispersion_thread.cu:97-217).
- * Pass fields used: lowdm, highdm, dmstep, sub_dmstep, ncalls, calldms (binsize must be 1). */
+/* Two-stage subband plan, one or more passes.  Replaces the subband set-up of initialiseMDSM
+ * and subband_dedispersion (src/mdsm/dedispersion_thread.cu:97-217).  Pass fields used:
+ * lowdm, highdm, dmstep, sub_dmstep, ncalls, calldms, binsize.  A pass with binsize b > 1
+ * dedisperses the block summed over b samples (mdsm_downsample_device, mode 0) at tsamp*b and
+ * writes nsamp/b samples per output row; nsamp must be a multiple of every binsize. */
 typedef struct {
     int nchans;
     float fch1, foff, tsamp;
@@ -211,6 +213,42 @@ mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, in
                                       int nsamp, int nwidths, double threshold,
                                       mdsm_candidate *h_cands, long long cap, long long *ncand,
                                       void *stream);
+
+/* Time downsampling of a channel-major block: out[c][t] = f(sum_{k<b} in[c][t*b+k]) for
+ * t < len/b, f = sum (mode 0; integer samples widen: uint8 -> uint16 or int32, 16-bit -> int32),
+ * mean (mode 1) or sum/sqrt(b) (mode 2) in float32.  The reference's binning kernels
+ * (src/mdsm/dedispersion_kernel.cu:203-264, src/prototypes/binner.cu:13-71) compute the
+ * mean and sum/sqrt(b) but index channel-major blocks as interleaved. */
+mdsm_status mdsm_downsample_device(const void *d_in, int in_dtype, int nchans,
+                                   long long in_stride, long long len, int binsize, int mode,
+                                   void *d_out, int out_dtype, long long out_stride, void *stream);
+
+/* ---------------------------------------------------------------------------------------- */
+/* Sigproc filterbank ingest.                                                                */
+typedef struct {
+    int nchans, nbits, nifs, machine_id, telescope_id, data_type, nbeams, ibeam;
+    int barycentric, pulsarcentric, nbins, nsamples, nfchannels;
+    double tstart, tsamp, fch1, foff, refdm, az_start, za_start, src_raj, src_dej, period;
+    long long npuls;
+    long long header_bytes;  /* bytes before the first sample                              */
+    char source_name[81], rawdatafile[81];
+} mdsm_sigproc_header;
+
+/* src/mdsm/file_handler.cpp:33-187 (same keywords and types; an unknown keyword returns
+ * MDSM_EPARSE instead of exiting). */
+mdsm_status mdsm_sigproc_read_header(const char *path, mdsm_sigproc_header *h);
+/* Header of a dedispersed-series file, one channel of 32-bit samples
+ * (src/pelican-mdsm/modules/DedispersedDataWriter.cpp:49-63); samples are appended after. */
+mdsm_status mdsm_sigproc_write_series_header(const char *path, double fch1, double foff,
+                                             double tsamp, double tstart);
+/* Unpack nspectra time-major spectra of nchans nbits-bit samples (1/2/4 least significant
+ * field first, 16-bit unsigned, 32-bit float: file_handler.cpp:193-290) on the device and
+ * write them channel-major into d_out (uint8, uint16 or float32) at columns
+ * [col0, col0 + nspectra) of rows of out_stride elements; invert reverses the channel order
+ * (the corner turns of src/MDSM.cpp:100-125 and MdsmModule.cpp:135-151). */
+mdsm_status mdsm_unpack_device(const void *d_raw, long long nspectra, int nchans, int nbits,
+                               int invert, void *d_out, int out_dtype, long long out_stride,
+                               long long col0, void *stream);
 
 /* ---------------------------------------------------------------------------------------- */
 /* Batched form: several brute-force plans (beams of uneven block length, channel count and  */

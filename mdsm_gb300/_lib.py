@@ -86,6 +86,18 @@ class PlanInfo(ctypes.Structure):
                 ("work_bytes", ctypes.c_longlong)]
 
 
+class SigprocHeader(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("nchans", "nbits", "nifs", "machine_id",
+                                            "telescope_id", "data_type", "nbeams", "ibeam",
+                                            "barycentric", "pulsarcentric", "nbins", "nsamples",
+                                            "nfchannels")] + \
+               [(n, ctypes.c_double) for n in ("tstart", "tsamp", "fch1", "foff", "refdm",
+                                               "az_start", "za_start", "src_raj", "src_dej",
+                                               "period")] + \
+               [("npuls", ctypes.c_longlong), ("header_bytes", ctypes.c_longlong),
+                ("source_name", ctypes.c_char * 81), ("rawdatafile", ctypes.c_char * 81)]
+
+
 class Candidate(ctypes.Structure):
     _fields_ = [("dm_idx", ctypes.c_int32), ("sample", ctypes.c_int32), ("snr", ctypes.c_float),
                 ("width", ctypes.c_int32)]
@@ -125,6 +137,10 @@ SIGNATURES = {
                                              ctypes.POINTER(_f), _vp]),
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
+    "mdsm_downsample_device": (_st, [_vp, _i, _i, _ll, _ll, _i, _i, _vp, _i, _ll, _vp]),
+    "mdsm_sigproc_read_header": (_st, [ctypes.c_char_p, ctypes.POINTER(SigprocHeader)]),
+    "mdsm_sigproc_write_series_header": (_st, [ctypes.c_char_p, _d, _d, _d, _d]),
+    "mdsm_unpack_device": (_st, [_vp, _ll, _i, _i, _i, _vp, _i, _ll, _ll, _vp]),
     "mdsm_batch_create": (_st, [ctypes.POINTER(_vp), _i, ctypes.POINTER(_vp)]),
     "mdsm_batch_set_buffers": (_st, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_ll),
                                      ctypes.POINTER(_vp), ctypes.POINTER(_ll)]),

@@ -40,6 +40,8 @@ void plan_release(Plan &p)
 {
     for (auto &g : p.stages) free_stage(g);
     if (p.d_work) cudaFree(p.d_work);
+    if (p.d_ds) cudaFree(p.d_ds);
+    p.d_ds = nullptr;
     if (p.d_in) cudaFree(p.d_in);
     if (p.d_out) cudaFree(p.d_out);
     if (p.d_err) cudaFree(p.d_err);
@@ -191,7 +193,8 @@ mdsm_status mdsm_subband_shift_tables(const mdsm_subband_desc *desc, int pass, i
     std::vector<float> dms(desc->nchans), dmv;
     dmshifts_ref(desc->nchans, desc->fch1, desc->foff, dms.data());
     std::vector<int32_t> a, b;
-    subband_tables(desc->passes[pass], desc->nchans, desc->nsubs, desc->tsamp,
+    const int bsz = desc->passes[pass].binsize > 1 ? desc->passes[pass].binsize : 1;
+    subband_tables(desc->passes[pass], desc->nchans, desc->nsubs, desc->tsamp * (float)bsz,
                    desc->use_fma != 0, dms.data(), a, b, dmv);
     if (S1) std::memcpy(S1, a.data(), a.size() * sizeof(int32_t));
     if (S2) std::memcpy(S2, b.data(), b.size() * sizeof(int32_t));

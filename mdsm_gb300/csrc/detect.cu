@@ -346,6 +346,49 @@ __global__ void k_series_finish(const double2 *__restrict__ part, int ndms, int 
     musig[d] = make_double2(m, var > 0.0 ? __dsqrt_rn(var) : 0.0);
 }
 
+// Exact statistics of int32 series: one CTA per DM, int64 sum and 128-bit (hi, lo) sum of
+// squares.  Integer sums do not depend on order, so the reduction is parallel; the conversion
+// to mean and sigma is the fixed double formula the oracle uses.
+__global__ void __launch_bounds__(256)
+    k_series_stats_int(const int32_t *__restrict__ y, long long n, double2 *__restrict__ musig)
+{
+    const int d = blockIdx.x;
+    const int32_t *r = y + (size_t)d * n;
+    long long s1 = 0;
+    unsigned long long lo = 0, hi = 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const long long v = __ldg(r + i);
+        s1 += v;
+        const unsigned long long q = (unsigned long long)(v * v);
+        const unsigned long long nl = lo + q;
+        hi += (nl < lo);
+        lo = nl;
+    }
+    __shared__ long long a1[256];
+    __shared__ unsigned long long alo[256], ahi[256];
+    a1[threadIdx.x] = s1;
+    alo[threadIdx.x] = lo;
+    ahi[threadIdx.x] = hi;
+    __syncthreads();
+    for (int o = 128; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            a1[threadIdx.x] += a1[threadIdx.x + o];
+            const unsigned long long nl = alo[threadIdx.x] + alo[threadIdx.x + o];
+            ahi[threadIdx.x] += ahi[threadIdx.x + o] + (nl < alo[threadIdx.x]);
+            alo[threadIdx.x] = nl;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const double e2 = __ddiv_rn(__dadd_rn(__dmul_rn((double)ahi[0], 18446744073709551616.0),
+                                              (double)alo[0]),
+                                    (double)n);
+        const double m = __ddiv_rn((double)a1[0], (double)n);
+        const double var = __dadd_rn(e2, -__dmul_rn(m, m));
+        musig[d] = make_double2(m, var > 0.0 ? __dsqrt_rn(var) : 0.0);
+    }
+}
+
 constexpr int kBoxTile = 2048;   // output samples per CTA
 constexpr int kBoxHaloL = 128;   // NMS radius for the widest boxcar (256/2)
 constexpr int kBoxThreads = 256;
@@ -405,11 +448,11 @@ __global__ void __launch_bounds__(kBoxThreads)
             __syncthreads();
         }
         const float wm = __fmul_rn((float)w, mu_f);
-        const float den = __double2float_rn(__dmul_rn(sig, __dsqrt_rn((double)w)));
+        const float inv = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)w))));
         for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
             const long long t = r0 + i;
             if (t < 0 || t + w > n) continue;
-            const float s = __fdiv_rn(__fsub_rn(B[i], wm), den);
+            const float s = __fmul_rn(__fsub_rn(B[i], wm), inv);
             if (s > best[i]) {
                 best[i] = s;
                 bw[i] = w;
@@ -471,8 +514,7 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
                                                        d_count, cap);
     } else {
         const int32_t *y = static_cast<const int32_t *>(d_series);
-        k_series_chunk_sums<int32_t><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
-        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
+        k_series_stats_int<<<ndms, 256, 0, st>>>(y, nsamp, d_ms);
         MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<int32_t>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_boxcar<int32_t><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
@@ -528,8 +570,7 @@ mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, 
                                                        d_count, cap);
     } else {
         const int32_t *y = static_cast<const int32_t *>(d_series);
-        k_series_chunk_sums<int32_t><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
-        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
+        k_series_stats_int<<<ndms, 256, 0, st>>>(y, nsamp, d_ms);
         MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<int32_t>,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         k_boxcar<int32_t><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,

@@ -131,6 +131,11 @@ struct Plan {
     void *d_work = nullptr;
     size_t work_bytes = 0;
     std::vector<long long> pass_row0;   // first output row of each pass
+    std::vector<int> pass_bin;          // downsample factor of each pass
+    std::vector<int> pass_ds_dtype;     // sample type of its downsampled block
+    std::vector<long long> pass_ds_pitch;
+    void *d_ds = nullptr;               // downsampled block (passes with downsample > 1)
+    size_t ds_bytes = 0;
     // host-path buffers
     void *d_in = nullptr, *d_out = nullptr;
     size_t d_in_bytes = 0, d_out_bytes = 0;
@@ -168,6 +173,9 @@ mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, 
                           double threshold, void *d_work, size_t work_bytes, long long cap,
                           mdsm_candidate *h_cands, long long *h_count, cudaStream_t st);
 void devcand_to_candidate(mdsm_candidate *c, long long n);
+mdsm_status downsample(const void *in, int in_dtype, int nchans, long long in_stride,
+                       long long len, int b, int mode, void *out, int out_dtype,
+                       long long out_stride, cudaStream_t st);
 mdsm_status rfi_clip(void *d_x, int dtype, int nchans, long long stride, long long len,
                      double k_chan, double k_spec, cudaStream_t st);
 

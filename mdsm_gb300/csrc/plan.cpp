@@ -282,15 +282,27 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
     size_t zmax = 0;
     for (int pi = 0; pi < d.npasses; ++pi) {
         const SUBBAND_PASSES &ps = d.passes[pi];
-        if (ps.binsize != 1) return fail(MDSM_EINVAL, "subband plan: downsample must be 1");
+        const int bsz = std::max(1, ps.binsize);
+        if (d.nsamp % bsz != 0)
+            return fail(MDSM_EINVAL, "subband plan: nsamp must be a multiple of each downsample");
         if (ps.ncalls <= 0 || ps.calldms <= 0)
             return fail(MDSM_EINVAL, "subband plan: ncalls and calldms must be positive");
         const int ncalls = ps.ncalls, calldms = ps.calldms;
+        // a pass with downsample b dedisperses the block summed over b samples, at tsamp*b
+        // (src/mdsm/dedispersion_thread.cu:159-168,192-205)
+        const int nsb = d.nsamp / bsz;
+        const float tsb = d.tsamp * (float)bsz;
+        const int ds_dtype = bsz == 1 ? d.in_dtype
+                                      : (d.in_dtype == MDSM_U8 ? MDSM_U16
+                                                               : (d.in_dtype == MDSM_F32 ? MDSM_F32
+                                                                                         : MDSM_I32));
+        if (bsz > 257 && d.in_dtype == MDSM_U8)
+            return fail(MDSM_EINVAL, "subband plan: downsample above 257 for uint8 samples");
         std::vector<int32_t> S1, S2;
-        subband_tables(ps, d.nchans, nsubs, d.tsamp, d.use_fma != 0, dms, S1, S2, p.dm_values);
+        subband_tables(ps, d.nchans, nsubs, tsb, d.use_fma != 0, dms, S1, S2, p.dm_values);
         int m2 = 0, m1 = 0;
         for (int32_t v : S2) m2 = std::max(m2, (int)v);
-        const long long n1 = (long long)d.nsamp + m2;
+        const long long n1 = (long long)nsb + m2;
         const long long n1p = round_pitch(n1, zdtype);
         // stage 1: groups = subbands, rows = sub-DMs
         StageGeom g1;
@@ -298,7 +310,7 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         g1.ndms = ncalls;
         g1.ngroups = nsubs;
         g1.nsamp = (int)n1;
-        g1.in_dtype = d.in_dtype;
+        g1.in_dtype = ds_dtype;
         g1.acc_int = ai;
         g1.out_i32 = ai;
         g1.DPW = 4;
@@ -316,7 +328,7 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         g2.nchans = nsubs;
         g2.ndms = calldms;
         g2.ngroups = ncalls;
-        g2.nsamp = d.nsamp;
+        g2.nsamp = nsb;
         g2.in_dtype = zdtype;
         g2.acc_int = ai;
         g2.out_i32 = d.out_dtype == MDSM_OUT_I32;
@@ -331,10 +343,13 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         const size_t zwrite = (size_t)ncalls * nsubs * n1p * 4;
         const size_t zread = (size_t)stage_in_bytes(g2, n1p, (long long)nsubs * n1p);
         zmax = std::max(zmax, std::max(zwrite, zread) + 4096);
-        maxshift = std::max(maxshift, (int)(n1 - d.nsamp) + m1);
+        // original samples read: (n1 + m1) downsampled samples of bsz each
+        maxshift = std::max(maxshift, (int)((n1 - nsb + m1) * bsz));
         p.stages.push_back(std::move(g1));
         p.stages.push_back(std::move(g2));
         p.pass_row0.push_back(row0);
+        p.pass_bin.push_back(bsz);
+        p.pass_ds_dtype.push_back(ds_dtype);
         row0 += (long long)ncalls * calldms;
         if (pi == 0) {
             p.S1 = S1;
@@ -348,6 +363,26 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
     MDSM_CUDA_TRY(cudaMalloc(&p.d_work, p.work_bytes));
     MDSM_CUDA_TRY(cudaMemset(p.d_work, 0, p.work_bytes));
     p.in_stride = round_pitch((long long)p.nsamp + p.maxshift, p.in_dtype);
+    // downsampled copies of the block for passes with downsample > 1
+    size_t dsmax = 0;
+    for (size_t i = 0; i < p.pass_bin.size(); ++i) {
+        const int b = p.pass_bin[i];
+        const long long len = ((long long)p.nsamp + p.maxshift) / b;
+        const long long pitch = b == 1 ? 0 : round_pitch(len, p.pass_ds_dtype[i]);
+        p.pass_ds_pitch.push_back(pitch);
+        if (b == 1) continue;
+        const StageGeom &g1 = p.stages[2 * i];
+        const size_t need = (size_t)std::max<long long>(
+            stage_in_bytes(g1, pitch, g1.in_group_stride * pitch),
+            (long long)p.nchans * pitch * (long long)dtype_size(p.pass_ds_dtype[i]));
+        dsmax = std::max(dsmax, need + 4096);
+    }
+    if (dsmax) {
+        MDSM_CUDA_TRY(cudaMalloc(&p.d_ds, dsmax));
+        MDSM_CUDA_TRY(cudaMemset(p.d_ds, 0, dsmax));
+        p.ds_bytes = dsmax;
+        p.work_bytes += dsmax;
+    }
     return alloc_err(p);
 }
 
@@ -366,7 +401,11 @@ mdsm_status plan_in_requirements(const Plan &p, long long in_stride, long long *
     } else {
         for (size_t i = 0; i < p.stages.size(); i += 2) {
             const StageGeom &g1 = p.stages[i];
-            need = std::max(need, stage_in_bytes(g1, in_stride, g1.in_group_stride * in_stride));
+            if (p.pass_bin[i / 2] == 1)
+                need = std::max(need, stage_in_bytes(g1, in_stride, g1.in_group_stride * in_stride));
+            else  // the downsampling kernel reads whole rows of nsamp + maxshift samples
+                need = std::max(need, ((long long)(p.nchans - 1) * in_stride + p.nsamp +
+                                       p.maxshift) * (long long)dtype_size(p.in_dtype));
         }
     }
     *in_bytes = need;
@@ -391,7 +430,18 @@ mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size
     for (size_t i = 0; i < p.stages.size(); i += 2) {
         const StageGeom &g1 = p.stages[i];
         const StageGeom &g2 = p.stages[i + 1];
-        MDSM_TRY(launch_stage(g1, d_in, in_stride, g1.in_group_stride * in_stride, p.d_work,
+        const int b = p.pass_bin[i / 2];
+        const void *src = d_in;
+        long long pitch = in_stride;
+        if (b > 1) {
+            pitch = p.pass_ds_pitch[i / 2];
+            MDSM_TRY(downsample(d_in, p.in_dtype, p.nchans, in_stride,
+                                (long long)p.nsamp + p.maxshift, b, 0, p.d_ds,
+                                p.pass_ds_dtype[i / 2], pitch, st));
+            p.last_launches += 1;
+            src = p.d_ds;
+        }
+        MDSM_TRY(launch_stage(g1, src, pitch, g1.in_group_stride * pitch, p.d_work,
                               g1.out_stride, g1.out_group_stride, p.d_err, st, &p.last_launches));
         void *o = static_cast<char *>(d_out) + (size_t)p.pass_row0[i / 2] * out_stride * osz;
         MDSM_TRY(launch_stage(g2, p.d_work, g2.in_stride, g2.in_group_stride, o, out_stride,

@@ -435,8 +435,29 @@ void orc_series_stats(const double *y, long n, double *mean, double *sigma)
 /* src/prototypes/singlepulse.cpp restated: boxcars normalised by 1/sqrt(w) (:41-67), a
  * threshold (:240-245), and pruning of neighbours around the strongest response (:90-146),
  * here as a per-sample best width followed by non-maximum suppression. */
+/* Exact statistics of an integer series: sum in int64, sum of squares in 128 bits, then
+ * mean = S1/n and sigma = sqrt(S2/n - mean^2) in double, with S2 converted as
+ * hi*2^64 + lo (two roundings). */
+void orc_series_stats_int(const double *y, long n, double *mean, double *sigma)
+{
+    long long s1 = 0;
+    unsigned __int128 s2 = 0;
+    for (long i = 0; i < n; i++) {
+        long long v = (long long)y[i];
+        s1 += v;
+        s2 += (unsigned __int128)((unsigned long long)(v * v));
+    }
+    unsigned long long hi = (unsigned long long)(s2 >> 64), lo = (unsigned long long)s2;
+    double e2 = ((double)hi * 18446744073709551616.0 + (double)lo) / (double)n;
+    double m = (double)s1 / (double)n;
+    double var = e2 - m * m;
+    *mean = m;
+    *sigma = var > 0.0 ? sqrt(var) : 0.0;
+}
+
 long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double threshold,
-                       int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap)
+                       int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap,
+                       int is_int)
 {
     long total = 0;
     float *B = (float *)malloc(sizeof(float) * (size_t)n);
@@ -446,7 +467,10 @@ long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double thresho
     for (int d = 0; d < ndms; d++) {
         const double *yr = y + (long)d * n;
         double mu, sig;
-        orc_series_stats(yr, n, &mu, &sig);
+        if (is_int)
+            orc_series_stats_int(yr, n, &mu, &sig);
+        else
+            orc_series_stats(yr, n, &mu, &sig);
         if (!(sig > 0.0)) continue;
         const float mu_f = (float)mu;
         for (long t = 0; t < n; t++) B[t] = (float)yr[t];
@@ -458,9 +482,9 @@ long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double thresho
                 for (long t = 0; t + w <= n; t++) B[t] = B[t] + B[t + h];
             }
             const float wm = (float)w * mu_f;
-            const float den = (float)(sig * sqrt((double)w));
+            const float inv = (float)(1.0 / (sig * sqrt((double)w)));
             for (long t = 0; t + w <= n; t++) {
-                const float s = (B[t] - wm) / den;
+                const float s = (B[t] - wm) * inv;
                 if (s > best[t]) { best[t] = s; bw[t] = (int)w; }
             }
         }

@@ -106,13 +106,16 @@ void orc_rfi_clip(void *x, int kind, int nchans, long stride, long len, double k
 /* ---- boxcar single-pulse detector (singlepulse.cpp:41-146, restated) ---- */
 /* Per-DM mean/sigma in double with a fixed chunked order (chunk = 1024 samples). */
 void orc_series_stats(const double *y, long n, double *mean, double *sigma);
-/* Widths 1,2,4..2^(nw-1).  Per DM: mean and sigma in double (orc_series_stats); the series in
- * float; boxcar sums by pairwise doubling in float; SNR = (B - w*mu)/den in float with
- * den = (float)(sigma*sqrt(w)); per-sample best width (first of equals); non-maximum
- * suppression with radius max(w/2,1).  y is [ndms][n] (double; exact copies of int32 or float
- * series).  Returns candidates found. */
+/* Exact statistics of an integer series (int64 / 128-bit sums). */
+void orc_series_stats_int(const double *y, long n, double *mean, double *sigma);
+/* Widths 1,2,4..2^(nw-1).  Per DM: mean and sigma in double (orc_series_stats_int for integer
+ * series, orc_series_stats otherwise); the series in float; boxcar sums by pairwise doubling in
+ * float; SNR = (B - w*mu) * inv in float with inv = (float)(1/(sigma*sqrt(w))); per-sample
+ * best width (first of equals); non-maximum suppression with radius max(w/2,1).  y is
+ * [ndms][n] (double; exact copies of int32 or float series).  Returns candidates found. */
 long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double threshold,
-                       int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap);
+                       int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap,
+                       int is_int);
 
 /* ---- sigproc sample unpack (file_handler.cpp:193-290) ---- */
 long orc_unpack(const uint8_t *raw, long nbytes, int nbits, float *out);

@@ -170,7 +170,11 @@ def rfi_clip(x, length, k_chan=4.0, k_spec=4.0):
     return x
 
 
-def boxcar_detect(y, nw=9, threshold=6.0, cap=1 << 22):
+def boxcar_detect(y, nw=9, threshold=6.0, cap=1 << 22, is_int=None):
+    """is_int: exact integer statistics (default: y has an integer dtype, or every value of a
+    float array is integral)."""
+    if is_int is None:
+        is_int = np.issubdtype(np.asarray(y).dtype, np.integer)
     yd = np.ascontiguousarray(y, np.float64)
     ndms, n = yd.shape
     dm = np.empty(cap, np.int32)
@@ -178,7 +182,8 @@ def boxcar_detect(y, nw=9, threshold=6.0, cap=1 << 22):
     wd = np.empty(cap, np.int32)
     sn = np.empty(cap, np.float32)
     cnt = lib().orc_boxcar_detect(_p(yd), ndms, ctypes.c_long(n), nw, ctypes.c_double(threshold),
-                                  _p(dm), _p(sa), _p(wd), _p(sn), ctypes.c_long(cap))
+                                  _p(dm), _p(sa), _p(wd), _p(sn), ctypes.c_long(cap),
+                                  int(bool(is_int)))
     k = min(cnt, cap)
     return dm[:k].copy(), sa[:k].copy(), wd[:k].copy(), sn[:k].copy()
 

@@ -51,3 +51,22 @@ extern "C" long ref_read_block(const char *path, int nbits, float *out, unsigned
     fclose(fp);
     return n;
 }
+
+/* file_handler.cpp:56-187 on a file: the fields the tests compare. */
+extern "C" int ref_read_header(const char *path, int *ints, double *dbls, long long *total,
+                               char *source)
+{
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return -1;
+    FILE_HEADER *h = read_header(fp);
+    fclose(fp);
+    if (!h) return -2;
+    ints[0] = h->nchans; ints[1] = h->nbits; ints[2] = h->nifs; ints[3] = h->machine_id;
+    ints[4] = h->telescope_id; ints[5] = h->data_type; ints[6] = h->nbeams; ints[7] = h->ibeam;
+    dbls[0] = h->tstart; dbls[1] = h->tsamp; dbls[2] = h->fch1; dbls[3] = h->foff;
+    dbls[4] = h->src_raj; dbls[5] = h->src_dej; dbls[6] = h->refdm;
+    *total = h->total_bytes;
+    strcpy(source, h->source_name);
+    free(h);
+    return 0;
+}

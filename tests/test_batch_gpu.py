@@ -110,7 +110,7 @@ def test_batch_autotune_and_fused_clip_detect(lib, orc, cuda):
         xc = orc.rfi_clip(x.copy(), info.nsamp + info.maxshift, 4.0, 4.0)
         y = orc.dedisperse(xc, p.shift_table(), info.nsamp)
         assert np.array_equal(d_out[k].cpu().numpy(), y), k
-        dm, samp, wid, snr = orc.boxcar_detect(y.astype(np.float64), 6, 6.0)
+        dm, samp, wid, snr = orc.boxcar_detect(y, 6, 6.0)
         c = b.candidates(k)
         assert np.array_equal(c["dm_idx"], dm) and np.array_equal(c["sample"], samp)
         assert np.array_equal(c["width"], wid) and np.array_equal(c["snr"], snr)

@@ -65,7 +65,7 @@ def test_boxcar_matches_oracle(lib, orc, cuda, dtype):
         y[3, 1000:1064] += np.float32(0.9)
         y[10, 5000:5002] += np.float32(8.0)
     cands, cnt = m.boxcar_detect_device(torch.from_numpy(y).cuda(), nwidths=9, threshold=6.0)
-    dm, samp, wid, snr = orc.boxcar_detect(y.astype(np.float64), 9, 6.0)
+    dm, samp, wid, snr = orc.boxcar_detect(y, 9, 6.0)
     assert cnt == len(dm) > 0
     assert np.array_equal(cands["dm_idx"], dm)
     assert np.array_equal(cands["sample"], samp)

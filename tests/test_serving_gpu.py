@@ -73,7 +73,7 @@ def test_alone_equals_mixed_and_oracle(lib, orc, cuda):
             m = mixed[(pos, k)]
             assert np.array_equal(a, m), (pos, k)
             y = orc.dedisperse(x[:, k * nsamp:], S, nsamp)
-            dm, samp, wid, snr = orc.boxcar_detect(y.astype(np.float64), 7, 6.0)
+            dm, samp, wid, snr = orc.boxcar_detect(y, 7, 6.0)
             assert np.array_equal(a["dm_idx"], dm) and np.array_equal(a["sample"], samp)
             assert np.array_equal(a["width"], wid) and np.array_equal(a["snr"], snr)
     # the injected pulses are found

@@ -265,6 +265,116 @@ def run_serve(args):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """Batched form: 32 beams, blocks of 2^14..2^18 samples, 1024 or 4096 channels, each with
+    its own DM plan (1024-4096 trials to 500-2000), uint8; one persistent dedispersion launch
+    (plus clip before and boxcar search after) replayed as one CUDA graph, launch shape
+    chosen by the autotuner."""
+    import torch
+
+    import mdsm_gb300 as m
+    from mdsm_gb300.batch import Batch
+    rng = np.random.default_rng(4)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(7)
+    plans, d_in, d_out = [], [], []
+    for b in range(args.batch_beams):
+        nsamp = 1 << int(rng.integers(14, 19))
+        nch = int(rng.choice([1024, 4096]))
+        ndms = int(rng.integers(32, 129)) * 32
+        maxdm = float(rng.uniform(500, 2000))
+        p = m.BrutePlan(nch, FCH1, -BW / nch, TSAMP, nsamp, [(0.0, maxdm / ndms, ndms)],
+                        in_dtype="u8", out_dtype="i32")
+        t = p.alloc_input()
+        n = p.info.nchans * p.info.in_stride
+        v = torch.randn(n, generator=gen, device="cuda")
+        t[:n].copy_(torch.clamp(torch.round(v * 16 + 128), 0, 255).to(torch.uint8))
+        del v
+        plans.append(p)
+        d_in.append(t)
+        d_out.append(p.alloc_output())
+    batch = Batch(plans)
+    batch.set_buffers(d_in, d_out)
+    if args.batch_fused:
+        batch.enable_clip(4.0, 4.0)
+        batch.enable_detect(nwidths=9, threshold=6.0, cap=4096)
+    choice = batch.autotune()
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        batch.run(graph=True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.run(graph=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    units = sum(p.info.ndms * p.info.nsamp for p in plans)
+    adds = sum(float(p.info.ndms) * p.info.nsamp * p.info.nchans for p in plans)
+    packed = sum(1 for p in plans if p.info.kernel == 2)
+    data_s = sum(p.info.nsamp * TSAMP for p in plans)
+    line = {"metric": METRIC, "value": units / (ms / 1e3), "unit": METRIC, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic (seeded Gaussian uint8 on the device)",
+            "config": {"workload": "batched: %d beams, 2^14-2^18 samples, 1024/4096 ch, "
+                                   "1024-4096 DM trials to 500-2000, %s, one CUDA graph"
+                                   % (args.batch_beams, "clip+dedisperse+boxcar"
+                                      if args.batch_fused else "dedisperse"),
+                       "autotune_choice": ["persistent tile-major", "persistent DM-block-major",
+                                           "one launch per beam"][choice],
+                       "packed_beams": packed},
+            "real_time_factor": data_s / (ms / 1e3),
+            "add_rate_tadd_s": adds / (ms / 1e3) / 1e12}
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
+def run_precision(args):
+    """Precision report: INT32 and FP32 accumulation against the FP64 oracle, per sample type
+    (uint8 mean 128 sigma 16, int16 sigma 1000, float32 N(0,1)), 4096 channels, 64 DM trials."""
+    import torch
+
+    import mdsm_gb300 as m
+    from mdsm_gb300 import synth
+    from oracle import oracle as orc
+    orc.build(reference=False)
+    out = {}
+    nchans, nsamp, segs = 4096, 4096, [(0.0, 0.5, 64)]
+    for dtype in ("u8", "i16", "f32"):
+        accs = ("i32", "f32") if dtype != "f32" else ("f32",)
+        res = {}
+        for acc in accs:
+            plan = m.BrutePlan(nchans, FCH1, -BW / nchans, TSAMP, nsamp, segs, in_dtype=dtype,
+                               out_dtype="i32" if acc == "i32" else "f32", acc=acc)
+            nch, stride = plan.input_shape()
+            if dtype == "u8":
+                x = synth.gaussian_u8(nch, stride, 1)
+            elif dtype == "i16":
+                x = synth.gaussian_i16(nch, stride, 1)
+            else:
+                x = synth.gaussian_f32(nch, stride, 1)
+            d_in = plan.alloc_input()
+            d_in[: x.size].copy_(torch.from_numpy(x.ravel()))
+            d_out = plan.alloc_output()
+            plan.dedisperse_device(d_in, d_out)
+            torch.cuda.synchronize()
+            y = d_out.cpu().numpy().astype(np.float64)
+            S = plan.shift_table()
+            xf = x.astype(np.float32)
+            y64 = orc.dedisperse(xf, S, nsamp, out="f64")
+            scale = orc.dedisperse(np.abs(xf), S, nsamp, out="f64")
+            err = np.abs(y - y64)
+            res[acc] = {"max_abs": float(err.max()),
+                        "max_rel_sum_abs": float((err / np.maximum(scale, 1e-30)).max()),
+                        "max_rel_value": float((err / np.maximum(np.abs(y64), 1.0)).max()),
+                        "exact": bool(err.max() == 0.0)}
+        out[dtype] = res
+    print(json.dumps({"precision": out, "config": {"nchans": nchans, "nsamp": nsamp,
+                                                   "ndms": 64}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -273,7 +383,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
-    ap.add_argument("--case", default="full", choices=["full", "small", "serve"],
+    ap.add_argument("--case", default="full",
+                    choices=["full", "small", "serve", "batch", "precision"],
                     help="small: 2048 ch x 2^16 samples x 512 DM trials (profiling case); "
                          "serve: the multi-beam serving form")
     ap.add_argument("--algo", default="subband", choices=["subband", "brute"])
@@ -282,10 +393,16 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-speed", type=float, default=1.0,
                     help="arrival speed factor over real time (inf: all at once)")
+    ap.add_argument("--batch-beams", type=int, default=32)
+    ap.add_argument("--batch-fused", type=int, default=1)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.case == "serve":
         return run_serve(args)
+    if args.case == "batch":
+        return run_batch(args)
+    if args.case == "precision":
+        return run_precision(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -328,6 +328,13 @@ mdsm_status mdsm_server_drain(mdsm_server *sv);
 mdsm_status mdsm_server_get_stats(mdsm_server *sv, mdsm_server_stats *out);
 void mdsm_server_destroy(mdsm_server *sv);
 
+/* Detrend and normalise float series in place (src/prototypes/detrend.cu:12-100): per block
+ * of len samples of each of ndms rows of nsamp samples, subtract the least-squares line on
+ * x = -len/2 + 0.5 + i and divide by the residual rms (sums in double).  A trailing partial
+ * block is left as it is. */
+mdsm_status mdsm_detrend_normalise_device(float *d_series, int ndms, long long nsamp, int len,
+                                          void *stream);
+
 /* ---------------------------------------------------------------------------------------- */
 /* Compatibility layer: the reference stage interface (src/mdsm/dedispersion_manager.h:7-12) */
 /* with C linkage.  include/dedispersion_manager.h wraps these under the reference's C++      */

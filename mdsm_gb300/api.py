@@ -213,3 +213,11 @@ def boxcar_detect_device(series, nwidths=9, threshold=6.0, cap=1 << 20, stream=N
                                            int(nwidths), float(threshold), buf, cap,
                                            ctypes.byref(n), _stream_ptr(stream)))
     return _cands_to_array(buf, min(n.value, cap)), n.value
+
+
+def detrend_normalise_device(series, length=1024, stream=None):
+    """In-place detrend and normalise of a float32 device series [ndms][nsamp]."""
+    ndms, nsamp = series.shape
+    check(load().mdsm_detrend_normalise_device(ctypes.c_void_p(series.data_ptr()), ndms, nsamp,
+                                               int(length), _stream_ptr(stream)))
+    return series

@@ -597,4 +597,69 @@ void devcand_to_candidate(mdsm_candidate *c, long long n)
     }
 }
 
+// ---------------------------------------------------------------------------------------------
+// detrend and normalise (src/prototypes/detrend.cu:12-100): per block of len samples of each
+// DM series, fit a line on x_i = -len/2 + 0.5 + i by least squares, subtract it, divide by the
+// residual rms.  Sums in double (the prototype's are float tree reductions).
+// ---------------------------------------------------------------------------------------------
+__device__ __forceinline__ double block_sum_d(double v, double *red)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    __syncthreads();
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) t += red[i];
+    return t;
+}
+
+__global__ void __launch_bounds__(256)
+    k_detrend(float *__restrict__ y, long long n, int len)
+{
+    __shared__ double red[8];
+    float *b = y + (size_t)blockIdx.y * n + (size_t)blockIdx.x * len;
+    double sy = 0, sxy = 0, sxx = 0;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        const double x = -len / 2.0 + 0.5 + i;
+        const double v = (double)b[i];
+        sy += v;
+        sxy += x * v;
+        sxx += x * x;
+    }
+    sy = block_sum_d(sy, red);
+    sxy = block_sum_d(sxy, red);
+    sxx = block_sum_d(sxx, red);
+    const double a = sy / len, bb = sxy / sxx;
+    double ss = 0;
+    for (int i = threadIdx.x; i < len; i += blockDim.x) {
+        const double x = -len / 2.0 + 0.5 + i;
+        const float v = (float)((double)b[i] - (a + bb * x));
+        b[i] = v;
+        ss += (double)v * (double)v;
+    }
+    ss = block_sum_d(ss, red);
+    const double sd = sqrt(ss / len);
+    for (int i = threadIdx.x; i < len; i += blockDim.x) b[i] = (float)((double)b[i] / sd);
+}
+
+mdsm_status detrend_normalise(float *d_series, int ndms, long long nsamp, int len,
+                              cudaStream_t st)
+{
+    if (!d_series || ndms <= 0 || len <= 0 || nsamp < len)
+        return fail(MDSM_EINVAL, "detrend: bad arguments");
+    const long long nblk = nsamp / len;
+    if (nblk > 2147483647LL || ndms > 65535) return fail(MDSM_EINVAL, "detrend: too large");
+    k_detrend<<<dim3((unsigned)nblk, (unsigned)ndms), 256, 0, st>>>(d_series, nsamp, len);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return MDSM_OK;
+}
+
 }  // namespace mdsm
+
+extern "C" mdsm_status mdsm_detrend_normalise_device(float *d_series, int ndms, long long nsamp,
+                                                     int len, void *stream)
+{
+    return mdsm::detrend_normalise(d_series, ndms, nsamp, len, static_cast<cudaStream_t>(stream));
+}

@@ -29,9 +29,9 @@ def test_downsample_sum_mean_sqrt(lib, cuda, b):
     x = rng.integers(0, 256, (nchans, stride), dtype=np.uint8)
     nout = length // b
     want = x[:, : nout * b].reshape(nchans, nout, b).astype(np.int64).sum(axis=2)
-    got = _ds(torch, x, "u8", nchans, stride, length, b, 0, "u16", 512)
+    got = _ds(torch, x, "u8", nchans, stride, length, b, 0, "u16", 1024)
     assert np.array_equal(got[:, :nout], want) and not got[:, nout:].any()
-    got = _ds(torch, x, "u8", nchans, stride, length, b, 0, "i32", 512)
+    got = _ds(torch, x, "u8", nchans, stride, length, b, 0, "i32", 1024)
     assert np.array_equal(got[:, :nout], want)
     # mean and 1/sqrt(b) in float32: left-to-right float sums, then one multiply
     acc = np.zeros((nchans, nout), np.float32)
@@ -39,7 +39,7 @@ def test_downsample_sum_mean_sqrt(lib, cuda, b):
         acc = acc + x[:, k: nout * b: b][:, :nout].astype(np.float32)
     for mode, scale in ((1, np.float32(1.0) / np.float32(b)),
                         (2, np.float32(1.0) / np.sqrt(np.float32(b)))):
-        got = _ds(torch, x, "u8", nchans, stride, length, b, mode, "f32", 512)
+        got = _ds(torch, x, "u8", nchans, stride, length, b, mode, "f32", 1024)
         assert np.array_equal(got[:, :nout], acc * scale), mode
 
 

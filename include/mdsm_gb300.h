@@ -340,6 +340,8 @@ mdsm_status mdsm_detrend_normalise_device(float *d_series, int ndms, long long n
 /* with C linkage.  include/dedispersion_manager.h wraps these under the reference's C++      */
 /* names and default arguments.  Same buffer ownership, one-block latency and stop protocol.  */
 SURVEY *mdsm_processSurveyParameters(const char *xml_path);
+/* Returns the library-owned host input buffer, float [nchans][nsamp + maxshift]
+ * (dedispersion_manager.cpp's layout, as MDSM.cpp:113 and MdsmModule.cpp:143-149 fill it). */
 float *mdsm_initialiseMDSM(SURVEY *survey);
 float *mdsm_next_chunk(unsigned int data_read, unsigned *samples, double timestamp,
                        double blockRate, float *mean, float *rms);

@@ -27,8 +27,7 @@ def initialiseMDSM(survey):
 
 
 def _pitch(s):
-    row = s.nsamp + s.maxshift
-    return (row + 3) // 4 * 4
+    return s.nsamp + s.maxshift
 
 
 def next_chunk(data_read, timestamp=0.0, blockRate=0.0, mean=None, rms=None):

@@ -45,6 +45,11 @@ void plan_release(Plan &p)
     if (p.d_in) cudaFree(p.d_in);
     if (p.d_out) cudaFree(p.d_out);
     if (p.d_err) cudaFree(p.d_err);
+    for (cudaEvent_t e : p.seg_ev) cudaEventDestroy(e);
+    p.seg_ev.clear();
+    if (p.s_in) cudaStreamDestroy(p.s_in);
+    if (p.s_out) cudaStreamDestroy(p.s_out);
+    p.s_in = p.s_out = nullptr;
     p.d_work = p.d_in = p.d_out = nullptr;
     p.d_err = nullptr;
 }
@@ -64,6 +69,73 @@ mdsm_status ensure(void **buf, size_t *have, size_t want)
 }  // namespace mdsm
 
 using namespace mdsm;
+
+namespace {
+
+constexpr long long kHostSegMin = 16384;  // output samples per segment, at least
+constexpr int kHostSegMax = 8;            // segments per block, at most
+
+// Brute force from host buffers with the block cut into time segments: segment s's new input
+// columns are copied in on one stream, its output columns are computed on the caller's stream
+// once they have landed, and copied out on a third stream while later segments compute, so
+// the host-link copies hide behind the kernel.  Segment s computes outputs [t0, t0 + len) and
+// needs input columns [t0, t0 + len + maxshift); the copy of segment s + 1 only writes columns
+// past those.  Results are those of one launch over the whole block: every output sample is
+// computed by the same tile code from the same inputs.
+mdsm_status dedisperse_host_pipelined(Plan &p, const void *h_in, long long h_in_stride,
+                                      void *h_out, cudaStream_t st)
+{
+    const StageGeom &g = p.stages[0];
+    const long long SZ = (long long)dtype_size(p.in_dtype);
+    const long long row = (long long)p.nsamp + p.maxshift;
+    long long nseg = std::min<long long>(kHostSegMax, p.nsamp / kHostSegMin);
+    long long seg = (p.nsamp + nseg - 1) / nseg;
+    seg = (seg + 511) / 512 * 512;  // whole tiles of either kernel; 16-byte aligned offsets
+    nseg = (p.nsamp + seg - 1) / seg;
+    if (!p.s_in) MDSM_CUDA_TRY(cudaStreamCreateWithFlags(&p.s_in, cudaStreamNonBlocking));
+    if (!p.s_out) MDSM_CUDA_TRY(cudaStreamCreateWithFlags(&p.s_out, cudaStreamNonBlocking));
+    while ((long long)p.seg_ev.size() < 2 * nseg + 2) {
+        cudaEvent_t e;
+        MDSM_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        p.seg_ev.push_back(e);
+    }
+    // the previous work of the caller's stream (earlier users of d_in / d_out) comes first
+    MDSM_CUDA_TRY(cudaEventRecord(p.seg_ev[2 * nseg], st));
+    MDSM_CUDA_TRY(cudaStreamWaitEvent(p.s_in, p.seg_ev[2 * nseg], 0));
+    MDSM_CUDA_TRY(cudaStreamWaitEvent(p.s_out, p.seg_ev[2 * nseg], 0));
+    const char *hi = static_cast<const char *>(h_in);
+    char *ho = static_cast<char *>(h_out);
+    char *di = static_cast<char *>(p.d_in);
+    char *dout = static_cast<char *>(p.d_out);
+    long long done = 0;  // input columns copied so far
+    p.last_launches = 0;
+    for (long long s = 0; s < nseg; ++s) {
+        const long long t0 = s * seg;
+        const long long len = std::min(seg, (long long)p.nsamp - t0);
+        const long long hi_col = s == nseg - 1 ? row : std::min(row, t0 + len + p.maxshift);
+        if (hi_col > done) {
+            MDSM_CUDA_TRY(cudaMemcpy2DAsync(di + done * SZ, (size_t)(p.in_stride * SZ),
+                                            hi + done * SZ, (size_t)(h_in_stride * SZ),
+                                            (size_t)((hi_col - done) * SZ), (size_t)p.nchans,
+                                            cudaMemcpyHostToDevice, p.s_in));
+            done = hi_col;
+        }
+        MDSM_CUDA_TRY(cudaEventRecord(p.seg_ev[2 * s], p.s_in));
+        MDSM_CUDA_TRY(cudaStreamWaitEvent(st, p.seg_ev[2 * s], 0));
+        MDSM_TRY(launch_stage(g, di + t0 * SZ, p.in_stride, 0, dout + t0 * 4, p.nsamp, 0,
+                              p.d_err, st, &p.last_launches, len));
+        MDSM_CUDA_TRY(cudaEventRecord(p.seg_ev[2 * s + 1], st));
+        MDSM_CUDA_TRY(cudaStreamWaitEvent(p.s_out, p.seg_ev[2 * s + 1], 0));
+        MDSM_CUDA_TRY(cudaMemcpy2DAsync(ho + t0 * 4, (size_t)p.nsamp * 4, dout + t0 * 4,
+                                        (size_t)p.nsamp * 4, (size_t)len * 4, (size_t)p.ndms,
+                                        cudaMemcpyDeviceToHost, p.s_out));
+    }
+    MDSM_CUDA_TRY(cudaEventRecord(p.seg_ev[2 * nseg + 1], p.s_out));
+    MDSM_CUDA_TRY(cudaStreamWaitEvent(st, p.seg_ev[2 * nseg + 1], 0));
+    return check_err_word(p.d_err, st);
+}
+
+}  // namespace
 
 extern "C" {
 
@@ -225,6 +297,8 @@ mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_
     MDSM_TRY(ensure(&p.d_in, &p.d_in_bytes, (size_t)need + 256));
     const size_t out_bytes = (size_t)p.ndms * p.nsamp * 4;
     MDSM_TRY(ensure(&p.d_out, &p.d_out_bytes, out_bytes));
+    if (p.kind == 1 && p.nsamp >= 2 * kHostSegMin)
+        return dedisperse_host_pipelined(p, h_in, h_in_stride, h_out, st);
     MDSM_CUDA_TRY(cudaMemcpy2DAsync(p.d_in, (size_t)p.in_stride * SZ, h_in,
                                     (size_t)h_in_stride * SZ, (size_t)row * SZ,
                                     (size_t)p.nchans, cudaMemcpyHostToDevice, st));

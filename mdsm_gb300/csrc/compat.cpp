@@ -167,7 +167,8 @@ struct Instance {
     void *d_in[2] = {nullptr, nullptr};
     size_t d_in_bytes = 0;
     void *d_out = nullptr;
-    long long stride = 0;             // host and device row pitch (elements)
+    long long stride = 0;             // device row pitch (elements, 16-byte rows)
+    long long hstride = 0;            // host row pitch: nsamp + maxshift, as callers index it
     long long blocks = 0;             // blocks processed
     unsigned pending_read = 0;        // data_read given to the last next_chunk
     unsigned prev_read = 0;           // samples of the last processed block
@@ -238,7 +239,7 @@ mdsm_status process_block(unsigned data_read)
     const long long ms = p.maxshift, ns = p.nsamp;
     const int cur = (int)(g.blocks & 1), prv = cur ^ 1;
     if (g.blocks == 0) {
-        MDSM_CUDA_TRY(cudaMemcpy2DAsync(g.d_in[cur], g.stride * 4, g.h_in, g.stride * 4,
+        MDSM_CUDA_TRY(cudaMemcpy2DAsync(g.d_in[cur], g.stride * 4, g.h_in, g.hstride * 4,
                                         (size_t)(ns + ms) * 4, p.nchans, cudaMemcpyHostToDevice,
                                         g.st));
     } else {
@@ -248,7 +249,7 @@ mdsm_status process_block(unsigned data_read)
                                             (size_t)ms * 4, p.nchans, cudaMemcpyDeviceToDevice,
                                             g.st));
         MDSM_CUDA_TRY(cudaMemcpy2DAsync(static_cast<float *>(g.d_in[cur]) + ms, g.stride * 4,
-                                        g.h_in + ms, g.stride * 4, (size_t)ns * 4, p.nchans,
+                                        g.h_in + ms, g.hstride * 4, (size_t)ns * 4, p.nchans,
                                         cudaMemcpyHostToDevice, g.st));
     }
     // The host input buffer may be refilled once the copies above have run.
@@ -439,13 +440,16 @@ float *mdsm_initialiseMDSM(SURVEY *s)
     s->maxshift = (unsigned)p.maxshift;
     s->num_threads = 1;
     if (s->samplesPerChunk == 0) s->samplesPerChunk = s->nsamp;
-    g.stride = (long long)p.nsamp + p.maxshift;
+    // The host buffer keeps the reference's layout, rows of nsamp + maxshift samples
+    // (dedispersion_manager.cpp allocates it so and the callers, MDSM.cpp:113 and
+    // MdsmModule.cpp:143-149, index it so); the device copy uses the plan's padded pitch.
+    g.hstride = (long long)p.nsamp + p.maxshift;
     const long long dev_stride = p.in_stride;
     long long need = 0;
     if (plan_in_requirements(p, dev_stride, &need) != MDSM_OK) return nullptr;
-    g.stride = dev_stride;  // host pitch = device pitch (>= nsamp + maxshift)
+    g.stride = dev_stride;
     if (cudaStreamCreateWithFlags(&g.st, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaHostAlloc((void **)&g.h_in, (size_t)g.stride * p.nchans * 4, 0) != cudaSuccess ||
+        cudaHostAlloc((void **)&g.h_in, (size_t)g.hstride * p.nchans * 4, 0) != cudaSuccess ||
         cudaHostAlloc((void **)&g.h_out[0], (size_t)p.ndms * p.nsamp * 4, 0) != cudaSuccess ||
         cudaHostAlloc((void **)&g.h_out[1], (size_t)p.ndms * p.nsamp * 4, 0) != cudaSuccess ||
         cudaMalloc(&g.d_in[0], (size_t)need + 256) != cudaSuccess ||
@@ -457,7 +461,7 @@ float *mdsm_initialiseMDSM(SURVEY *s)
     }
     cudaMemset(g.d_in[0], 0, (size_t)need + 256);
     cudaMemset(g.d_in[1], 0, (size_t)need + 256);
-    memset(g.h_in, 0, (size_t)g.stride * p.nchans * 4);
+    memset(g.h_in, 0, (size_t)g.hstride * p.nchans * 4);
     g.d_in_bytes = (size_t)need + 256;
     g.live = true;
     return g.h_in;

@@ -13,11 +13,18 @@
 // mbarrier, NST stages deep, while all warps accumulate from the previous stage: each lane
 // holds DPW DMs x R samples (strided by 32) in registers, so every staged sample is reused
 // by up to Db DM trials and all shared-memory reads are bank-conflict free.
+//
+// Integer samples with FP32 accumulation (the precision form's path for sums that may not fit
+// INT32): each staged chunk of CC channels is summed exactly in INT32 and the chunk sums are
+// added into the FP32 result with Kahan compensation, so the error stays within about
+// 2 * 2^-24 * sum_c |x| however many channels are summed.  Float samples keep the plain
+// sequential FP32 sum of the reference kernels.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "internal.h"
 #include "ptx.cuh"
@@ -110,11 +117,21 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
     if (warp == 0)
         for (int s = 0; s < nst && s < nchunks; ++s) fill(s, s);
 
-    TAcc acc[DPW][R];
+    // Integer samples summed in FP32: exact INT32 chunk sums, Kahan-compensated across chunks.
+    constexpr bool kSplit = std::is_same<TAcc, float>::value && !std::is_same<TIn, float>::value;
+    using TPart = typename std::conditional<kSplit, int, TAcc>::type;
+    TPart acc[DPW][R];
+    float ksum[kSplit ? DPW : 1][R], kcomp[kSplit ? DPW : 1][R];
 #pragma unroll
     for (int j = 0; j < DPW; ++j)
 #pragma unroll
-        for (int r = 0; r < R; ++r) acc[j][r] = TAcc(0);
+        for (int r = 0; r < R; ++r) acc[j][r] = TPart(0);
+    if constexpr (kSplit) {
+#pragma unroll
+        for (int j = 0; j < DPW; ++j)
+#pragma unroll
+            for (int r = 0; r < R; ++r) ksum[j][r] = kcomp[j][r] = 0.0f;
+    }
 
     int k = 0;
     bool aborted = false;
@@ -135,8 +152,20 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
                 for (int j = 0; j < DPW; ++j) {
                     const TIn *p = row + rs[ci * DB + j];
 #pragma unroll
-                    for (int r = 0; r < R; ++r) acc[j][r] += static_cast<TAcc>(p[32 * r]);
+                    for (int r = 0; r < R; ++r) acc[j][r] += static_cast<TPart>(p[32 * r]);
                 }
+            }
+            if constexpr (kSplit) {
+#pragma unroll
+                for (int j = 0; j < DPW; ++j)
+#pragma unroll
+                    for (int r = 0; r < R; ++r) {
+                        const float y = __fsub_rn((float)acc[j][r], kcomp[j][r]);
+                        const float t = __fadd_rn(ksum[j][r], y);
+                        kcomp[j][r] = __fsub_rn(__fsub_rn(t, ksum[j][r]), y);
+                        ksum[j][r] = t;
+                        acc[j][r] = 0;
+                    }
             }
         }
         if (__syncthreads_or(!ok)) {
@@ -166,7 +195,11 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 #pragma unroll
         for (int r = 0; r < R; ++r) {
             const long long t = t0 + lane + 32 * r;
-            if (t < a.nsamp) store_out<TAcc>(orow, (int)t, acc[j][r], a.out_i32);
+            if (t >= a.nsamp) continue;
+            if constexpr (kSplit)
+                store_out<float>(orow, (int)t, __fsub_rn(ksum[j][r], kcomp[j][r]), a.out_i32);
+            else
+                store_out<TAcc>(orow, (int)t, acc[j][r], a.out_i32);
         }
     }
 }
@@ -180,13 +213,13 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 //  * each staged row is expanded once into four phase copies, P_a[j] = bytes 4j+a .. 4j+a+3,
 //    so any run of 4 samples starting at any offset is one aligned word, and a warp's 32
 //    lanes read 32 consecutive words (no bank conflicts);
-//  * PRMT splits a word into (s0, s2) and (s1, s3) zero-extended 16-bit lanes;
-//  * those lanes are added with HADD2 (fp16x2, on the FMA pipe): a 16-bit pattern v < 2048
-//    is the fp16 number v * 2^-24 (subnormal below 1024, exponent 1 above), sums of such
-//    numbers below 2048 * 2^-24 are exact, so the bit pattern stays the integer sum;
-//  * every 8 channels (8 * 255 < 2048) the fp16 lanes are added as integers into int16x2
-//    accumulators, every 256 channels (32 * 2040 < 65536) those into int32.
-// Per 4 sample-adds: 1 LDS, 2 PRMT, 2 HADD2 and a fraction of an IADD.
+//  * the raw words are summed as 32-bit integers, A = sum w (mod 2^32), and one PRMT per word
+//    extracts the odd samples as zero-extended 16-bit lanes, O = sum (s1 | s3 << 16);
+//  * since w = (s0 | s2 << 16) + 2^8 (s1 | s3 << 16), E = A - 2^8 O = sum (s0 | s2 << 16)
+//    (mod 2^32); over at most 256 channels every lane sum is <= 256 * 255 < 2^16, so E and O
+//    hold the four sums exactly and are added into int32 every 256 channels;
+//  * two channels share each 3-input integer add (A += wa + wz, O += odd(wa) + odd(wz)).
+// Per 4 sample-adds per channel: 1 LDS, 1 PRMT and one 3-input add.
 // ------------------------------------------------------------------------------------------
 constexpr int kPNW = 16;            // warps
 constexpr int kPDPW = 2;            // DM trials per warp
@@ -195,13 +228,6 @@ constexpr int kPCC = 16;            // channels per stage
 constexpr int kPNR = 3;             // raw stages in flight
 constexpr int kPT = 128 * kPR4;     // samples per tile (512)
 constexpr int kPDB = kPNW * kPDPW;  // DM trials per tile (32)
-
-__device__ __forceinline__ uint32_t hadd2_bits(uint32_t a, uint32_t b)
-{
-    uint32_t d;
-    asm("add.rn.f16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
-    return d;
-}
 
 // One (DM block, time tile, group) item of the packed kernel.  `kc` counts the chunks this CTA
 // has staged so far: it selects the mbarrier stage, phase parity and phase buffer, so a CTA can
@@ -254,14 +280,14 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
     if (warp == 0)
         for (int i = 0; i < kPNR && i < nchunks; ++i) fill((int)((kc + i) % kPNR), i);
 
-    uint32_t hl[kPDPW][kPR4], hh[kPDPW][kPR4];  // fp16x2 partials (<= 8 channels)
-    uint32_t il[kPDPW][kPR4], ih[kPDPW][kPR4];  // int16x2 partials (<= 256 channels)
-    int32_t f[kPDPW][kPR4][4];                  // int32 sums
+    uint32_t A[kPDPW][kPR4];  // raw 4-sample words summed mod 2^32 (<= 256 channels)
+    uint32_t O[kPDPW][kPR4];  // odd samples (s1, s3) as uint16 lanes (<= 256 channels)
+    int32_t f[kPDPW][kPR4][4];  // int32 sums
 #pragma unroll
     for (int j = 0; j < kPDPW; ++j)
 #pragma unroll
         for (int r = 0; r < kPR4; ++r) {
-            hl[j][r] = hh[j][r] = il[j][r] = ih[j][r] = 0u;
+            A[j][r] = O[j][r] = 0u;
 #pragma unroll
             for (int e = 0; e < 4; ++e) f[j][r][e] = 0;
         }
@@ -311,64 +337,63 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
             reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * 4 * nwp) + lane * 4;
         const int32_t *oc = offcur + pb * kPCC * kPDB + warp * kPDPW;
         static_assert(kPDPW == 2, "the channel loop below handles two DM trials per warp");
-        // groups of 8 channels: the first channel of a group sets the fp16 partials, the
-        // others add to them, then the group is added into the int16x2 partials
-        for (int c8 = 0; c8 < nc; c8 += 8) {
-            const int ng = min(8, nc - c8);
-            const unsigned char *prow = pbase + (size_t)c8 * 4 * ps;
-            const int32_t *oco = oc + c8 * kPDB;
-            {
-                const int2 o2 = *reinterpret_cast<const int2 *>(oco);
-                const uint32_t *p0 = reinterpret_cast<const uint32_t *>(prow + o2.x);
-                const uint32_t *p1 = reinterpret_cast<const uint32_t *>(prow + o2.y);
+        // Two channels per step: A += wa + wz and O += odd(wa) + odd(wz) are one 3-input
+        // integer add each.
+        int ci = 0;
+        auto pair = [&](int c) {
+            const unsigned char *pa = pbase + (size_t)c * 4 * ps;
+            const unsigned char *pz = pa + 4 * ps;
+            const int2 oa = *reinterpret_cast<const int2 *>(oc + c * kPDB);
+            const int2 oz = *reinterpret_cast<const int2 *>(oc + (c + 1) * kPDB);
+            const uint32_t *a0 = reinterpret_cast<const uint32_t *>(pa + oa.x);
+            const uint32_t *a1 = reinterpret_cast<const uint32_t *>(pa + oa.y);
+            const uint32_t *z0 = reinterpret_cast<const uint32_t *>(pz + oz.x);
+            const uint32_t *z1 = reinterpret_cast<const uint32_t *>(pz + oz.y);
 #pragma unroll
-                for (int r = 0; r < kPR4; ++r) {
-                    const uint32_t w0 = p0[32 * r], w1 = p1[32 * r];
-                    hl[0][r] = __byte_perm(w0, 0u, 0x4240);
-                    hh[0][r] = __byte_perm(w0, 0u, 0x4341);
-                    hl[1][r] = __byte_perm(w1, 0u, 0x4240);
-                    hh[1][r] = __byte_perm(w1, 0u, 0x4341);
-                }
+            for (int r = 0; r < kPR4; ++r) {
+                const uint32_t wa0 = a0[32 * r], wa1 = a1[32 * r];
+                const uint32_t wz0 = z0[32 * r], wz1 = z1[32 * r];
+                A[0][r] += wa0 + wz0;
+                O[0][r] += __byte_perm(wa0, 0u, 0x4341) + __byte_perm(wz0, 0u, 0x4341);
+                A[1][r] += wa1 + wz1;
+                O[1][r] += __byte_perm(wa1, 0u, 0x4341) + __byte_perm(wz1, 0u, 0x4341);
             }
-            auto step = [&](int ci) {
-                const unsigned char *pr = prow + (size_t)ci * 4 * ps;
-                const int2 o2 = *reinterpret_cast<const int2 *>(oco + ci * kPDB);
-                const uint32_t *p0 = reinterpret_cast<const uint32_t *>(pr + o2.x);
-                const uint32_t *p1 = reinterpret_cast<const uint32_t *>(pr + o2.y);
+        };
+        if (nc == kPCC) {
 #pragma unroll
-                for (int r = 0; r < kPR4; ++r) {
-                    const uint32_t w0 = p0[32 * r], w1 = p1[32 * r];
-                    hl[0][r] = hadd2_bits(hl[0][r], __byte_perm(w0, 0u, 0x4240));
-                    hh[0][r] = hadd2_bits(hh[0][r], __byte_perm(w0, 0u, 0x4341));
-                    hl[1][r] = hadd2_bits(hl[1][r], __byte_perm(w1, 0u, 0x4240));
-                    hh[1][r] = hadd2_bits(hh[1][r], __byte_perm(w1, 0u, 0x4341));
-                }
-            };
-            if (ng == 8) {
-#pragma unroll
-                for (int ci = 1; ci < 8; ++ci) step(ci);
-            } else {
+            for (int c = 0; c < kPCC; c += 2) pair(c);
+            ci = kPCC;
+        } else {
 #pragma unroll 1
-                for (int ci = 1; ci < ng; ++ci) step(ci);
+            for (; ci + 1 < nc; ci += 2) pair(ci);
+        }
+        if (ci < nc) {  // odd channel count: the last channel alone
+            const unsigned char *pa = pbase + (size_t)ci * 4 * ps;
+            const int2 oa = *reinterpret_cast<const int2 *>(oc + ci * kPDB);
+            const uint32_t *a0 = reinterpret_cast<const uint32_t *>(pa + oa.x);
+            const uint32_t *a1 = reinterpret_cast<const uint32_t *>(pa + oa.y);
+#pragma unroll
+            for (int r = 0; r < kPR4; ++r) {
+                const uint32_t wa0 = a0[32 * r], wa1 = a1[32 * r];
+                A[0][r] += wa0;
+                O[0][r] += __byte_perm(wa0, 0u, 0x4341);
+                A[1][r] += wa1;
+                O[1][r] += __byte_perm(wa1, 0u, 0x4341);
             }
-#pragma unroll
-            for (int j = 0; j < kPDPW; ++j)
-#pragma unroll
-                for (int r = 0; r < kPR4; ++r) {
-                    il[j][r] += hl[j][r];
-                    ih[j][r] += hh[j][r];
-                }
         }
         if (((k + 1) & 15) == 0 || k == nchunks - 1) {
+            // A = E + 2^8 O (mod 2^32) with E = (s0, s2) as uint16 lanes: every lane sum is at
+            // most 256 * 255 < 2^16, so E and O hold the four sums exactly.
 #pragma unroll
             for (int j = 0; j < kPDPW; ++j)
 #pragma unroll
                 for (int r = 0; r < kPR4; ++r) {
-                    f[j][r][0] += (int32_t)(il[j][r] & 0xFFFFu);
-                    f[j][r][2] += (int32_t)(il[j][r] >> 16);
-                    f[j][r][1] += (int32_t)(ih[j][r] & 0xFFFFu);
-                    f[j][r][3] += (int32_t)(ih[j][r] >> 16);
-                    il[j][r] = ih[j][r] = 0u;
+                    const uint32_t E = A[j][r] - (O[j][r] << 8);
+                    f[j][r][0] += (int32_t)(E & 0xFFFFu);
+                    f[j][r][2] += (int32_t)(E >> 16);
+                    f[j][r][1] += (int32_t)(O[j][r] & 0xFFFFu);
+                    f[j][r][3] += (int32_t)(O[j][r] >> 16);
+                    A[j][r] = O[j][r] = 0u;
                 }
         }
     }
@@ -652,9 +677,11 @@ long long stage_in_bytes(const StageGeom &g, long long in_stride, long long in_g
 mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride,
                          long long in_group_stride, void *out, long long out_stride,
                          long long out_group_stride, unsigned *d_err, cudaStream_t st,
-                         int *launches)
+                         int *launches, long long nsamp_run)
 {
     const int SZ = (int)dtype_size(g.in_dtype);
+    const long long nsamp = nsamp_run >= 0 ? std::min<long long>(nsamp_run, g.nsamp) : g.nsamp;
+    if (nsamp == 0) return MDSM_OK;
     if (((uintptr_t)in & 15) != 0) return fail(MDSM_EINVAL, "input must be 16-byte aligned");
     if ((in_stride * SZ) % 16 != 0)
         return fail(MDSM_EINVAL, "input row pitch must be a multiple of 16 bytes");
@@ -675,14 +702,14 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     a.sminspan = g.d_sminspan;
     a.nchans = g.nchans;
     a.ndms = g.ndms;
-    a.nsamp = g.nsamp;
+    a.nsamp = (int)nsamp;
     a.nblk = g.nblk;
     a.rowcap = g.rowcap;
     a.nst = g.nst;
     a.out_i32 = g.out_i32;
     a.ps = g.ps;
     a.err = d_err;
-    const long long ntiles = (g.nsamp + g.T - 1) / g.T;
+    const long long ntiles = (nsamp + g.T - 1) / g.T;
     if (ntiles > 65535 || g.ngroups > 65535)
         return fail(MDSM_EINVAL, "block too long for one launch");
     dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);

@@ -77,10 +77,12 @@ void free_stage(StageGeom &g);
 // Bytes of input (from the group base) the kernel may read for in_stride, with tile overrun.
 long long stage_in_bytes(const StageGeom &g, long long in_stride, long long in_group_stride);
 // Launch the stage kernel.  Returns number of kernels launched via *launches.
+// nsamp_run >= 0 computes only output samples [0, nsamp_run) (a time segment of the block,
+// with in/out already offset to its first sample); -1 computes all g.nsamp.
 mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride,
                          long long in_group_stride, void *out, long long out_stride,
                          long long out_group_stride, unsigned *d_err, cudaStream_t st,
-                         int *launches);
+                         int *launches, long long nsamp_run = -1);
 
 // ----------------------------------------------------------------------------------------
 // batched persistent launch (dedisp.cu)
@@ -139,6 +141,9 @@ struct Plan {
     // host-path buffers
     void *d_in = nullptr, *d_out = nullptr;
     size_t d_in_bytes = 0, d_out_bytes = 0;
+    // host path, brute force: copy-in and copy-out streams and per-segment events
+    cudaStream_t s_in = nullptr, s_out = nullptr;
+    std::vector<cudaEvent_t> seg_ev;
     unsigned *d_err = nullptr;
     int last_launches = 0;
     long long in_stride = 0;         // device pitch for the host path

@@ -177,6 +177,16 @@ def serve_passes(nchans):
     return out
 
 
+def block_adds(algo, nchans, nsamp):
+    """Algorithmic adds of one block: brute force nchans per DM-trial-sample; subband, per
+    output sample, ncalls * nchans for stage 1 plus ndms * nsubs for stage 2 per pass."""
+    if algo != "subband":
+        return sum(n for _, _, n in SEGMENTS) * nchans * nsamp
+    nsubs = 64 if nchans == 4096 else 32
+    return sum(p["ncalls"] * nchans + p["ncalls"] * p["calldms"] * nsubs
+               for p in serve_passes(nchans)) * nsamp
+
+
 def run_serve(args):
     """Serving form: 64 beams (10% at 1024 channels), blocks of 2^16 uint8 samples arriving per
     beam as Poisson streams at 1.0-1.5x real time, continuous batching on one GPU."""
@@ -247,6 +257,7 @@ def run_serve(args):
     st = srv.stats()
     srv.close()
     units = sum(beams[b][2].ndms * nsamp for _, b, _ in order)
+    adds = sum(block_adds(args.algo, beams[b][1], nsamp) for _, b, _ in order)
     data_s = len(order) * block_s
     line = {"metric": METRIC, "value": units / wall, "unit": METRIC, "n_gpus": 1,
             "steps": len(order), "warmup": 0, "ms_per_step": wall * 1e3 / len(order),
@@ -261,7 +272,76 @@ def run_serve(args):
             "latency": {"p50_s": st["p50_latency_s"], "p99_s": st["p99_latency_s"],
                         "max_s": st["max_latency_s"]},
             "admission": {"admitted": st["admitted"], "deferred_submits": delayed},
+            "algorithmic_adds_per_unit": adds / units, "add_rate_tadd_s": adds / wall / 1e12,
+            "slowest_blocks": [[r["beam"], r["block"], r["ticket"], round(r["latency_s"], 4)]
+                               for r in sorted(got, key=lambda r: -r["latency_s"])[:6]],
             "candidates": int(sum(r["ncand"] for r in got))}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve_plain(args):
+    """The serving workload through the plain per-block path, for the serving form's ratio:
+    64 beams' blocks one after another on one stream, each block copied in whole (tail
+    included, from pinned host memory), dedispersed, searched with the same boxcar detector,
+    and its candidates read back before the next block starts."""
+    import torch
+
+    import mdsm_gb300 as m
+    nbeams, nsamp = args.serve_beams, 1 << 16
+    block_s = nsamp * TSAMP
+    rng = np.random.default_rng(11)
+    plans = {}
+    for nch in (4096, 1024):
+        if args.algo == "subband":
+            plans[nch] = m.SubbandPlan(nch, FCH1, -BW / nch, TSAMP, nsamp,
+                                       64 if nch == 4096 else 32, serve_passes(nch),
+                                       in_dtype="u8", out_dtype="i32")
+        else:
+            plans[nch] = m.BrutePlan(nch, FCH1, -BW / nch, TSAMP, nsamp, SEGMENTS,
+                                     in_dtype="u8", out_dtype="i32")
+    bufs = {}
+    for nch, p in plans.items():
+        i = p.info
+        h = torch.from_numpy(rng.integers(96, 160, (nch, nsamp + i.maxshift), dtype=np.uint8))
+        bufs[nch] = (h.pin_memory(), p.alloc_input(), p.alloc_output())
+    st = torch.cuda.Stream()
+    order = [(b, k) for k in range(args.serve_blocks) for b in range(nbeams)]
+
+    def one(nch):
+        p = plans[nch]
+        h, d_in, d_out = bufs[nch]
+        i = p.info
+        with torch.cuda.stream(st):
+            d_in[: nch * i.in_stride].view(nch, i.in_stride)[:, : nsamp + i.maxshift].copy_(
+                h, non_blocking=True)
+        p.dedisperse_device(d_in, d_out, stream=st)
+        return m.boxcar_detect_device(d_out.view(i.ndms, nsamp), nwidths=9, threshold=6.0,
+                                      cap=4096, stream=st)[1]
+
+    for b in range(3):
+        one(4096 if b % 10 != 9 else 1024)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    ncand = 0
+    units = 0
+    adds = 0
+    for b, k in order:
+        nch = 1024 if b % 10 == 9 else 4096
+        ncand += one(nch)
+        units += plans[nch].info.ndms * nsamp
+        adds += block_adds(args.algo, nch, nsamp)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    line = {"metric": METRIC, "value": units / wall, "unit": METRIC, "n_gpus": 1,
+            "steps": len(order), "warmup": 3, "ms_per_step": wall * 1e3 / len(order),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+            "data": "synthetic uint8 blocks (uniform 96-159) in pinned host memory",
+            "config": {"workload": "plain per-block path on the serving workload: %d beams "
+                                   "(10%% at 1024 ch) x 2^16-sample blocks x 4096 DM trials "
+                                   "0-2000, %s, one block at a time" % (nbeams, args.algo),
+                       "blocks_per_beam": args.serve_blocks},
+            "real_time_factor": len(order) * block_s / wall, "candidates": int(ncand),
+            "algorithmic_adds_per_unit": adds / units, "add_rate_tadd_s": adds / wall / 1e12}
     print(json.dumps(line), flush=True)
 
 
@@ -393,12 +473,14 @@ def main():
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-speed", type=float, default=1.0,
                     help="arrival speed factor over real time (inf: all at once)")
+    ap.add_argument("--serve-plain", type=int, default=0,
+                    help="1: the same workload through the plain per-block path")
     ap.add_argument("--batch-beams", type=int, default=32)
     ap.add_argument("--batch-fused", type=int, default=1)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.case == "serve":
-        return run_serve(args)
+        return run_serve_plain(args) if args.serve_plain else run_serve(args)
     if args.case == "batch":
         return run_batch(args)
     if args.case == "precision":

@@ -316,10 +316,18 @@ mdsm_status mdsm_server_add_beam_subband(mdsm_server *sv, const mdsm_subband_des
                                          int *beam);
 mdsm_status mdsm_server_beam_info(mdsm_server *sv, int beam, mdsm_plan_info *info);
 /* Block 0 of a beam holds nsamp + maxshift samples per channel, later blocks nsamp new samples
- * (row pitch h_stride elements).  The data are copied before return.  MDSM_EBUDGET: not
- * admitted now (staging budget full); retry after results are polled. */
+ * (row pitch h_stride elements).  The data are copied into a pinned staging buffer before
+ * return.  MDSM_EBUDGET: not admitted now (staging budget full); retry after results are
+ * polled. */
 mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
                                long long h_stride, long long *ticket);
+/* Zero-copy form of submit, as the reference hands its caller the input buffer to fill
+ * (initialiseMDSM / next_chunk): acquire returns a pinned staging buffer for the beam's next
+ * block, [nchans][*cols] samples of the beam's type (*cols = nsamp + maxshift for block 0, else
+ * nsamp); the producer writes the block there and commit queues it.  One acquired block per
+ * beam at a time; one producer thread per beam.  MDSM_EBUDGET as for submit. */
+mdsm_status mdsm_server_acquire(mdsm_server *sv, int beam, void **h_block, long long *cols);
+mdsm_status mdsm_server_commit(mdsm_server *sv, int beam, long long *ticket);
 /* One finished block (completion order), its candidates sorted by dm then sample.
  * MDSM_EAGAIN when none is ready within wait_ms. */
 mdsm_status mdsm_server_poll(mdsm_server *sv, mdsm_block_result *res, mdsm_candidate *cands,

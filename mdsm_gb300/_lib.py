@@ -169,7 +169,7 @@ _LIB = None
 SERVER_SYMBOLS = ("mdsm_server_create", "mdsm_server_add_beam_brute",
                   "mdsm_server_add_beam_subband", "mdsm_server_beam_info", "mdsm_server_submit",
                   "mdsm_server_poll", "mdsm_server_drain", "mdsm_server_get_stats",
-                  "mdsm_server_destroy")
+                  "mdsm_server_destroy", "mdsm_server_acquire", "mdsm_server_commit")
 
 
 def load(path=None):

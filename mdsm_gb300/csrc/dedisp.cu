@@ -228,6 +228,7 @@ constexpr int kPCC = 16;            // channels per stage
 constexpr int kPNR = 3;             // raw stages in flight
 constexpr int kPT = 128 * kPR4;     // samples per tile (512)
 constexpr int kPDB = kPNW * kPDPW;  // DM trials per tile (32)
+constexpr int kPThreads = (kPNW + 1) * 32;  // compute warps + one producer warp (index kPNW)
 
 // One (DM block, time tile, group) item of the packed kernel.  `kc` counts the chunks this CTA
 // has staged so far: it selects the mbarrier stage, phase parity and phase buffer, so a CTA can
@@ -253,15 +254,16 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
     const int32_t *ss_b = a.sminspan + bofs * 2;
     const int nchunks = (a.nchans + kPCC - 1) / kPCC;
 
-    auto fill = [&](int s, int k) {
+    // Warp 0 stages chunk k into stage s; lane c's (smin, span) of its channel is `ss`.
+    auto fill = [&](int s, int k, int2 ss) {
         const int c0 = k * kPCC;
         const int nc = min(kPCC, a.nchans - c0);
         unsigned bytes = 0;
         const unsigned char *src = nullptr;
         if (lane < nc) {
             const int c = c0 + lane;
-            const long long start = t0 + ss_b[2 * c];
-            const long long end = start + kPT + ss_b[2 * c + 1];
+            const long long start = t0 + ss.x;
+            const long long end = start + kPT + ss.y;
             const long long sb = start & ~15LL;
             const long long eb = (end + 15) & ~15LL;
             bytes = (unsigned)(eb - sb);
@@ -276,9 +278,21 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
         if (lane == 0)
             bulk_g2s(offsm + s * kPCC * kPDB, off_b + (size_t)c0 * kPDB, offbytes, &bars[s]);
     };
+    // (smin, span) of the next chunk to stage, loaded one chunk ahead so that the fill after
+    // each barrier does not wait on a global load
+    int2 ss_next = make_int2(0, 0);
+    auto load_ss = [&](int k) {
+        const int c = k * kPCC + lane;
+        if (k < nchunks && c < a.nchans) ss_next = __ldg(reinterpret_cast<const int2 *>(ss_b) + c);
+    };
 
-    if (warp == 0)
-        for (int i = 0; i < kPNR && i < nchunks; ++i) fill((int)((kc + i) % kPNR), i);
+    if (warp == kPNW) {
+        for (int i = 0; i < kPNR && i < nchunks; ++i) {
+            load_ss(i);
+            fill((int)((kc + i) % kPNR), i, ss_next);
+        }
+        load_ss(kPNR);
+    }
 
     uint32_t A[kPDPW][kPR4];  // raw 4-sample words summed mod 2^32 (<= 256 channels)
     uint32_t O[kPDPW][kPR4];  // odd samples (s1, s3) as uint16 lanes (<= 256 channels)
@@ -300,7 +314,9 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
         const int pb = (int)(kk & 1u);  // phase buffer of this chunk
         const unsigned par = (kk / kPNR) & 1u;
         const int nc = min(kPCC, a.nchans - k * kPCC);
-        const bool ok = mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
+        // the producer warp reads nothing the copies write
+        const bool ok =
+            warp == kPNW || mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
         if (ok) {
             // Expand staged row `warp` into its four phase copies (16-byte loads and stores).
             // P[pb] was last read by chunk k-2, before the barrier of iteration k-1.
@@ -323,15 +339,20 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
                                    __funnelshift_r(w.z, w.w, 24), __funnelshift_r(w.w, w4, 24));
                 }
             }
-            offcur[pb * kPCC * kPDB + tid] = offsm[s * kPCC * kPDB + tid];  // 512 entries
+            if (tid < kPCC * kPDB) offcur[pb * kPCC * kPDB + tid] = offsm[s * kPCC * kPDB + tid];
         }
         if (__syncthreads_or(!ok)) {
             aborted = true;
             break;
         }
-        if (warp == 0 && k + kPNR < nchunks) {
-            fence_proxy_async_smem();
-            fill(s, k + kPNR);
+        if (warp == kPNW) {
+            // stage k's rows have been expanded by every warp (the barrier above): refill it
+            if (k + kPNR < nchunks) {
+                fence_proxy_async_smem();
+                fill(s, k + kPNR, ss_next);
+                load_ss(k + kPNR + 1);
+            }
+            continue;
         }
         const unsigned char *pbase =
             reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * 4 * nwp) + lane * 4;
@@ -353,9 +374,9 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
             for (int r = 0; r < kPR4; ++r) {
                 const uint32_t wa0 = a0[32 * r], wa1 = a1[32 * r];
                 const uint32_t wz0 = z0[32 * r], wz1 = z1[32 * r];
-                A[0][r] += wa0 + wz0;
+                A[0][r] = A[0][r] + wa0 + wz0;
                 O[0][r] += __byte_perm(wa0, 0u, 0x4341) + __byte_perm(wz0, 0u, 0x4341);
-                A[1][r] += wa1 + wz1;
+                A[1][r] = A[1][r] + wa1 + wz1;
                 O[1][r] += __byte_perm(wa1, 0u, 0x4341) + __byte_perm(wz1, 0u, 0x4341);
             }
         };
@@ -406,6 +427,7 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
         return false;
     }
     kc += (unsigned)nchunks;
+    if (warp == kPNW) return true;
 
 #pragma unroll
     for (int j = 0; j < kPDPW; ++j) {
@@ -434,7 +456,7 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
     return true;
 }
 
-__global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
+__global__ void __launch_bounds__(kPThreads, 1) k_shift_sum_u8x4(KArgs a)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     if (threadIdx.x == 0) {
@@ -451,7 +473,7 @@ __global__ void __launch_bounds__(kPNW * 32, 1) k_shift_sum_u8x4(KArgs a)
 // from a global counter until the list is exhausted.  Beams may differ in channels, samples
 // and DM plan; they share one staging geometry (rowcap, ps) so the shared-memory layout stays
 // fixed across items.
-__global__ void __launch_bounds__(kPNW * 32, 1)
+__global__ void __launch_bounds__(kPThreads, 1)
     k_shift_sum_u8x4_batch(const KArgs *__restrict__ beams, const int4 *__restrict__ items,
                            int nitems, unsigned *__restrict__ counter)
 {
@@ -714,7 +736,7 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
         return fail(MDSM_EINVAL, "block too long for one launch");
     dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);
     void *args[] = {&a};
-    const unsigned threads = g.kernel == 2 ? kPNW * 32 : kNW * 32;
+    const unsigned threads = g.kernel == 2 ? kPThreads : kNW * 32;
     MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, g.smem_bytes, st));
     if (launches) *launches += 1;
     return MDSM_OK;
@@ -801,7 +823,7 @@ mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in
         a.nst = g.nst;
         a.out_i32 = g.out_i32;
         a.ps = g.kernel == 2 ? b.ps : g.ps;
-        a.err = d_err;
+            a.err = d_err;
     }
     for (int i : order) {
         const StageGeom &g = *b.beams[i].g;
@@ -843,7 +865,7 @@ mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches
         MDSM_CUDA_TRY(cudaGetDevice(&dev));
         MDSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const int grid = std::min(sms, b.nitems);
-        k_shift_sum_u8x4_batch<<<grid, kPNW * 32, b.smem, st>>>(
+        k_shift_sum_u8x4_batch<<<grid, kPThreads, b.smem, st>>>(
             reinterpret_cast<const KArgs *>(b.d_kargs), reinterpret_cast<const int4 *>(b.d_items),
             b.nitems, b.d_counter);
         MDSM_CUDA_TRY(cudaGetLastError());

@@ -427,6 +427,11 @@ __global__ void __launch_bounds__(kBoxThreads)
         best[i] = -INFINITY;
         bw[i] = 0;
     }
+    // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
+    __shared__ float inv_w[9];
+    if (threadIdx.x < nw)
+        inv_w[threadIdx.x] = __double2float_rn(
+            __ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << threadIdx.x)))));
     __syncthreads();
     constexpr int PER = (kBoxTile + 2 * 128 + 256 + kBoxThreads - 1) / kBoxThreads;
     for (int l = 0; l < nw; ++l) {
@@ -448,7 +453,7 @@ __global__ void __launch_bounds__(kBoxThreads)
             __syncthreads();
         }
         const float wm = __fmul_rn((float)w, mu_f);
-        const float inv = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)w))));
+        const float inv = inv_w[l];
         for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
             const long long t = r0 + i;
             if (t < 0 || t + w > n) continue;
@@ -484,7 +489,7 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
 {
     if (dtype != MDSM_OUT_F32 && dtype != MDSM_OUT_I32)
         return fail(MDSM_EINVAL, "boxcar detector: series must be float32 or int32");
-    if (nwidths > 9) return fail(MDSM_EINVAL, "boxcar detector: widths up to 256");
+    if (nwidths < 1 || nwidths > 9) return fail(MDSM_EINVAL, "boxcar detector: widths up to 256");
     if (cap < 0) cap = 0;
     const int nch = (nsamp + 1023) / 1024;
     const size_t off_cnt = 0, off_part = 256;

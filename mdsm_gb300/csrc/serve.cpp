@@ -14,7 +14,11 @@
 //  * a block's pipeline is H2D of the new samples -> tail copy -> dedispersion -> boxcar
 //    search -> D2H of the candidates only (the dedispersed block stays on the device);
 //  * one dispatcher thread admits, one completion step records per-block latency (submit to
-//    candidates on the host) and returns results in completion order.
+//    candidates on the host) and returns results in completion order;
+//  * new samples wait in pinned staging buffers from a pool that is allocated once up to the
+//    host staging budget and reused (pinning memory per block would cost more than copying
+//    it); a producer either hands its block to submit (copied in by several threads) or
+//    writes it in place into a buffer from acquire and queues it with commit.
 // A beam's blocks are processed in order; different beams are independent, so a beam's
 // results are the same whether it runs alone or mixed with others.
 #include <algorithm>
@@ -41,8 +45,15 @@ double now_s()
         .count();
 }
 
+struct StageBuf {
+    void *h = nullptr;  // pinned
+    size_t bytes = 0;
+    bool used = false;
+};
+
 struct Beam {
     mdsm_plan *plan = nullptr;
+    int acquired = -1;         // staging buffer handed out by acquire, not yet committed
     void *d_buf[2] = {nullptr, nullptr};
     size_t buf_bytes = 0;
     long long stride = 0;      // device row pitch (elements)
@@ -57,8 +68,7 @@ struct Pending {
     long long block;
     long long ticket;
     double t_submit;
-    void *h_stage;  // pinned copy of the new samples [nchans][cols]
-    size_t stage_bytes;
+    int stage;      // staging buffer holding the new samples [nchans][cols]
     long long cols;
 };
 
@@ -90,7 +100,8 @@ struct Server {
     bool stop = false;
     long long tickets = 0;
     long long held_bytes = 0;     // device bytes held (beams + slots)
-    long long staged_bytes = 0;   // pinned bytes of queued blocks
+    std::vector<StageBuf> pool;   // pinned staging buffers
+    long long pool_bytes = 0;     // pinned bytes allocated (<= host staging budget)
     std::vector<double> latencies;
     long long admitted = 0, refused = 0, completed = 0, units = 0;
     double t_first = 0, t_last = 0;
@@ -100,7 +111,81 @@ struct Server {
     void run();
     bool launch(Slot &s, Pending &p);
     void harvest(Slot &s);
+    mdsm_status stage_get(size_t bytes, int *idx, bool admission = true);
+    void prestage(size_t bytes, int count);
+    void *stage_ptr(int idx)
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        return pool[(size_t)idx].h;
+    }
 };
+
+// Pin `count` staging buffers of at least `bytes` ahead of time (as far as the budget allows),
+// so that the first blocks of a beam do not wait for page pinning.
+void Server::prestage(size_t bytes, int count)
+{
+    std::vector<int> got;
+    for (int i = 0; i < count; ++i) {
+        int idx = -1;
+        if (stage_get(bytes, &idx, false) != MDSM_OK) break;
+        got.push_back(idx);
+    }
+    std::lock_guard<std::mutex> lk(mu);
+    for (int idx : got) pool[(size_t)idx].used = false;
+}
+
+// A free pinned buffer of at least `bytes` (the smallest that fits), else a new one while the
+// budget allows (freeing idle buffers that are too small to make room), else MDSM_EBUDGET.
+mdsm_status Server::stage_get(size_t bytes, int *idx, bool admission)
+{
+    std::unique_lock<std::mutex> lk(mu);
+    int best = -1;
+    for (size_t i = 0; i < pool.size(); ++i)
+        if (!pool[i].used && pool[i].h && pool[i].bytes >= bytes &&
+            (best < 0 || pool[i].bytes < pool[(size_t)best].bytes))
+            best = (int)i;
+    if (best >= 0) {
+        pool[(size_t)best].used = true;
+        *idx = best;
+        return MDSM_OK;
+    }
+    std::vector<void *> drop;
+    for (size_t i = 0; i < pool.size() && pool_bytes + (long long)bytes > desc.host_stage_bytes;
+         ++i)
+        if (!pool[i].used && pool[i].h) {
+            drop.push_back(pool[i].h);
+            pool_bytes -= (long long)pool[i].bytes;
+            pool[i] = StageBuf();
+        }
+    if (pool_bytes + (long long)bytes > desc.host_stage_bytes) {
+        if (admission) refused++;
+        lk.unlock();
+        for (void *h : drop) cudaFreeHost(h);
+        return fail(MDSM_EBUDGET, "admission: host staging budget full, retry later");
+    }
+    pool_bytes += (long long)bytes;  // reserved before the (slow) pinning, outside the lock
+    lk.unlock();
+    for (void *h : drop) cudaFreeHost(h);
+    void *h = nullptr;
+    if (cudaHostAlloc(&h, bytes, 0) != cudaSuccess) {
+        lk.lock();
+        pool_bytes -= (long long)bytes;
+        return fail(MDSM_ENOMEM, "pinned staging allocation failed");
+    }
+    lk.lock();
+    size_t slot = pool.size();
+    for (size_t i = 0; i < pool.size(); ++i)
+        if (!pool[i].h) {
+            slot = i;
+            break;
+        }
+    if (slot == pool.size()) pool.emplace_back();
+    pool[slot].h = h;
+    pool[slot].bytes = bytes;
+    pool[slot].used = true;
+    *idx = (int)slot;
+    return MDSM_OK;
+}
 
 void Server::harvest(Slot &s)
 {
@@ -125,8 +210,7 @@ void Server::harvest(Slot &s)
     units += (long long)p.ndms * p.nsamp;
     t_last = r.done_time;
     results.emplace_back(r, std::move(c));
-    cudaFreeHost(s.job.h_stage);
-    staged_bytes -= (long long)s.job.stage_bytes;
+    pool[(size_t)s.job.stage].used = false;
     s.busy = false;
     cv.notify_all();
 }
@@ -139,6 +223,7 @@ bool Server::launch(Slot &s, Pending &job)
     const long long ms = p.maxshift, ns = p.nsamp;
     const size_t E = b.elem;
     cudaStream_t st = s.st;
+    const void *h_stage = stage_ptr(job.stage);
     // A beam's blocks run one after another: the previous block's input holds this block's
     // tail, and its dedispersion must be done (the plan's intermediate buffers are per beam,
     // and the block before it read the buffer this block overwrites).  Other beams overlap.
@@ -146,7 +231,7 @@ bool Server::launch(Slot &s, Pending &job)
     if (job.block > 0) cudaStreamWaitEvent(st, b.buf_free[prv], 0);
     cudaError_t e = cudaSuccess;
     if (job.block == 0) {
-        e = cudaMemcpy2DAsync(b.d_buf[cur], b.stride * E, job.h_stage, (size_t)job.cols * E,
+        e = cudaMemcpy2DAsync(b.d_buf[cur], b.stride * E, h_stage, (size_t)job.cols * E,
                               (size_t)(ns + ms) * E, p.nchans, cudaMemcpyHostToDevice, st);
     } else {
         if (ms > 0)
@@ -155,7 +240,7 @@ bool Server::launch(Slot &s, Pending &job)
                                   (size_t)ms * E, p.nchans, cudaMemcpyDeviceToDevice, st);
         if (e == cudaSuccess)
             e = cudaMemcpy2DAsync(static_cast<char *>(b.d_buf[cur]) + ms * E, b.stride * E,
-                                  job.h_stage, (size_t)job.cols * E, (size_t)ns * E, p.nchans,
+                                  h_stage, (size_t)job.cols * E, (size_t)ns * E, p.nchans,
                                   cudaMemcpyHostToDevice, st);
     }
     if (e == cudaSuccess) e = cudaEventRecord(b.in_ready, st);
@@ -283,9 +368,13 @@ mdsm_status add_beam(mdsm_server *sv, mdsm_plan *plan, int *beam)
             sl.det_bytes = det;
         }
     }
-    std::lock_guard<std::mutex> lk(S.mu);
-    S.beams.push_back(b);
-    *beam = (int)S.beams.size() - 1;
+    {
+        std::lock_guard<std::mutex> lk(S.mu);
+        S.beams.push_back(b);
+        *beam = (int)S.beams.size() - 1;
+    }
+    // staging for the blocks in flight plus two queued, sized for a first block (with tail)
+    S.prestage((size_t)(p.nsamp + p.maxshift) * p.nchans * b.elem, S.desc.max_inflight + 2);
     return MDSM_OK;
 }
 
@@ -346,39 +435,38 @@ mdsm_status mdsm_server_beam_info(mdsm_server *sv, int beam, mdsm_plan_info *inf
     return mdsm_plan_get_info(sv->s.beams[beam].plan, info);
 }
 
-mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
-                               long long h_stride, long long *ticket)
+mdsm_status mdsm_server_acquire(mdsm_server *sv, int beam, void **h_block, long long *cols)
 {
-    if (!sv || !h_block) return fail(MDSM_EINVAL, "null argument");
+    if (!sv || !h_block || !cols) return fail(MDSM_EINVAL, "null argument");
     Server &S = sv->s;
     if (beam < 0 || beam >= (int)S.beams.size()) return fail(MDSM_EINVAL, "bad beam");
     Beam &b = S.beams[beam];
-    const Plan &p = b.plan->p;
-    const long long first = b.next_block == 0;
-    const long long cols = first ? (long long)p.nsamp + p.maxshift : p.nsamp;
-    if (h_stride < cols) return fail(MDSM_ERANGE, "block row pitch smaller than its samples");
-    const size_t bytes = (size_t)cols * p.nchans * b.elem;
     {
         std::lock_guard<std::mutex> lk(S.mu);
         if (S.fault != MDSM_OK) return fail(S.fault, "server stopped after a fault: " + S.fault_msg);
-        if (S.staged_bytes + (long long)bytes > S.desc.host_stage_bytes) {
-            S.refused++;
-            return fail(MDSM_EBUDGET, "admission: host staging budget full, retry later");
-        }
-        S.staged_bytes += (long long)bytes;
+        if (b.acquired >= 0) return fail(MDSM_EINVAL, "beam already holds an acquired block");
     }
-    void *stage = nullptr;
-    if (cudaHostAlloc(&stage, bytes, 0) != cudaSuccess) {
-        std::lock_guard<std::mutex> lk(S.mu);
-        S.staged_bytes -= (long long)bytes;
-        return fail(MDSM_ENOMEM, "pinned staging allocation failed");
-    }
-    // copy the new samples (row pitch cols) so the caller's buffer is free on return
-    for (int c = 0; c < p.nchans; ++c)
-        std::memcpy(static_cast<char *>(stage) + (size_t)c * cols * b.elem,
-                    static_cast<const char *>(h_block) + (size_t)c * h_stride * b.elem,
-                    (size_t)cols * b.elem);
-    Pending job{beam, b.next_block, 0, now_s(), stage, bytes, cols};
+    const Plan &p = b.plan->p;
+    const long long c = b.next_block == 0 ? (long long)p.nsamp + p.maxshift : p.nsamp;
+    int idx = -1;
+    MDSM_TRY(S.stage_get((size_t)c * p.nchans * b.elem, &idx));
+    b.acquired = idx;
+    *h_block = S.stage_ptr(idx);
+    *cols = c;
+    return MDSM_OK;
+}
+
+mdsm_status mdsm_server_commit(mdsm_server *sv, int beam, long long *ticket)
+{
+    if (!sv) return fail(MDSM_EINVAL, "null argument");
+    Server &S = sv->s;
+    if (beam < 0 || beam >= (int)S.beams.size()) return fail(MDSM_EINVAL, "bad beam");
+    Beam &b = S.beams[beam];
+    if (b.acquired < 0) return fail(MDSM_EINVAL, "commit without an acquired block");
+    const Plan &p = b.plan->p;
+    const long long cols = b.next_block == 0 ? (long long)p.nsamp + p.maxshift : p.nsamp;
+    Pending job{beam, b.next_block, 0, now_s(), b.acquired, cols};
+    b.acquired = -1;
     {
         std::lock_guard<std::mutex> lk(S.mu);
         job.ticket = S.tickets++;
@@ -389,6 +477,42 @@ mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
     S.cv.notify_all();
     if (ticket) *ticket = job.ticket;
     return MDSM_OK;
+}
+
+mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
+                               long long h_stride, long long *ticket)
+{
+    if (!sv || !h_block) return fail(MDSM_EINVAL, "null argument");
+    Server &S = sv->s;
+    if (beam < 0 || beam >= (int)S.beams.size()) return fail(MDSM_EINVAL, "bad beam");
+    Beam &b = S.beams[beam];
+    const Plan &p = b.plan->p;
+    const long long need = b.next_block == 0 ? (long long)p.nsamp + p.maxshift : p.nsamp;
+    if (h_stride < need) return fail(MDSM_ERANGE, "block row pitch smaller than its samples");
+    void *stage = nullptr;
+    long long cols = 0;
+    MDSM_TRY(mdsm_server_acquire(sv, beam, &stage, &cols));
+    // copy the new samples (row pitch cols) so the caller's buffer is free on return; large
+    // blocks are copied by several threads, a band of channels each
+    const size_t row = (size_t)cols * b.elem;
+    const int nthr = (int)std::min<long long>(
+        std::max(1u, std::min(8u, std::thread::hardware_concurrency())),
+        std::max<long long>(1, (long long)row * p.nchans / (4ll << 20)));
+    auto copy_rows = [&](int c0, int c1) {
+        for (int c = c0; c < c1; ++c)
+            std::memcpy(static_cast<char *>(stage) + (size_t)c * row,
+                        static_cast<const char *>(h_block) + (size_t)c * h_stride * b.elem, row);
+    };
+    if (nthr <= 1) {
+        copy_rows(0, p.nchans);
+    } else {
+        std::vector<std::thread> th;
+        for (int i = 0; i < nthr; ++i)
+            th.emplace_back(copy_rows, (int)((long long)p.nchans * i / nthr),
+                            (int)((long long)p.nchans * (i + 1) / nthr));
+        for (auto &t : th) t.join();
+    }
+    return mdsm_server_commit(sv, beam, ticket);
 }
 
 mdsm_status mdsm_server_poll(mdsm_server *sv, mdsm_block_result *res, mdsm_candidate *cands,
@@ -476,7 +600,8 @@ void mdsm_server_destroy(mdsm_server *sv)
             if (b.buf_free[i]) cudaEventDestroy(b.buf_free[i]);
         mdsm_plan_destroy(b.plan);
     }
-    for (auto &q : S.queue) cudaFreeHost(q.h_stage);
+    for (auto &sb : S.pool)
+        if (sb.h) cudaFreeHost(sb.h);
     delete sv;
 }
 

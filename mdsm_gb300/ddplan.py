@@ -163,8 +163,29 @@ def to_segments(passes):
     return [(p.lo_dm, p.d_dm, p.numdms) for p in passes]
 
 
+def adds_per_sample(passes, numchan, numsub):
+    """Adds per input time sample of a plan, brute force and subband (a pass with downsample b
+    runs at 1/b of the rate).  Brute force: numdms * numchan.  Subband: stage 1 sums every
+    channel once per sub-DM call, stage 2 sums numsub subbands per fine trial."""
+    brute = sub = 0.0
+    for p in passes:
+        brute += p.numdms * numchan / p.downsamp
+        sub += (p.ncalls * numchan + p.numdms * numsub) / p.downsamp
+    return brute, sub
+
+
+def choose_algorithm(passes, numchan, numsub, min_gain=1.5):
+    """'subband' when the plan has subbands and its adds are at least min_gain times fewer than
+    brute force's, else 'brute' (brute force has no subband smearing)."""
+    if not numsub or any(not p.numsub for p in passes):
+        return "brute"
+    brute, sub = adds_per_sample(passes, numchan, numsub)
+    return "subband" if brute >= min_gain * sub else "brute"
+
+
 def to_subband_passes(passes):
-    """Subband pass dicts for SubbandPlan (downsample must be 1 for the device path)."""
+    """Subband pass dicts for SubbandPlan; a pass with downsample b > 1 dedisperses the block
+    summed over b samples."""
     out = []
     for p in passes:
         if not p.numsub:

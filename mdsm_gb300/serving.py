@@ -6,6 +6,7 @@ import time
 import numpy as np
 
 from . import _lib
+from .api import _NP_OF
 from ._lib import (ACC, DTYPES, OUT_DTYPES, SHIFT_MODES, BruteDesc, Candidate, PlanInfo,
                    Segment, SubbandDesc, SUBBAND_PASSES, check, load)
 
@@ -45,6 +46,9 @@ SIGNATURES = {
     "mdsm_server_poll": (ctypes.c_int, [_vp, ctypes.POINTER(BlockResult),
                                         ctypes.POINTER(Candidate), ctypes.c_longlong,
                                         ctypes.c_int]),
+    "mdsm_server_acquire": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(_vp),
+                                           ctypes.POINTER(ctypes.c_longlong)]),
+    "mdsm_server_commit": (ctypes.c_int, [_vp, ctypes.c_int, ctypes.POINTER(ctypes.c_longlong)]),
     "mdsm_server_drain": (ctypes.c_int, [_vp]),
     "mdsm_server_get_stats": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
     "mdsm_server_destroy": (None, [_vp]),
@@ -80,6 +84,7 @@ class Server:
         self._h = h
         self.cand_cap = cand_cap
         self.beams = []
+        self._beam_shape = {}
 
     def close(self):
         if self._h:
@@ -103,6 +108,7 @@ class Server:
         b = ctypes.c_int()
         check(lib().mdsm_server_add_beam_brute(self._h, ctypes.byref(d), ctypes.byref(b)))
         self.beams.append(segs)
+        self._beam_shape[b.value] = (int(nchans), _NP_OF[in_dtype])
         return b.value
 
     def add_beam_subband(self, nchans, fch1, foff, tsamp, nsamp, nsubs, passes, in_dtype="u8"):
@@ -111,13 +117,14 @@ class Server:
             for f in ("lowdm", "highdm", "dmstep", "sub_dmstep", "ncalls", "calldms", "ndms"):
                 if f in p:
                     setattr(arr[k], f, p[f])
-            arr[k].binsize = 1
+            arr[k].binsize = int(p.get("binsize", 1))
         d = SubbandDesc(int(nchans), float(fch1), float(foff), float(tsamp), int(nsamp),
                         int(nsubs), arr, len(passes), 1, DTYPES[in_dtype],
                         OUT_DTYPES["i32" if in_dtype != "f32" else "f32"], ACC["auto"])
         b = ctypes.c_int()
         check(lib().mdsm_server_add_beam_subband(self._h, ctypes.byref(d), ctypes.byref(b)))
         self.beams.append(arr)
+        self._beam_shape[b.value] = (int(nchans), _NP_OF[in_dtype])
         return b.value
 
     def beam_info(self, beam):
@@ -134,6 +141,25 @@ class Server:
         if st == 7:  # MDSM_EBUDGET
             return None
         check(st)
+        return t.value
+
+    def acquire(self, beam):
+        """A pinned staging buffer for the beam's next block as a writable numpy view
+        [nchans][cols], or None when admission refuses for now.  Fill it, then commit(beam)."""
+        ptr = _vp()
+        cols = ctypes.c_longlong()
+        st = lib().mdsm_server_acquire(self._h, beam, ctypes.byref(ptr), ctypes.byref(cols))
+        if st == 7:  # MDSM_EBUDGET
+            return None
+        check(st)
+        nchans, dtype = self._beam_shape[beam]
+        n = nchans * cols.value * np.dtype(dtype).itemsize
+        buf = (ctypes.c_char * n).from_address(ptr.value)
+        return np.frombuffer(buf, dtype=dtype).reshape(nchans, cols.value)
+
+    def commit(self, beam):
+        t = ctypes.c_longlong()
+        check(lib().mdsm_server_commit(self._h, beam, ctypes.byref(t)))
         return t.value
 
     def poll(self, wait_ms=0):

@@ -44,3 +44,18 @@ def test_passes_xml_round_trip(lib, tmp_path):
                                                             p.dms_per_call, p.ncalls)
     load = __import__("mdsm_gb300")._lib.load()
     load.mdsm_free_survey(compat.processSurveyParameters(path))
+
+
+def test_algorithm_choice_by_adds():
+    from mdsm_gb300 import ddplan
+    passes = ddplan.plan(0.0, 1000.0, 1400.0, 300.0, 4096, 64, 0.000064)
+    brute, sub = ddplan.adds_per_sample(passes, 4096, 64)
+    # hand count from the pass fields
+    assert brute == sum(p.numdms * 4096 / p.downsamp for p in passes)
+    assert sub == sum((p.ncalls * 4096 + p.numdms * 64) / p.downsamp for p in passes)
+    assert sub < brute
+    assert ddplan.choose_algorithm(passes, 4096, 64) == "subband"
+    # no subbands: brute force; a gain below the bar: brute force
+    assert ddplan.choose_algorithm(ddplan.plan(0.0, 100.0, 1400.0, 300.0, 256, 0, 64e-6),
+                                   256, 0) == "brute"
+    assert ddplan.choose_algorithm(passes, 4096, 64, min_gain=brute / sub * 2) == "brute"

@@ -99,3 +99,59 @@ def test_reference_subband_bitexact(lib, orc, cuda, refgpu):
     ok_rows = (S2 <= tempval).all(axis=1)
     assert ok_rows.sum() > 0.9 * len(ok_rows)
     assert np.array_equal(got[ok_rows], ref[ok_rows])
+
+
+def test_reference_kernels_timing_data_point(lib, orc, cuda, refgpu):
+    """The reference's two brute-force kernels and ours on the same GB300, the same float
+    input and the same plan (2048 channels x 65520 samples x 512 DM trials 0-255.5): kernel-only
+    DM-trial-samples/s of each, printed as one JSON line (run with -s).  Ours must be faster
+    than both, and equal to the L1 kernel's output on the region it computes."""
+    import json
+    import mdsm_gb300 as m
+    torch = cuda
+    nchans, nsamp, tsamp = 2048, 210 * 312, 64e-6
+    fch1, foff = 1500.0, -300.0 / 2048
+    lowdm, dmstep, tdms = 0.0, 0.5, 512
+    plan = m.BrutePlan(nchans, fch1, foff, tsamp, nsamp, [(lowdm, dmstep, tdms)],
+                       shift_mode="l1", in_dtype="f32")
+    ms = plan.maxshift + 2
+    rng = np.random.default_rng(9)
+    x = rng.standard_normal((nchans, nsamp + ms), dtype=np.float32)
+    rates = {}
+    ref = None
+    for kind, name in ((0, "reference global_for_time_dedisperse_loop"),
+                       (1, "reference opt_dedisperse_loop")):
+        t = []
+        for _ in range(2):
+            y, ms_k = refgpu.brute(kind, x, nsamp, ms, lowdm, dmstep, tsamp, tdms,
+                                   plan.dmshifts())
+            t.append(ms_k)
+        covered = (tdms // 32 * 32) * (nsamp // 210 * 210) if kind == 0 else \
+            tdms * (nsamp // 128 * 128)
+        rates[name] = covered / (min(t) / 1e3)
+        if kind == 0:
+            ref = y
+    d_in = plan.alloc_input()
+    nch, stride = plan.input_shape()
+    buf = np.zeros((nch, stride), np.float32)
+    w = min(stride, x.shape[1])
+    buf[:, :w] = x[:, :w]
+    d_in[: buf.size].copy_(torch.from_numpy(buf.ravel()))
+    d_out = plan.alloc_output()
+    st = torch.cuda.current_stream()
+    t = []
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        plan.dedisperse_device(d_in, d_out, stream=st)
+        e1.record(st)
+        torch.cuda.synchronize()
+        t.append(e0.elapsed_time(e1))
+    rates["mdsm_gb300 k_shift_sum (float in, same plan)"] = tdms * nsamp / (min(t[1:]) / 1e3)
+    got = d_out.cpu().numpy()
+    assert np.array_equal(got, ref)
+    print(json.dumps({"case": "float32 2048 ch x 65520 samples x 512 DM trials, kernel only",
+                      "dm_trial_samples_per_s": rates}))
+    ours = rates["mdsm_gb300 k_shift_sum (float in, same plan)"]
+    assert ours > rates["reference global_for_time_dedisperse_loop"]
+    assert ours > rates["reference opt_dedisperse_loop"]

@@ -108,3 +108,41 @@ def test_host_staging_budget_defers_blocks(lib, cuda):
     st = srv.stats()
     srv.close()
     assert st["completed"] >= 1
+
+
+def test_acquire_commit_equals_submit(lib, cuda):
+    """The zero-copy form (write into the server's pinned staging buffer, then commit) gives the
+    same candidates as submit; staging buffers are reused block after block."""
+    from mdsm_gb300.serving import Server
+    nchans, nsamp, segs, seed = BEAMS[1]
+
+    def run(zero_copy):
+        # room for two staging buffers (maxshift is 507 here): the third block must reuse one
+        srv = Server(max_inflight=2, nwidths=7, threshold=6.0, cand_cap=2048,
+                     host_stage_bytes=nchans * (2 * nsamp + 600))
+        b = srv.add_beam(nchans, FCH1, -BW / nchans, TSAMP, nsamp, segs)
+        ms = srv.beam_info(b).maxshift
+        assert 2 * nsamp + ms <= 2 * nsamp + 600 < 3 * nsamp
+        blocks = _blocks(_stream(nchans, nsamp, ms, seed), nsamp, ms)
+        out = []
+        for k, blk in enumerate(blocks):
+            while True:
+                if zero_copy:
+                    view = srv.acquire(b)
+                    if view is not None:
+                        assert view.shape == blk.shape and view.dtype == blk.dtype
+                        view[...] = blk
+                        srv.commit(b)
+                        break
+                elif srv.submit(b, blk) is not None:
+                    break
+                out += srv.results(1)  # staging full: take a result, which frees a buffer
+        out += srv.results(NBLOCKS - len(out))
+        srv.drain()
+        srv.close()
+        return {r["block"]: r["cands"] for r in out}
+
+    a, z = run(False), run(True)
+    assert sorted(a) == sorted(z) == list(range(NBLOCKS))
+    for k in a:
+        assert np.array_equal(a[k], z[k])

@@ -221,106 +221,200 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 //  * two channels share each 3-input integer add (A += wa + wz, O += odd(wa) + odd(wz)).
 // Per 4 sample-adds per channel: 1 LDS, 1 PRMT and one 3-input add.
 // ------------------------------------------------------------------------------------------
-constexpr int kPNW = 16;            // warps
+constexpr int kPNW = 19;            // compute warps
 constexpr int kPDPW = 2;            // DM trials per warp
 constexpr int kPR4 = 4;             // 4-sample words per lane per DM trial
 constexpr int kPCC = 16;            // channels per stage
 constexpr int kPNR = 3;             // raw stages in flight
 constexpr int kPT = 128 * kPR4;     // samples per tile (512)
-constexpr int kPDB = kPNW * kPDPW;  // DM trials per tile (32)
+constexpr int kPDB = kPNW * kPDPW;  // DM trials per tile (38)
+constexpr int kPDBS = (kPDB + 3) / 4 * 4;  // offsets per channel as stored: whole 16-byte units
 constexpr int kPThreads = (kPNW + 1) * 32;  // compute warps + one producer warp (index kPNW)
+static_assert(kPNW >= kPCC, "one compute warp per staged row expands it");
+static_assert(kPNW * 32 == kPCC * kPDB, "one compute thread per staged offset");
 
-// One (DM block, time tile, group) item of the packed kernel.  `kc` counts the chunks this CTA
-// has staged so far: it selects the mbarrier stage, phase parity and phase buffer, so a CTA can
-// process any number of items in a row.  Returns false if a bounded wait ran out.
-__device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long tile, int g,
-                                            unsigned char *smem, unsigned &kc)
+// Work items of the packed kernel are (beam, DM block, time tile, group) tiles; a CTA runs a
+// stream of them.  The producer warp stages the stream's chunks (16 channels of one item) into
+// a ring of kPNR stages, running ahead across item boundaries, and writes each chunk's
+// (item, chunk index, channels, flags) beside it; the compute warps take the chunks in order,
+// start an item's sums on its first chunk and store them after its last.  So short items
+// (few channels, as in the first subband stage) keep the copies in flight between items.
+constexpr int kChunkFirst = 1, kChunkLast = 2, kChunkStop = 4;
+
+// CTA barrier 0 returning whether any thread passed true.  The producer and the compute warps
+// reach it from their own loops, once per chunk each (a barrier counts warps, so the program
+// locations may differ between warps).
+__device__ __forceinline__ bool cta_any(bool pred)
 {
-    const int rawcap = a.rowcap;  // bytes per raw row (multiple of 16)
-    const int ps = a.ps;          // bytes per phase copy (multiple of 16)
-    const int nwp = ps >> 2;      // words per phase copy
-    const int nq = nwp >> 2;      // 16-byte quads per phase copy
+    uint32_t r;
+    asm volatile(
+        "{\n\t.reg .pred p, q;\n\t"
+        "setp.ne.u32 p, %1, 0;\n\t"
+        "bar.red.or.pred q, 0, p;\n\t"
+        "selp.u32 %0, 1, 0, q;\n\t}"
+        : "=r"(r)
+        : "r"((uint32_t)pred)
+        : "memory");
+    return r != 0;
+}
+
+// Items of one plan, (DM block fastest, time tile, group); CTA b takes b, b + G, b + 2G, ...
+struct OnePlanItems {
+    const KArgs *a;
+    int ntiles, nitems;
+    int next_it;
+    __device__ int grab()
+    {
+        const int it = next_it;
+        next_it += gridDim.x;
+        return it < nitems ? it : -1;
+    }
+    __device__ int4 item(int it) const
+    {
+        const int blk = it % a->nblk, rest = it / a->nblk;
+        return make_int4(0, blk, rest % ntiles, rest / ntiles);
+    }
+    __device__ const KArgs &args(int) const { return *a; }
+};
+
+// Items of several plans from a list, taken from a global counter.
+struct ListItems {
+    const KArgs *beams;
+    const int4 *items;
+    int nitems;
+    unsigned *counter;
+    __device__ int grab()
+    {
+        const int it = (int)atomicAdd(counter, 1u);
+        return it < nitems ? it : -1;
+    }
+    __device__ int4 item(int it) const { return items[it]; }
+    __device__ const KArgs &args(int beam) const { return beams[beam]; }
+};
+
+template <class Src>
+__device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int rawcap, int ps,
+                                              unsigned *err)
+{
+    const int nwp = ps >> 2;  // words per phase copy
+    const int nq = nwp >> 2;  // 16-byte quads per phase copy
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+    int4 *meta = reinterpret_cast<int4 *>(smem + 64);  // kPNR entries
     unsigned char *raw = smem + 128;
     int32_t *offsm = reinterpret_cast<int32_t *>(raw + (size_t)kPNR * kPCC * rawcap);
-    int32_t *offcur = offsm + kPNR * kPCC * kPDB;                 // 2 x kPCC x kPDB
-    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + 2 * kPCC * kPDB);  // 2 x kPCC x 4 x nwp
-
-    const long long t0 = tile * kPT;
+    int32_t *offcur = offsm + kPNR * kPCC * kPDBS;                // 2 x kPCC x kPDBS
+    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + 2 * kPCC * kPDBS);  // 2 x kPCC x 4 x nwp
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    const unsigned char *in_g = a.in + (size_t)(g * a.in_group_stride);
-    const size_t bofs = (size_t)(g * a.nblk + blk) * a.nchans;
-    const int32_t *off_b = a.rel + bofs * kPDB;
-    const int32_t *ss_b = a.sminspan + bofs * 2;
-    const int nchunks = (a.nchans + kPCC - 1) / kPCC;
 
-    // Warp 0 stages chunk k into stage s; lane c's (smin, span) of its channel is `ss`.
-    auto fill = [&](int s, int k, int2 ss) {
-        const int c0 = k * kPCC;
+    // ---- producer state (warp kPNW): the item being staged, its next chunk, and the lane's
+    // (smin, span) for that chunk, loaded one fill ahead so that no fill waits on a global load
+    int p_it = -1, p_k = 0, p_nchunks = 0;
+    int4 p_w = make_int4(0, 0, 0, 0);
+    int2 p_ss = make_int2(0, 0);
+    auto p_next_item = [&]() {
+        int it = 0;
+        if (lane == 0) it = src.grab();
+        p_it = __shfl_sync(0xffffffffu, it, 0);
+        p_k = 0;
+        if (p_it >= 0) {
+            p_w = src.item(p_it);
+            p_nchunks = (src.args(p_w.x).nchans + kPCC - 1) / kPCC;
+        }
+    };
+    auto p_load_ss = [&]() {
+        if (p_it < 0) return;
+        const KArgs &a = src.args(p_w.x);
+        const int c = p_k * kPCC + lane;
+        if (c < a.nchans) {
+            const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
+            p_ss = __ldg(reinterpret_cast<const int2 *>(a.sminspan + bofs * 2) + c);
+        }
+    };
+    // Stage the next chunk of the stream into stage s (or mark the end of the stream).
+    auto fill_next = [&](int s) {
+        if (p_it < 0) {
+            if (lane == 0) {
+                meta[s] = make_int4(-1, 0, 0, kChunkStop);
+                mbar_arrive(&bars[s]);
+            }
+            __syncwarp();
+            return;
+        }
+        const KArgs &a = src.args(p_w.x);
+        const long long t0 = (long long)p_w.z * kPT;
+        const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
+        const int c0 = p_k * kPCC;
         const int nc = min(kPCC, a.nchans - c0);
         unsigned bytes = 0;
-        const unsigned char *src = nullptr;
+        const unsigned char *src_row = nullptr;
         if (lane < nc) {
             const int c = c0 + lane;
-            const long long start = t0 + ss.x;
-            const long long end = start + kPT + ss.y;
+            const long long start = t0 + p_ss.x;
+            const long long end = start + kPT + p_ss.y;
             const long long sb = start & ~15LL;
             const long long eb = (end + 15) & ~15LL;
             bytes = (unsigned)(eb - sb);
-            src = in_g + (size_t)c * (size_t)a.in_stride + sb;
+            src_row = a.in + (size_t)(p_w.w * a.in_group_stride) +
+                      (size_t)c * (size_t)a.in_stride + sb;
         }
-        const unsigned offbytes = (unsigned)(nc * kPDB * 4);
+        const unsigned offbytes = (unsigned)(nc * kPDBS * 4);
         const unsigned total = warp_sum_u32(bytes) + offbytes;
         __syncwarp();
-        if (lane == 0) mbar_arrive_expect_tx(&bars[s], total);
-        __syncwarp();
-        if (lane < nc) bulk_g2s(raw + (size_t)(s * kPCC + lane) * rawcap, src, bytes, &bars[s]);
-        if (lane == 0)
-            bulk_g2s(offsm + s * kPCC * kPDB, off_b + (size_t)c0 * kPDB, offbytes, &bars[s]);
-    };
-    // (smin, span) of the next chunk to stage, loaded one chunk ahead so that the fill after
-    // each barrier does not wait on a global load
-    int2 ss_next = make_int2(0, 0);
-    auto load_ss = [&](int k) {
-        const int c = k * kPCC + lane;
-        if (k < nchunks && c < a.nchans) ss_next = __ldg(reinterpret_cast<const int2 *>(ss_b) + c);
-    };
-
-    if (warp == kPNW) {
-        for (int i = 0; i < kPNR && i < nchunks; ++i) {
-            load_ss(i);
-            fill((int)((kc + i) % kPNR), i, ss_next);
+        if (lane == 0) {
+            meta[s] = make_int4(p_it, p_k, nc,
+                                (p_k == 0 ? kChunkFirst : 0) |
+                                    (p_k == p_nchunks - 1 ? kChunkLast : 0));
+            mbar_arrive_expect_tx(&bars[s], total);  // releases the meta entry with the phase
         }
-        load_ss(kPNR);
+        __syncwarp();
+        if (lane < nc)
+            bulk_g2s(raw + (size_t)(s * kPCC + lane) * rawcap, src_row, bytes, &bars[s]);
+        if (lane == 0)
+            bulk_g2s(offsm + s * kPCC * kPDBS, a.rel + (bofs + (size_t)c0) * kPDBS, offbytes,
+                     &bars[s]);
+        if (++p_k == p_nchunks) p_next_item();
+        p_load_ss();
+    };
+    if (warp == kPNW) {
+        // The producer's loop: one CTA barrier per chunk, as the compute warps', then the
+        // refill of the stage every warp has just finished expanding.
+        p_next_item();
+        p_load_ss();
+        for (int i = 0; i < kPNR; ++i) fill_next(i);
+        for (unsigned gk = 0;; ++gk) {
+            const int s = (int)(gk % kPNR);
+            const bool stop = (meta[s].w & kChunkStop) != 0;  // written by this warp
+            if (cta_any(false)) {
+                for (unsigned q = gk; q < gk + kPNR; ++q)
+                    mbar_wait_bounded(&bars[q % kPNR], (q / kPNR) & 1u, nullptr, 0);
+                return;
+            }
+            if (stop) return;
+            fence_proxy_async_smem();
+            fill_next(s);
+        }
     }
 
-    uint32_t A[kPDPW][kPR4];  // raw 4-sample words summed mod 2^32 (<= 256 channels)
-    uint32_t O[kPDPW][kPR4];  // odd samples (s1, s3) as uint16 lanes (<= 256 channels)
+    // ---- compute warps ----
+    uint32_t A[kPDPW][kPR4];    // raw 4-sample words summed mod 2^32 (<= 256 channels)
+    uint32_t O[kPDPW][kPR4];    // odd samples (s1, s3) as uint16 lanes (<= 256 channels)
     int32_t f[kPDPW][kPR4][4];  // int32 sums
-#pragma unroll
-    for (int j = 0; j < kPDPW; ++j)
-#pragma unroll
-        for (int r = 0; r < kPR4; ++r) {
-            A[j][r] = O[j][r] = 0u;
-#pragma unroll
-            for (int e = 0; e < 4; ++e) f[j][r][e] = 0;
-        }
 
-    int k = 0;
+    unsigned gk = 0;  // chunk sequence number
     bool aborted = false;
-    for (; k < nchunks; ++k) {
-        const unsigned kk = kc + (unsigned)k;  // chunks staged by this CTA before this one
-        const int s = (int)(kk % kPNR);
-        const int pb = (int)(kk & 1u);  // phase buffer of this chunk
-        const unsigned par = (kk / kPNR) & 1u;
-        const int nc = min(kPCC, a.nchans - k * kPCC);
-        // the producer warp reads nothing the copies write
-        const bool ok =
-            warp == kPNW || mbar_wait_bounded(&bars[s], par, a.err, ERR_WAIT_TIMEOUT);
+    for (;; ++gk) {
+        const int s = (int)(gk % kPNR);
+        const int pb = (int)(gk & 1u);  // phase buffer of this chunk
+        const unsigned par = (gk / kPNR) & 1u;
+        const bool ok = mbar_wait_bounded(&bars[s], par, err, ERR_WAIT_TIMEOUT);
+        const int4 m = ok ? meta[s] : make_int4(-1, 0, 0, 0);
         if (ok) {
             // Expand staged row `warp` into its four phase copies (16-byte loads and stores).
-            // P[pb] was last read by chunk k-2, before the barrier of iteration k-1.
-            if (warp < nc) {
+            // P[pb] was last read for chunk gk-2, before the barrier of chunk gk-1.  All 16
+            // rows are expanded whatever the chunk holds (rows past its channels, or the whole
+            // stage at the end of the stream, hold earlier data nobody reads), so the
+            // expansion does not wait for the chunk's entry.  Warps past the 16 rows idle here.
+            if (warp < kPCC) {
                 const uint32_t *W =
                     reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + warp) * rawcap);
                 uint32_t *Pr = P + ((size_t)pb * kPCC + warp) * 4 * nwp;
@@ -339,24 +433,32 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
                                    __funnelshift_r(w.z, w.w, 24), __funnelshift_r(w.w, w4, 24));
                 }
             }
-            if (tid < kPCC * kPDB) offcur[pb * kPCC * kPDB + tid] = offsm[s * kPCC * kPDB + tid];
+            {  // one real entry per compute thread (the padding of the stored rows is not read)
+                const int i = tid / kPDB * kPDBS + tid % kPDB;
+                offcur[pb * kPCC * kPDBS + i] = offsm[s * kPCC * kPDBS + i];
+            }
         }
-        if (__syncthreads_or(!ok)) {
+        // Every thread that waited saw the same entry, so `stop` agrees across the CTA when
+        // no wait ran out.
+        if (cta_any(!ok)) {
             aborted = true;
             break;
         }
-        if (warp == kPNW) {
-            // stage k's rows have been expanded by every warp (the barrier above): refill it
-            if (k + kPNR < nchunks) {
-                fence_proxy_async_smem();
-                fill(s, k + kPNR, ss_next);
-                load_ss(k + kPNR + 1);
-            }
-            continue;
+        if (m.w & kChunkStop) break;
+        const int nc = m.z;
+        if (m.w & kChunkFirst) {
+#pragma unroll
+            for (int j = 0; j < kPDPW; ++j)
+#pragma unroll
+                for (int r = 0; r < kPR4; ++r) {
+                    A[j][r] = O[j][r] = 0u;
+#pragma unroll
+                    for (int e = 0; e < 4; ++e) f[j][r][e] = 0;
+                }
         }
         const unsigned char *pbase =
             reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * 4 * nwp) + lane * 4;
-        const int32_t *oc = offcur + pb * kPCC * kPDB + warp * kPDPW;
+        const int32_t *oc = offcur + pb * kPCC * kPDBS + warp * kPDPW;
         static_assert(kPDPW == 2, "the channel loop below handles two DM trials per warp");
         // Two channels per step: A += wa + wz and O += odd(wa) + odd(wz) are one 3-input
         // integer add each.
@@ -364,8 +466,8 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
         auto pair = [&](int c) {
             const unsigned char *pa = pbase + (size_t)c * 4 * ps;
             const unsigned char *pz = pa + 4 * ps;
-            const int2 oa = *reinterpret_cast<const int2 *>(oc + c * kPDB);
-            const int2 oz = *reinterpret_cast<const int2 *>(oc + (c + 1) * kPDB);
+            const int2 oa = *reinterpret_cast<const int2 *>(oc + c * kPDBS);
+            const int2 oz = *reinterpret_cast<const int2 *>(oc + (c + 1) * kPDBS);
             const uint32_t *a0 = reinterpret_cast<const uint32_t *>(pa + oa.x);
             const uint32_t *a1 = reinterpret_cast<const uint32_t *>(pa + oa.y);
             const uint32_t *z0 = reinterpret_cast<const uint32_t *>(pz + oz.x);
@@ -390,7 +492,7 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
         }
         if (ci < nc) {  // odd channel count: the last channel alone
             const unsigned char *pa = pbase + (size_t)ci * 4 * ps;
-            const int2 oa = *reinterpret_cast<const int2 *>(oc + ci * kPDB);
+            const int2 oa = *reinterpret_cast<const int2 *>(oc + ci * kPDBS);
             const uint32_t *a0 = reinterpret_cast<const uint32_t *>(pa + oa.x);
             const uint32_t *a1 = reinterpret_cast<const uint32_t *>(pa + oa.y);
 #pragma unroll
@@ -402,7 +504,8 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
                 O[1][r] += __byte_perm(wa1, 0u, 0x4341);
             }
         }
-        if (((k + 1) & 15) == 0 || k == nchunks - 1) {
+        const bool last = (m.w & kChunkLast) != 0;
+        if (((m.y + 1) & 15) == 0 || last) {
             // A = E + 2^8 O (mod 2^32) with E = (s0, s2) as uint16 lanes: every lane sum is at
             // most 256 * 255 < 2^16, so E and O hold the four sums exactly.
 #pragma unroll
@@ -417,84 +520,76 @@ __device__ __forceinline__ bool packed_tile(const KArgs &a, int blk, long long t
                     A[j][r] = O[j][r] = 0u;
                 }
         }
-    }
-
-    if (aborted) {
-        for (int q = k; q < nchunks && q < k + kPNR; ++q) {
-            const unsigned qq = kc + (unsigned)q;
-            mbar_wait_bounded(&bars[qq % kPNR], (qq / kPNR) & 1u, nullptr, 0);
-        }
-        return false;
-    }
-    kc += (unsigned)nchunks;
-    if (warp == kPNW) return true;
-
+        if (!last) continue;
+        // the item's sums are complete: store them
+        const int4 w = src.item(__shfl_sync(0xffffffffu, m.x, 0));
+        const KArgs &a = src.args(w.x);
+        const long long t0 = (long long)w.z * kPT;
 #pragma unroll
-    for (int j = 0; j < kPDPW; ++j) {
-        const int d = blk * kPDB + warp * kPDPW + j;
-        if (d >= a.ndms) continue;
-        unsigned char *orow =
-            a.out + (size_t)(g * a.out_group_stride + (long long)d * a.out_stride) * 4;
+        for (int j = 0; j < kPDPW; ++j) {
+            const int d = w.y * kPDB + warp * kPDPW + j;
+            if (d >= a.ndms) continue;
+            unsigned char *orow =
+                a.out + (size_t)(w.w * a.out_group_stride + (long long)d * a.out_stride) * 4;
 #pragma unroll
-        for (int r = 0; r < kPR4; ++r) {
-            const long long t = t0 + 4 * (lane + 32 * r);
-            if (t + 3 < a.nsamp && ((((uintptr_t)orow) | (t * 4)) & 15) == 0) {
-                if (a.out_i32)
-                    *reinterpret_cast<int4 *>(orow + t * 4) =
-                        make_int4(f[j][r][0], f[j][r][1], f[j][r][2], f[j][r][3]);
-                else
-                    *reinterpret_cast<float4 *>(orow + t * 4) =
-                        make_float4((float)f[j][r][0], (float)f[j][r][1], (float)f[j][r][2],
-                                    (float)f[j][r][3]);
-            } else {
+            for (int r = 0; r < kPR4; ++r) {
+                const long long t = t0 + 4 * (lane + 32 * r);
+                if (t + 3 < a.nsamp && ((((uintptr_t)orow) | (t * 4)) & 15) == 0) {
+                    if (a.out_i32)
+                        *reinterpret_cast<int4 *>(orow + t * 4) =
+                            make_int4(f[j][r][0], f[j][r][1], f[j][r][2], f[j][r][3]);
+                    else
+                        *reinterpret_cast<float4 *>(orow + t * 4) =
+                            make_float4((float)f[j][r][0], (float)f[j][r][1], (float)f[j][r][2],
+                                        (float)f[j][r][3]);
+                } else {
 #pragma unroll
-                for (int e = 0; e < 4; ++e)
-                    if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
+                    for (int e = 0; e < 4; ++e)
+                        if (t + e < a.nsamp)
+                            store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
+                }
             }
         }
     }
-    return true;
+    if (aborted) {
+        // let the copies already issued land before the CTA exits (bounded as well)
+        for (unsigned q = gk; q < gk + kPNR; ++q)
+            mbar_wait_bounded(&bars[q % kPNR], (q / kPNR) & 1u, nullptr, 0);
+    }
 }
 
-__global__ void __launch_bounds__(kPThreads, 1) k_shift_sum_u8x4(KArgs a)
+__device__ __forceinline__ void packed_init_barriers(unsigned char *smem)
 {
-    extern __shared__ __align__(128) unsigned char smem[];
     if (threadIdx.x == 0) {
         uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
         for (int s = 0; s < kPNR; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
     }
     __syncthreads();
-    unsigned kc = 0;
-    packed_tile(a, blockIdx.x, blockIdx.y, blockIdx.z, smem, kc);
 }
 
-// Persistent form over a work list: every CTA takes (beam, DM block, time tile, group) items
-// from a global counter until the list is exhausted.  Beams may differ in channels, samples
-// and DM plan; they share one staging geometry (rowcap, ps) so the shared-memory layout stays
-// fixed across items.
+// One plan: a persistent grid of at most one CTA per SM over the plan's items.
 __global__ void __launch_bounds__(kPThreads, 1)
-    k_shift_sum_u8x4_batch(const KArgs *__restrict__ beams, const int4 *__restrict__ items,
-                           int nitems, unsigned *__restrict__ counter)
+    k_shift_sum_u8x4(const __grid_constant__ KArgs a, int ntiles, int nitems)
 {
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_item;
-    if (threadIdx.x == 0) {
-        uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-        for (int s = 0; s < kPNR; ++s) mbar_init(&bars[s], 1);
-        fence_mbar_init();
-    }
-    unsigned kc = 0;
-    for (;;) {
-        __syncthreads();  // previous item done with s_item; barriers initialised
-        if (threadIdx.x == 0) s_item = (int)atomicAdd(counter, 1u);
-        __syncthreads();
-        const int it = s_item;
-        if (it >= nitems) break;
-        const int4 w = items[it];
-        const KArgs a = beams[w.x];
-        if (!packed_tile(a, w.y, (long long)w.z, w.w, smem, kc)) break;
-    }
+    packed_init_barriers(smem);
+    OnePlanItems src{&a, ntiles, nitems, (int)blockIdx.x};
+    packed_stream(src, smem, a.rowcap, a.ps, a.err);
+}
+
+// Several plans (beams that may differ in channels, samples and DM plan) from one work list,
+// sharing one staging geometry (rowcap, ps) so the shared-memory layout is the same for every
+// item.
+__global__ void __launch_bounds__(kPThreads, 1)
+    k_shift_sum_u8x4_batch(const KArgs *__restrict__ beams, const int4 *__restrict__ items,
+                           int nitems, unsigned *__restrict__ counter, int rawcap, int ps,
+                           unsigned *err)
+{
+    extern __shared__ __align__(128) unsigned char smem[];
+    packed_init_barriers(smem);
+    ListItems src{beams, items, nitems, counter};
+    packed_stream(src, smem, rawcap, ps, err);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -592,8 +687,8 @@ int tile_tables(StageGeom &g, const std::vector<int32_t> &S)
 
 size_t packed_smem(int rawcap, int ps)
 {
-    return 128 + (size_t)kPNR * kPCC * rawcap + (size_t)kPNR * kPCC * kPDB * 4 +
-           (size_t)2 * kPCC * kPDB * 4 + (size_t)2 * kPCC * 4 * ps;
+    return 128 + (size_t)kPNR * kPCC * rawcap + (size_t)kPNR * kPCC * kPDBS * 4 +
+           (size_t)2 * kPCC * kPDBS * 4 + (size_t)2 * kPCC * 4 * ps;
 }
 
 }  // namespace
@@ -629,13 +724,16 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
             g.rowcap = rawcap;
             g.ps = ps;
             // byte offset of (c, d)'s first word inside the phase-expanded row
+            // stored kPDBS per channel (the padding stays 0)
+            std::vector<int32_t> off(g.sminspan.size() / 2 * kPDBS, 0);
             for (size_t o = 0; o < g.sminspan.size() / 2; ++o) {
                 const int lo16 = g.sminspan[o * 2] & 15;
                 for (int j = 0; j < g.Db; ++j) {
                     const int e = lo16 + g.rel[o * g.Db + j];
-                    g.rel[o * g.Db + j] = (e & 3) * ps + (e >> 2) * 4;
+                    off[o * kPDBS + j] = (e & 3) * ps + (e >> 2) * 4;
                 }
             }
+            g.rel.swap(off);
             g.smem_bytes = packed_smem(rawcap, ps);
             g.kernel = 2;
             return MDSM_OK;
@@ -732,12 +830,24 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     a.ps = g.ps;
     a.err = d_err;
     const long long ntiles = (nsamp + g.T - 1) / g.T;
-    if (ntiles > 65535 || g.ngroups > 65535)
-        return fail(MDSM_EINVAL, "block too long for one launch");
-    dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);
-    void *args[] = {&a};
-    const unsigned threads = g.kernel == 2 ? kPThreads : kNW * 32;
-    MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, g.smem_bytes, st));
+    if (g.kernel == 2) {
+        // persistent: at most one CTA per SM walks the (DM block, tile, group) items
+        const long long nitems = (long long)g.nblk * ntiles * g.ngroups;
+        if (nitems > 0x7fffffffLL) return fail(MDSM_EINVAL, "block too long for one launch");
+        int dev = 0, sms = 0;
+        MDSM_CUDA_TRY(cudaGetDevice(&dev));
+        MDSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        int nt = (int)ntiles, ni = (int)nitems;
+        void *args[] = {&a, &nt, &ni};
+        const unsigned grid = (unsigned)std::min<long long>(sms, nitems);
+        MDSM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(kPThreads), args, g.smem_bytes, st));
+    } else {
+        if (ntiles > 65535 || g.ngroups > 65535)
+            return fail(MDSM_EINVAL, "block too long for one launch");
+        dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);
+        void *args[] = {&a};
+        MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kNW * 32), args, g.smem_bytes, st));
+    }
     if (launches) *launches += 1;
     return MDSM_OK;
 }
@@ -867,7 +977,7 @@ mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches
         const int grid = std::min(sms, b.nitems);
         k_shift_sum_u8x4_batch<<<grid, kPThreads, b.smem, st>>>(
             reinterpret_cast<const KArgs *>(b.d_kargs), reinterpret_cast<const int4 *>(b.d_items),
-            b.nitems, b.d_counter);
+            b.nitems, b.d_counter, b.rawcap, b.ps, b.d_err);
         MDSM_CUDA_TRY(cudaGetLastError());
         if (launches) *launches += 1;
     }

@@ -395,7 +395,11 @@ constexpr int kBoxThreads = 256;
 
 // One CTA per (DM, tile).  Region [t0 - HL, t0 + TILE + HL + wmax - 1) is staged in float.
 // Arithmetic per sample and width is FP32 (explicitly rounded, same order as the oracle); only
-// the per-DM statistics are FP64.
+// the per-DM statistics are FP64.  Each thread owns the positions tid + q * kBoxThreads: it
+// keeps their boxcar sums and their best SNR / width in registers across the widths, and
+// reads only the partner sum B[i + w/2] from shared memory, so one width costs one shared
+// load, one shared store and one barrier per position (the sums alternate between two
+// buffers).
 template <typename T>
 __global__ void __launch_bounds__(kBoxThreads)
     k_boxcar(const T *__restrict__ y, long long n, int nw, double threshold,
@@ -403,13 +407,14 @@ __global__ void __launch_bounds__(kBoxThreads)
              unsigned long long *__restrict__ count, long long cap)
 {
     extern __shared__ __align__(16) unsigned char sm[];
+    constexpr int PER = (kBoxTile + 2 * kBoxHaloL + 256 + kBoxThreads - 1) / kBoxThreads;
     const int wmax = 1 << (nw - 1);
     const int hl = max(wmax / 2, 1);
     const int span = kBoxTile + 2 * hl + wmax;  // staged samples
     const int nbest = kBoxTile + 2 * hl;        // positions with a best value
-    float *B = reinterpret_cast<float *>(sm);
-    float *best = B + span;
-    int *bw = reinterpret_cast<int *>(best + nbest);
+    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + span;
+    float *best_s = B1 + span;
+    int *bw_s = reinterpret_cast<int *>(best_s + nbest);
 
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
@@ -419,68 +424,89 @@ __global__ void __launch_bounds__(kBoxThreads)
     const long long t0 = (long long)blockIdx.x * kBoxTile;
     const long long r0 = t0 - hl;  // series index of B[0] and best[0]
     const T *r = y + (size_t)d * n;
-    for (int i = threadIdx.x; i < span; i += blockDim.x) {
+    const int tid = threadIdx.x;
+    float b[PER], best[PER];
+    int bw[PER];
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int i = tid + q * kBoxThreads;
         const long long t = r0 + i;
-        B[i] = (t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
-    }
-    for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
-        best[i] = -INFINITY;
-        bw[i] = 0;
+        b[q] = (i < span && t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
+        if (i < span) B0[i] = b[q];
+        best[q] = -INFINITY;
+        bw[q] = 0;
     }
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
     __shared__ float inv_w[9];
-    if (threadIdx.x < nw)
-        inv_w[threadIdx.x] = __double2float_rn(
-            __ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << threadIdx.x)))));
+    if (tid < nw)
+        inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
     __syncthreads();
-    constexpr int PER = (kBoxTile + 2 * 128 + 256 + kBoxThreads - 1) / kBoxThreads;
     for (int l = 0; l < nw; ++l) {
         const int w = 1 << l;
         if (l > 0) {
+            // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
             const int h = w >> 1;
-            float nv[PER];
+            const float *cur = (l & 1) ? B0 : B1;
+            float *nxt = (l & 1) ? B1 : B0;
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x + q * kBoxThreads;
-                nv[q] = (i + h < span) ? __fadd_rn(B[i], B[i + h]) : 0.0f;
-            }
-            __syncthreads();
-#pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int i = threadIdx.x + q * kBoxThreads;
-                if (i < span) B[i] = nv[q];
+                const int i = tid + q * kBoxThreads;
+                if (i < span) {
+                    b[q] = (i + h < span) ? __fadd_rn(b[q], cur[i + h]) : 0.0f;
+                    nxt[i] = b[q];
+                }
             }
             __syncthreads();
         }
         const float wm = __fmul_rn((float)w, mu_f);
         const float inv = inv_w[l];
-        for (int i = threadIdx.x; i < nbest; i += blockDim.x) {
+#pragma unroll
+        for (int q = 0; q < PER; ++q) {
+            const int i = tid + q * kBoxThreads;
             const long long t = r0 + i;
-            if (t < 0 || t + w > n) continue;
-            const float s = __fmul_rn(__fsub_rn(B[i], wm), inv);
-            if (s > best[i]) {
-                best[i] = s;
-                bw[i] = w;
+            if (i < nbest && t >= 0 && t + w <= n) {
+                const float s = __fmul_rn(__fsub_rn(b[q], wm), inv);
+                if (s > best[q]) {
+                    best[q] = s;
+                    bw[q] = w;
+                }
             }
         }
-        __syncthreads();
     }
-    for (int q = threadIdx.x; q < kBoxTile; q += blockDim.x) {
+#pragma unroll
+    for (int q = 0; q < PER; ++q) {
+        const int i = tid + q * kBoxThreads;
+        if (i < nbest) {
+            best_s[i] = best[q];
+            bw_s[i] = bw[q];
+        }
+    }
+    __syncthreads();
+    for (int q = tid; q < kBoxTile; q += blockDim.x) {
         const long long t = t0 + q;
         if (t >= n) break;
         const int i = q + hl;
-        const float b = best[i];
-        if (!(b >= thr)) continue;
-        const int h = max(bw[i] / 2, 1);
+        const float bv = best_s[i];
+        if (!(bv >= thr)) continue;
+        const int h = max(bw_s[i] / 2, 1);
         bool keep = true;
         for (int u = 1; u <= h && keep; ++u)
-            if (t - u >= 0 && !(best[i - u] < b)) keep = false;
+            if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
         for (int u = 1; u <= h && keep; ++u)
-            if (t + u <= n - 1 && !(best[i + u] <= b)) keep = false;
+            if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
         if (!keep) continue;
         const unsigned long long at = atomicAdd(count, 1ull);
-        if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw[i], b};
+        if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw_s[i], bv};
     }
+}
+
+// Shared memory of k_boxcar: two sum buffers of span floats, best (float) and width (int) of
+// nbest positions.
+static size_t boxcar_smem(int nwidths)
+{
+    const int wmax = 1 << (nwidths - 1);
+    const int hl = std::max(wmax / 2, 1);
+    return (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 8;
 }
 
 mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
@@ -505,9 +531,7 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
     auto *d_c = reinterpret_cast<DevCand *>(base + off_c);
     MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
     dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
-    const int wmax = 1 << (nwidths - 1);
-    const int hl = std::max(wmax / 2, 1);
-    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 4 + (size_t)(kBoxTile + 2 * hl) * 8;
+    const size_t smem = boxcar_smem(nwidths);
     dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
     if (dtype == MDSM_OUT_F32) {
         const float *y = static_cast<const float *>(d_series);
@@ -561,9 +585,7 @@ mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, 
                                             ((size_t)ndms * sizeof(double2) + 255) / 256 * 256);
     MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
     dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
-    const int wmax = 1 << (nwidths - 1);
-    const int hl = std::max(wmax / 2, 1);
-    const size_t smem = (size_t)(kBoxTile + 2 * hl + wmax) * 4 + (size_t)(kBoxTile + 2 * hl) * 8;
+    const size_t smem = boxcar_smem(nwidths);
     dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
     if (dtype == MDSM_OUT_F32) {
         const float *y = static_cast<const float *>(d_series);

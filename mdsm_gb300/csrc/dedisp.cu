@@ -220,6 +220,9 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 //    hold the four sums exactly and are added into int32 every 256 channels;
 //  * two channels share each 3-input integer add (A += wa + wz, O += odd(wa) + odd(wz)).
 // Per 4 sample-adds per channel: 1 LDS, 1 PRMT and one 3-input add.
+// A CTA is 19 compute warps of 2 DM trials (38 per tile; 20 warps keep 96 registers a thread)
+// and one producer warp that only issues the copies, so no compute warp carries the copy
+// latency into the per-chunk barrier.  One CTA per SM (the staging takes ~200 KB).
 // ------------------------------------------------------------------------------------------
 constexpr int kPNW = 19;            // compute warps
 constexpr int kPDPW = 2;            // DM trials per warp

@@ -400,21 +400,21 @@ constexpr int kBoxThreads = 256;
 // reads only the partner sum B[i + w/2] from shared memory, so one width costs one shared
 // load, one shared store and one barrier per position (the sums alternate between two
 // buffers).
-template <typename T>
+template <typename T, int NW>
 __global__ void __launch_bounds__(kBoxThreads)
-    k_boxcar(const T *__restrict__ y, long long n, int nw, double threshold,
+    k_boxcar(const T *__restrict__ y, long long n, double threshold,
              const double2 *__restrict__ musig, DevCand *__restrict__ cands,
              unsigned long long *__restrict__ count, long long cap)
 {
     extern __shared__ __align__(16) unsigned char sm[];
-    constexpr int PER = (kBoxTile + 2 * kBoxHaloL + 256 + kBoxThreads - 1) / kBoxThreads;
-    const int wmax = 1 << (nw - 1);
-    const int hl = max(wmax / 2, 1);
-    const int span = kBoxTile + 2 * hl + wmax;  // staged samples
-    const int nbest = kBoxTile + 2 * hl;        // positions with a best value
-    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + span;
-    float *best_s = B1 + span;
-    int *bw_s = reinterpret_cast<int *>(best_s + nbest);
+    constexpr int WMAX = 1 << (NW - 1);
+    constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
+    constexpr int SPAN = kBoxTile + 2 * HL + WMAX;  // staged samples
+    constexpr int NBEST = kBoxTile + 2 * HL;        // positions with a best value
+    constexpr int PER = (SPAN + kBoxThreads - 1) / kBoxThreads;
+    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + SPAN;
+    float *best_s = B1 + SPAN;
+    int *bw_s = reinterpret_cast<int *>(best_s + NBEST);
 
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
@@ -422,7 +422,9 @@ __global__ void __launch_bounds__(kBoxThreads)
     const float mu_f = __double2float_rn(mu);
     const float thr = __double2float_rn(threshold);
     const long long t0 = (long long)blockIdx.x * kBoxTile;
-    const long long r0 = t0 - hl;  // series index of B[0] and best[0]
+    const long long r0 = t0 - HL;  // series index of B[0] and best[0]
+    // every staged sample and every boxcar of the tile inside the series: no per-element tests
+    const bool interior = r0 >= 0 && r0 + SPAN <= n;
     const T *r = y + (size_t)d * n;
     const int tid = threadIdx.x;
     float b[PER], best[PER];
@@ -431,17 +433,18 @@ __global__ void __launch_bounds__(kBoxThreads)
     for (int q = 0; q < PER; ++q) {
         const int i = tid + q * kBoxThreads;
         const long long t = r0 + i;
-        b[q] = (i < span && t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
-        if (i < span) B0[i] = b[q];
+        b[q] = (i < SPAN && (interior || (t >= 0 && t < n))) ? (float)__ldg(r + t) : 0.0f;
+        if (i < SPAN) B0[i] = b[q];
         best[q] = -INFINITY;
         bw[q] = 0;
     }
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
-    __shared__ float inv_w[9];
-    if (tid < nw)
+    __shared__ float inv_w[NW];
+    if (tid < NW)
         inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
     __syncthreads();
-    for (int l = 0; l < nw; ++l) {
+#pragma unroll
+    for (int l = 0; l < NW; ++l) {
         const int w = 1 << l;
         if (l > 0) {
             // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
@@ -451,8 +454,8 @@ __global__ void __launch_bounds__(kBoxThreads)
 #pragma unroll
             for (int q = 0; q < PER; ++q) {
                 const int i = tid + q * kBoxThreads;
-                if (i < span) {
-                    b[q] = (i + h < span) ? __fadd_rn(b[q], cur[i + h]) : 0.0f;
+                if (i < SPAN) {
+                    b[q] = (i + h < SPAN) ? __fadd_rn(b[q], cur[i + h]) : 0.0f;
                     nxt[i] = b[q];
                 }
             }
@@ -464,28 +467,31 @@ __global__ void __launch_bounds__(kBoxThreads)
         for (int q = 0; q < PER; ++q) {
             const int i = tid + q * kBoxThreads;
             const long long t = r0 + i;
-            if (i < nbest && t >= 0 && t + w <= n) {
-                const float s = __fmul_rn(__fsub_rn(b[q], wm), inv);
-                if (s > best[q]) {
-                    best[q] = s;
+            if (i < NBEST && (interior || (t >= 0 && t + w <= n))) {
+                const float sv = __fmul_rn(__fsub_rn(b[q], wm), inv);
+                if (sv > best[q]) {
+                    best[q] = sv;
                     bw[q] = w;
                 }
             }
         }
     }
+    bool any = false;
 #pragma unroll
     for (int q = 0; q < PER; ++q) {
         const int i = tid + q * kBoxThreads;
-        if (i < nbest) {
+        if (i < NBEST) {
             best_s[i] = best[q];
             bw_s[i] = bw[q];
+            any |= best[q] >= thr;
         }
     }
-    __syncthreads();
+    // most tiles hold no sample over the threshold: skip the neighbourhood test there
+    if (!__syncthreads_or(any)) return;
     for (int q = tid; q < kBoxTile; q += blockDim.x) {
         const long long t = t0 + q;
         if (t >= n) break;
-        const int i = q + hl;
+        const int i = q + HL;
         const float bv = best_s[i];
         if (!(bv >= thr)) continue;
         const int h = max(bw_s[i] / 2, 1);
@@ -500,6 +506,12 @@ __global__ void __launch_bounds__(kBoxThreads)
     }
 }
 
+// The boxcar search of every DM row, for 1..9 widths (a template per width count).
+template <typename T>
+static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, double threshold,
+                                 const double2 *musig, DevCand *cands,
+                                 unsigned long long *count, long long cap, cudaStream_t st);
+
 // Shared memory of k_boxcar: two sum buffers of span floats, best (float) and width (int) of
 // nbest positions.
 static size_t boxcar_smem(int nwidths)
@@ -507,6 +519,33 @@ static size_t boxcar_smem(int nwidths)
     const int wmax = 1 << (nwidths - 1);
     const int hl = std::max(wmax / 2, 1);
     return (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 8;
+}
+
+template <typename T, int NW>
+static cudaError_t launch_boxcar_nw(const T *y, int ndms, long long n, double threshold,
+                                    const double2 *musig, DevCand *cands,
+                                    unsigned long long *count, long long cap, cudaStream_t st)
+{
+    const size_t smem = boxcar_smem(NW);
+    cudaError_t e = cudaFuncSetAttribute(k_boxcar<T, NW>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    dim3 g3((unsigned)((n + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
+    k_boxcar<T, NW><<<g3, kBoxThreads, smem, st>>>(y, n, threshold, musig, cands, count, cap);
+    return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, double threshold,
+                                 const double2 *musig, DevCand *cands,
+                                 unsigned long long *count, long long cap, cudaStream_t st)
+{
+    switch (nw) {
+#define BOX(K) case K: return launch_boxcar_nw<T, K>(y, ndms, n, threshold, musig, cands, count, cap, st)
+    BOX(1); BOX(2); BOX(3); BOX(4); BOX(5); BOX(6); BOX(7); BOX(8); BOX(9);
+#undef BOX
+    default: return cudaErrorInvalidValue;
+    }
 }
 
 mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
@@ -531,23 +570,17 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
     auto *d_c = reinterpret_cast<DevCand *>(base + off_c);
     MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
     dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
-    const size_t smem = boxcar_smem(nwidths);
-    dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
     if (dtype == MDSM_OUT_F32) {
         const float *y = static_cast<const float *>(d_series);
         k_series_chunk_sums<float><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
         k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
-        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<float>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_boxcar<float><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
-                                                       d_count, cap);
+        MDSM_CUDA_TRY(launch_boxcar(y, ndms, nsamp, nwidths, threshold, d_ms, d_c, d_count, cap,
+                                    st));
     } else {
         const int32_t *y = static_cast<const int32_t *>(d_series);
         k_series_stats_int<<<ndms, 256, 0, st>>>(y, nsamp, d_ms);
-        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<int32_t>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_boxcar<int32_t><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
-                                                         d_count, cap);
+        MDSM_CUDA_TRY(launch_boxcar(y, ndms, nsamp, nwidths, threshold, d_ms, d_c, d_count, cap,
+                                    st));
     }
     MDSM_CUDA_TRY(cudaGetLastError());
     return fetch_cands(d_c, d_count, cap, h_cands, ncand, st);
@@ -585,23 +618,17 @@ mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, 
                                             ((size_t)ndms * sizeof(double2) + 255) / 256 * 256);
     MDSM_CUDA_TRY(cudaMemsetAsync(d_count, 0, sizeof(unsigned long long), st));
     dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
-    const size_t smem = boxcar_smem(nwidths);
-    dim3 g3((unsigned)((nsamp + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
     if (dtype == MDSM_OUT_F32) {
         const float *y = static_cast<const float *>(d_series);
         k_series_chunk_sums<float><<<g1, 128, 0, st>>>(y, nsamp, nch, d_part);
         k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(d_part, ndms, nch, nsamp, d_ms);
-        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<float>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_boxcar<float><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
-                                                       d_count, cap);
+        MDSM_CUDA_TRY(launch_boxcar(y, ndms, nsamp, nwidths, threshold, d_ms, d_c, d_count, cap,
+                                    st));
     } else {
         const int32_t *y = static_cast<const int32_t *>(d_series);
         k_series_stats_int<<<ndms, 256, 0, st>>>(y, nsamp, d_ms);
-        MDSM_CUDA_TRY(cudaFuncSetAttribute(k_boxcar<int32_t>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        k_boxcar<int32_t><<<g3, kBoxThreads, smem, st>>>(y, nsamp, nwidths, threshold, d_ms, d_c,
-                                                         d_count, cap);
+        MDSM_CUDA_TRY(launch_boxcar(y, ndms, nsamp, nwidths, threshold, d_ms, d_c, d_count, cap,
+                                    st));
     }
     MDSM_CUDA_TRY(cudaGetLastError());
     MDSM_CUDA_TRY(cudaMemcpyAsync(h_count, d_count, sizeof(long long), cudaMemcpyDeviceToHost, st));

@@ -45,7 +45,10 @@ typedef enum {
 enum { MDSM_U8 = 0, MDSM_U16 = 1, MDSM_I16 = 2, MDSM_F32 = 3, MDSM_I32 = 4 };
 /* output (dedispersed series) types */
 enum { MDSM_OUT_F32 = 0, MDSM_OUT_I32 = 1 };
-/* accumulation: AUTO = exact INT32 for integer samples, FP32 for float samples */
+/* accumulation: AUTO = exact INT32 for integer samples whose sums over all channels fit INT32,
+ * else FP32 (integer samples: exact INT32 sums per 16 channels, Kahan-compensated FP32 across
+ * them); I32 is refused (MDSM_ERANGE) where the sums may not fit.  The plan info reports the
+ * accumulation in effect (I32 or F32). */
 enum { MDSM_ACC_AUTO = 0, MDSM_ACC_I32 = 1, MDSM_ACC_F32 = 2 };
 
 /* How a DM trial's integer sample shift is formed (all computed once, on the host, into a

@@ -39,7 +39,7 @@ struct KArgs {
     const int32_t *rel;                      // [g][blk][c][DB]
     const int32_t *sminspan;                 // [g][blk][c][2]
     int nchans, ndms, nsamp, nblk, rowcap, nst, out_i32;
-    int ps;  // packed kernel: bytes per phase copy of a staged row
+    int ps;  // packed kernels: bytes per phase copy of a staged row
     unsigned *err;
 };
 
@@ -205,43 +205,57 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 }
 
 // ------------------------------------------------------------------------------------------
-// Packed 8-bit kernel (uint8 samples, exact integer sums).
+// Packed kernels (uint8 and uint16 samples, exact integer sums).
 //
 // The generic kernel spends one shared-memory load per add, which caps it at 32 adds per
-// clock per SM (the 128 B/clk shared-memory port).  Here one 32-bit load brings four
-// consecutive samples:
-//  * each staged row is expanded once into four phase copies, P_a[j] = bytes 4j+a .. 4j+a+3,
-//    so any run of 4 samples starting at any offset is one aligned word, and a warp's 32
-//    lanes read 32 consecutive words (no bank conflicts);
-//  * the raw words are summed as 32-bit integers, A = sum w (mod 2^32), and one PRMT per word
-//    extracts the odd samples as zero-extended 16-bit lanes, O = sum (s1 | s3 << 16);
-//  * since w = (s0 | s2 << 16) + 2^8 (s1 | s3 << 16), E = A - 2^8 O = sum (s0 | s2 << 16)
-//    (mod 2^32); over at most 256 channels every lane sum is <= 256 * 255 < 2^16, so E and O
-//    hold the four sums exactly and are added into int32 every 256 channels;
+// clock per SM (the 128 B/clk shared-memory port).  Here one 32-bit load brings several
+// consecutive samples (4 uint8 or 2 uint16):
+//  * each staged row is expanded once into phase copies, P_a[j] = the word starting at sample
+//    (words per sample) * j + a, so any run of samples starting at any offset is one aligned
+//    word, and a warp's 32 lanes read 32 consecutive words (no bank conflicts);
+//  * the raw words are summed as 32-bit integers, A = sum w (mod 2^32), and one extraction per
+//    word sums the odd samples separately: uint8, O = sum (s1 | s3 << 16) by one PRMT; uint16,
+//    O = sum s1 by one shift;
+//  * w = (even lanes) + 2^(8*bytes) O, so E = A - 2^(8*bytes) O (mod 2^32) are the even lanes'
+//    sums; over at most 256 channels every uint8 lane sum is <= 256 * 255 < 2^16 and every
+//    uint16 one < 2^32, so E and O hold the sums exactly; they are added into int32 every
+//    256 channels;
 //  * two channels share each 3-input integer add (A += wa + wz, O += odd(wa) + odd(wz)).
-// Per 4 sample-adds per channel: 1 LDS, 1 PRMT and one 3-input add.
-// A CTA is 19 compute warps of 2 DM trials (38 per tile; 20 warps keep 96 registers a thread)
-// and one producer warp that only issues the copies, so no compute warp carries the copy
-// latency into the per-chunk barrier.  One CTA per SM (the staging takes ~200 KB).
+// Per word (4 or 2 sample-adds) and channel: 1 LDS, 1 PRMT or shift, one 3-input add.
+// A CTA is NW compute warps of DPW DM trials each and one producer warp that only issues the
+// copies, so no compute warp carries the copy latency into the per-chunk barrier; uint8 uses
+// 19 x 2 (38 trials a tile; 20 warps keep 96 registers a thread), uint16 (the second subband
+// stage, 16 trials per call) 16 x 1.  One CTA per SM (the staging takes ~200 KB).
 // ------------------------------------------------------------------------------------------
-constexpr int kPNW = 19;            // compute warps
-constexpr int kPDPW = 2;            // DM trials per warp
-constexpr int kPR4 = 4;             // 4-sample words per lane per DM trial
-constexpr int kPCC = 16;            // channels per stage
-constexpr int kPNR = 3;             // raw stages in flight
-constexpr int kPT = 128 * kPR4;     // samples per tile (512)
-constexpr int kPDB = kPNW * kPDPW;  // DM trials per tile (38)
-constexpr int kPDBS = (kPDB + 3) / 4 * 4;  // offsets per channel as stored: whole 16-byte units
-constexpr int kPThreads = (kPNW + 1) * 32;  // compute warps + one producer warp (index kPNW)
-static_assert(kPNW >= kPCC, "one compute warp per staged row expands it");
-static_assert(kPNW * 32 == kPCC * kPDB, "one compute thread per staged offset");
+constexpr int kPCC = 16;         // channels per stage
+constexpr int kPNR = 3;          // raw stages in flight
+constexpr int kPT = 512;         // samples per tile
 
-// Work items of the packed kernel are (beam, DM block, time tile, group) tiles; a CTA runs a
+template <int SW_, int NW_, int DPW_, bool U16OUT_ = false>
+struct PackedCfg {
+    static constexpr bool U16OUT = U16OUT_;       // store the sums as uint16
+    static constexpr int SW = SW_;                // bytes per sample
+    static constexpr int SPW = 4 / SW;            // samples per word = phase copies
+    static constexpr int NW = NW_;                // compute warps (the producer is warp NW)
+    static constexpr int DPW = DPW_;              // DM trials per compute warp
+    static constexpr int PRW = kPT / (32 * SPW);  // words per lane per DM trial
+    static constexpr int DB = NW * DPW;           // DM trials per tile
+    static constexpr int DBS = (DB + 3) / 4 * 4;  // offsets per channel as stored (16-byte rows)
+    static constexpr int THREADS = (NW + 1) * 32;
+    static_assert(NW >= kPCC, "one compute warp per staged row expands it");
+    static_assert(NW * 32 >= kPCC * DB, "the compute threads copy a chunk's offsets");
+    static_assert(DPW == 1 || DPW == 2, "one or two DM trials per warp");
+};
+using CfgU8 = PackedCfg<1, 19, 2>;
+using CfgU8to16 = PackedCfg<1, 19, 2, true>;  // the first subband stage: uint16 subband series
+using CfgU16 = PackedCfg<2, 16, 1>;
+
+// Work items of the packed kernels are (beam, DM block, time tile, group) tiles; a CTA runs a
 // stream of them.  The producer warp stages the stream's chunks (16 channels of one item) into
 // a ring of kPNR stages, running ahead across item boundaries, and writes each chunk's
 // (item, chunk index, channels, flags) beside it; the compute warps take the chunks in order,
 // start an item's sums on its first chunk and store them after its last.  So short items
-// (few channels, as in the first subband stage) keep the copies in flight between items.
+// (few channels, as in the subband stages) keep the copies in flight between items.
 constexpr int kChunkFirst = 1, kChunkLast = 2, kChunkStop = 4;
 
 // CTA barrier 0 returning whether any thread passed true.  The producer and the compute warps
@@ -295,92 +309,104 @@ struct ListItems {
     __device__ const KArgs &args(int beam) const { return beams[beam]; }
 };
 
-template <class Src>
+// The odd samples of a word as 32-bit lanes: uint8, (s1, s3) as uint16 lanes; uint16, s1.
+template <int SW>
+__device__ __forceinline__ uint32_t odd_lanes(uint32_t w)
+{
+    if constexpr (SW == 1)
+        return __byte_perm(w, 0u, 0x4341);
+    else
+        return w >> 16;
+}
+
+template <class Cfg, class Src>
 __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int rawcap, int ps,
                                               unsigned *err)
 {
+    constexpr int SW = Cfg::SW, SPW = Cfg::SPW, NW = Cfg::NW, DPW = Cfg::DPW, PRW = Cfg::PRW;
+    constexpr int DB = Cfg::DB, DBS = Cfg::DBS;
     const int nwp = ps >> 2;  // words per phase copy
     const int nq = nwp >> 2;  // 16-byte quads per phase copy
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     int4 *meta = reinterpret_cast<int4 *>(smem + 64);  // kPNR entries
     unsigned char *raw = smem + 128;
     int32_t *offsm = reinterpret_cast<int32_t *>(raw + (size_t)kPNR * kPCC * rawcap);
-    int32_t *offcur = offsm + kPNR * kPCC * kPDBS;                // 2 x kPCC x kPDBS
-    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + 2 * kPCC * kPDBS);  // 2 x kPCC x 4 x nwp
+    int32_t *offcur = offsm + kPNR * kPCC * DBS;                 // 2 x kPCC x DBS
+    uint32_t *P = reinterpret_cast<uint32_t *>(offcur + 2 * kPCC * DBS);  // 2 x kPCC x SPW x nwp
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
 
-    // ---- producer state (warp kPNW): the item being staged, its next chunk, and the lane's
-    // (smin, span) for that chunk, loaded one fill ahead so that no fill waits on a global load
-    int p_it = -1, p_k = 0, p_nchunks = 0;
-    int4 p_w = make_int4(0, 0, 0, 0);
-    int2 p_ss = make_int2(0, 0);
-    auto p_next_item = [&]() {
-        int it = 0;
-        if (lane == 0) it = src.grab();
-        p_it = __shfl_sync(0xffffffffu, it, 0);
-        p_k = 0;
-        if (p_it >= 0) {
-            p_w = src.item(p_it);
-            p_nchunks = (src.args(p_w.x).nchans + kPCC - 1) / kPCC;
-        }
-    };
-    auto p_load_ss = [&]() {
-        if (p_it < 0) return;
-        const KArgs &a = src.args(p_w.x);
-        const int c = p_k * kPCC + lane;
-        if (c < a.nchans) {
+    if (warp == NW) {
+        // ---- producer: the item being staged, its next chunk, and the lane's (smin, span)
+        // for that chunk, loaded one fill ahead so that no fill waits on a global load
+        int p_it = -1, p_k = 0, p_nchunks = 0;
+        int4 p_w = make_int4(0, 0, 0, 0);
+        int2 p_ss = make_int2(0, 0);
+        auto p_next_item = [&]() {
+            int it = 0;
+            if (lane == 0) it = src.grab();
+            p_it = __shfl_sync(0xffffffffu, it, 0);
+            p_k = 0;
+            if (p_it >= 0) {
+                p_w = src.item(p_it);
+                p_nchunks = (src.args(p_w.x).nchans + kPCC - 1) / kPCC;
+            }
+        };
+        auto p_load_ss = [&]() {
+            if (p_it < 0) return;
+            const KArgs &a = src.args(p_w.x);
+            const int c = p_k * kPCC + lane;
+            if (c < a.nchans) {
+                const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
+                p_ss = __ldg(reinterpret_cast<const int2 *>(a.sminspan + bofs * 2) + c);
+            }
+        };
+        // Stage the next chunk of the stream into stage s (or mark the end of the stream).
+        auto fill_next = [&](int s) {
+            if (p_it < 0) {
+                if (lane == 0) {
+                    meta[s] = make_int4(-1, 0, 0, kChunkStop);
+                    mbar_arrive(&bars[s]);
+                }
+                __syncwarp();
+                return;
+            }
+            const KArgs &a = src.args(p_w.x);
+            const long long t0 = (long long)p_w.z * kPT;
             const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
-            p_ss = __ldg(reinterpret_cast<const int2 *>(a.sminspan + bofs * 2) + c);
-        }
-    };
-    // Stage the next chunk of the stream into stage s (or mark the end of the stream).
-    auto fill_next = [&](int s) {
-        if (p_it < 0) {
+            const int c0 = p_k * kPCC;
+            const int nc = min(kPCC, a.nchans - c0);
+            unsigned bytes = 0;
+            const unsigned char *src_row = nullptr;
+            if (lane < nc) {
+                const int c = c0 + lane;
+                const long long start = t0 + p_ss.x;
+                const long long end = start + kPT + p_ss.y;
+                const long long sb = (start * SW) & ~15LL;  // bytes
+                const long long eb = (end * SW + 15) & ~15LL;
+                bytes = (unsigned)(eb - sb);
+                src_row = a.in + (size_t)(p_w.w * a.in_group_stride) * SW +
+                          (size_t)c * (size_t)a.in_stride * SW + sb;
+            }
+            const unsigned offbytes = (unsigned)(nc * DBS * 4);
+            const unsigned total = warp_sum_u32(bytes) + offbytes;
+            __syncwarp();
             if (lane == 0) {
-                meta[s] = make_int4(-1, 0, 0, kChunkStop);
-                mbar_arrive(&bars[s]);
+                meta[s] = make_int4(p_it, p_k, nc,
+                                    (p_k == 0 ? kChunkFirst : 0) |
+                                        (p_k == p_nchunks - 1 ? kChunkLast : 0));
+                mbar_arrive_expect_tx(&bars[s], total);  // releases the meta entry with the phase
             }
             __syncwarp();
-            return;
-        }
-        const KArgs &a = src.args(p_w.x);
-        const long long t0 = (long long)p_w.z * kPT;
-        const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
-        const int c0 = p_k * kPCC;
-        const int nc = min(kPCC, a.nchans - c0);
-        unsigned bytes = 0;
-        const unsigned char *src_row = nullptr;
-        if (lane < nc) {
-            const int c = c0 + lane;
-            const long long start = t0 + p_ss.x;
-            const long long end = start + kPT + p_ss.y;
-            const long long sb = start & ~15LL;
-            const long long eb = (end + 15) & ~15LL;
-            bytes = (unsigned)(eb - sb);
-            src_row = a.in + (size_t)(p_w.w * a.in_group_stride) +
-                      (size_t)c * (size_t)a.in_stride + sb;
-        }
-        const unsigned offbytes = (unsigned)(nc * kPDBS * 4);
-        const unsigned total = warp_sum_u32(bytes) + offbytes;
-        __syncwarp();
-        if (lane == 0) {
-            meta[s] = make_int4(p_it, p_k, nc,
-                                (p_k == 0 ? kChunkFirst : 0) |
-                                    (p_k == p_nchunks - 1 ? kChunkLast : 0));
-            mbar_arrive_expect_tx(&bars[s], total);  // releases the meta entry with the phase
-        }
-        __syncwarp();
-        if (lane < nc)
-            bulk_g2s(raw + (size_t)(s * kPCC + lane) * rawcap, src_row, bytes, &bars[s]);
-        if (lane == 0)
-            bulk_g2s(offsm + s * kPCC * kPDBS, a.rel + (bofs + (size_t)c0) * kPDBS, offbytes,
-                     &bars[s]);
-        if (++p_k == p_nchunks) p_next_item();
-        p_load_ss();
-    };
-    if (warp == kPNW) {
-        // The producer's loop: one CTA barrier per chunk, as the compute warps', then the
-        // refill of the stage every warp has just finished expanding.
+            if (lane < nc)
+                bulk_g2s(raw + (size_t)(s * kPCC + lane) * rawcap, src_row, bytes, &bars[s]);
+            if (lane == 0)
+                bulk_g2s(offsm + s * kPCC * DBS, a.rel + (bofs + (size_t)c0) * DBS, offbytes,
+                         &bars[s]);
+            if (++p_k == p_nchunks) p_next_item();
+            p_load_ss();
+        };
+        // One CTA barrier per chunk, as the compute warps', then the refill of the stage every
+        // warp has just finished expanding.
         p_next_item();
         p_load_ss();
         for (int i = 0; i < kPNR; ++i) fill_next(i);
@@ -399,9 +425,9 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
     }
 
     // ---- compute warps ----
-    uint32_t A[kPDPW][kPR4];    // raw 4-sample words summed mod 2^32 (<= 256 channels)
-    uint32_t O[kPDPW][kPR4];    // odd samples (s1, s3) as uint16 lanes (<= 256 channels)
-    int32_t f[kPDPW][kPR4][4];  // int32 sums
+    uint32_t A[DPW][PRW];        // raw words summed mod 2^32 (<= 256 channels)
+    uint32_t O[DPW][PRW];        // odd lanes summed (<= 256 channels)
+    int32_t f[DPW][PRW][SPW];    // int32 sums
 
     unsigned gk = 0;  // chunk sequence number
     bool aborted = false;
@@ -412,7 +438,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         const bool ok = mbar_wait_bounded(&bars[s], par, err, ERR_WAIT_TIMEOUT);
         const int4 m = ok ? meta[s] : make_int4(-1, 0, 0, 0);
         if (ok) {
-            // Expand staged row `warp` into its four phase copies (16-byte loads and stores).
+            // Expand staged row `warp` into its phase copies (16-byte loads and stores).
             // P[pb] was last read for chunk gk-2, before the barrier of chunk gk-1.  All 16
             // rows are expanded whatever the chunk holds (rows past its channels, or the whole
             // stage at the end of the stream, hold earlier data nobody reads), so the
@@ -420,29 +446,27 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             if (warp < kPCC) {
                 const uint32_t *W =
                     reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + warp) * rawcap);
-                uint32_t *Pr = P + ((size_t)pb * kPCC + warp) * 4 * nwp;
+                uint32_t *Pr = P + ((size_t)pb * kPCC + warp) * SPW * nwp;
                 for (int i = lane; i < nq; i += 32) {
                     const uint4 w = reinterpret_cast<const uint4 *>(W)[i];
                     const uint32_t w4 = W[4 * i + 4];
                     reinterpret_cast<uint4 *>(Pr)[i] = w;
-                    reinterpret_cast<uint4 *>(Pr + nwp)[i] =
-                        make_uint4(__funnelshift_r(w.x, w.y, 8), __funnelshift_r(w.y, w.z, 8),
-                                   __funnelshift_r(w.z, w.w, 8), __funnelshift_r(w.w, w4, 8));
-                    reinterpret_cast<uint4 *>(Pr + 2 * nwp)[i] =
-                        make_uint4(__funnelshift_r(w.x, w.y, 16), __funnelshift_r(w.y, w.z, 16),
-                                   __funnelshift_r(w.z, w.w, 16), __funnelshift_r(w.w, w4, 16));
-                    reinterpret_cast<uint4 *>(Pr + 3 * nwp)[i] =
-                        make_uint4(__funnelshift_r(w.x, w.y, 24), __funnelshift_r(w.y, w.z, 24),
-                                   __funnelshift_r(w.z, w.w, 24), __funnelshift_r(w.w, w4, 24));
+#pragma unroll
+                    for (int a = 1; a < SPW; ++a)
+                        reinterpret_cast<uint4 *>(Pr + a * nwp)[i] =
+                            make_uint4(__funnelshift_r(w.x, w.y, 8 * SW * a),
+                                       __funnelshift_r(w.y, w.z, 8 * SW * a),
+                                       __funnelshift_r(w.z, w.w, 8 * SW * a),
+                                       __funnelshift_r(w.w, w4, 8 * SW * a));
                 }
             }
-            {  // one real entry per compute thread (the padding of the stored rows is not read)
-                const int i = tid / kPDB * kPDBS + tid % kPDB;
-                offcur[pb * kPCC * kPDBS + i] = offsm[s * kPCC * kPDBS + i];
+            if (tid < kPCC * DB) {  // one real entry per thread (the row padding is not read)
+                const int i = tid / DB * DBS + tid % DB;
+                offcur[pb * kPCC * DBS + i] = offsm[s * kPCC * DBS + i];
             }
         }
-        // Every thread that waited saw the same entry, so `stop` agrees across the CTA when
-        // no wait ran out.
+        // Every thread that waited saw the same entry, so the stop flag agrees across the CTA
+        // when no wait ran out.
         if (cta_any(!ok)) {
             aborted = true;
             break;
@@ -451,40 +475,51 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         const int nc = m.z;
         if (m.w & kChunkFirst) {
 #pragma unroll
-            for (int j = 0; j < kPDPW; ++j)
+            for (int j = 0; j < DPW; ++j)
 #pragma unroll
-                for (int r = 0; r < kPR4; ++r) {
+                for (int r = 0; r < PRW; ++r) {
                     A[j][r] = O[j][r] = 0u;
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) f[j][r][e] = 0;
+                    for (int e = 0; e < SPW; ++e) f[j][r][e] = 0;
                 }
         }
         const unsigned char *pbase =
-            reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * 4 * nwp) + lane * 4;
-        const int32_t *oc = offcur + pb * kPCC * kPDBS + warp * kPDPW;
-        static_assert(kPDPW == 2, "the channel loop below handles two DM trials per warp");
-        // Two channels per step: A += wa + wz and O += odd(wa) + odd(wz) are one 3-input
-        // integer add each.
-        int ci = 0;
-        auto pair = [&](int c) {
-            const unsigned char *pa = pbase + (size_t)c * 4 * ps;
-            const unsigned char *pz = pa + 4 * ps;
-            const int2 oa = *reinterpret_cast<const int2 *>(oc + c * kPDBS);
-            const int2 oz = *reinterpret_cast<const int2 *>(oc + (c + 1) * kPDBS);
-            const uint32_t *a0 = reinterpret_cast<const uint32_t *>(pa + oa.x);
-            const uint32_t *a1 = reinterpret_cast<const uint32_t *>(pa + oa.y);
-            const uint32_t *z0 = reinterpret_cast<const uint32_t *>(pz + oz.x);
-            const uint32_t *z1 = reinterpret_cast<const uint32_t *>(pz + oz.y);
-#pragma unroll
-            for (int r = 0; r < kPR4; ++r) {
-                const uint32_t wa0 = a0[32 * r], wa1 = a1[32 * r];
-                const uint32_t wz0 = z0[32 * r], wz1 = z1[32 * r];
-                A[0][r] = A[0][r] + wa0 + wz0;
-                O[0][r] += __byte_perm(wa0, 0u, 0x4341) + __byte_perm(wz0, 0u, 0x4341);
-                A[1][r] = A[1][r] + wa1 + wz1;
-                O[1][r] += __byte_perm(wa1, 0u, 0x4341) + __byte_perm(wz1, 0u, 0x4341);
+            reinterpret_cast<const unsigned char *>(P + (size_t)pb * kPCC * SPW * nwp) + lane * 4;
+        const int32_t *oc = offcur + pb * kPCC * DBS + warp * DPW;
+        // this warp's DM trials' word offsets (bytes) in channel c's phase-expanded row
+        auto offs = [&](int c, int (&o)[DPW]) {
+            if constexpr (DPW == 2) {
+                const int2 v = *reinterpret_cast<const int2 *>(oc + c * DBS);
+                o[0] = v.x;
+                o[1] = v.y;
+            } else {
+                o[0] = oc[c * DBS];
             }
         };
+        // Two channels per step: A += wa + wz and O += odd(wa) + odd(wz) are one 3-input
+        // integer add each.
+        auto pair = [&](int c) {
+            const unsigned char *pa = pbase + (size_t)c * SPW * ps;
+            const unsigned char *pz = pa + SPW * ps;
+            int oa[DPW], oz[DPW];
+            offs(c, oa);
+            offs(c + 1, oz);
+#pragma unroll
+            for (int r = 0; r < PRW; ++r) {
+                uint32_t wa[DPW], wz[DPW];
+#pragma unroll
+                for (int j = 0; j < DPW; ++j) {
+                    wa[j] = reinterpret_cast<const uint32_t *>(pa + oa[j])[32 * r];
+                    wz[j] = reinterpret_cast<const uint32_t *>(pz + oz[j])[32 * r];
+                }
+#pragma unroll
+                for (int j = 0; j < DPW; ++j) {
+                    A[j][r] = A[j][r] + wa[j] + wz[j];
+                    O[j][r] += odd_lanes<SW>(wa[j]) + odd_lanes<SW>(wz[j]);
+                }
+            }
+        };
+        int ci = 0;
         if (nc == kPCC) {
 #pragma unroll
             for (int c = 0; c < kPCC; c += 2) pair(c);
@@ -494,62 +529,88 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             for (; ci + 1 < nc; ci += 2) pair(ci);
         }
         if (ci < nc) {  // odd channel count: the last channel alone
-            const unsigned char *pa = pbase + (size_t)ci * 4 * ps;
-            const int2 oa = *reinterpret_cast<const int2 *>(oc + ci * kPDBS);
-            const uint32_t *a0 = reinterpret_cast<const uint32_t *>(pa + oa.x);
-            const uint32_t *a1 = reinterpret_cast<const uint32_t *>(pa + oa.y);
+            const unsigned char *pa = pbase + (size_t)ci * SPW * ps;
+            int oa[DPW];
+            offs(ci, oa);
 #pragma unroll
-            for (int r = 0; r < kPR4; ++r) {
-                const uint32_t wa0 = a0[32 * r], wa1 = a1[32 * r];
-                A[0][r] += wa0;
-                O[0][r] += __byte_perm(wa0, 0u, 0x4341);
-                A[1][r] += wa1;
-                O[1][r] += __byte_perm(wa1, 0u, 0x4341);
-            }
+            for (int r = 0; r < PRW; ++r)
+#pragma unroll
+                for (int j = 0; j < DPW; ++j) {
+                    const uint32_t wa = reinterpret_cast<const uint32_t *>(pa + oa[j])[32 * r];
+                    A[j][r] += wa;
+                    O[j][r] += odd_lanes<SW>(wa);
+                }
         }
         const bool last = (m.w & kChunkLast) != 0;
         if (((m.y + 1) & 15) == 0 || last) {
-            // A = E + 2^8 O (mod 2^32) with E = (s0, s2) as uint16 lanes: every lane sum is at
-            // most 256 * 255 < 2^16, so E and O hold the four sums exactly.
+            // A = E + 2^(8 SW) O (mod 2^32): E and O hold the lane sums exactly
 #pragma unroll
-            for (int j = 0; j < kPDPW; ++j)
+            for (int j = 0; j < DPW; ++j)
 #pragma unroll
-                for (int r = 0; r < kPR4; ++r) {
-                    const uint32_t E = A[j][r] - (O[j][r] << 8);
-                    f[j][r][0] += (int32_t)(E & 0xFFFFu);
-                    f[j][r][2] += (int32_t)(E >> 16);
-                    f[j][r][1] += (int32_t)(O[j][r] & 0xFFFFu);
-                    f[j][r][3] += (int32_t)(O[j][r] >> 16);
+                for (int r = 0; r < PRW; ++r) {
+                    const uint32_t E = A[j][r] - (O[j][r] << (8 * SW));
+                    if constexpr (SW == 1) {
+                        f[j][r][0] += (int32_t)(E & 0xFFFFu);
+                        f[j][r][2] += (int32_t)(E >> 16);
+                        f[j][r][1] += (int32_t)(O[j][r] & 0xFFFFu);
+                        f[j][r][3] += (int32_t)(O[j][r] >> 16);
+                    } else {
+                        f[j][r][0] += (int32_t)E;
+                        f[j][r][1] += (int32_t)O[j][r];
+                    }
                     A[j][r] = O[j][r] = 0u;
                 }
         }
         if (!last) continue;
-        // the item's sums are complete: store them
-        const int4 w = src.item(__shfl_sync(0xffffffffu, m.x, 0));
+        // the item's sums are complete: store them (int32, float32 or, for the uint16 subband
+        // series of the first stage, uint16)
+        const int4 w = src.item(m.x);
         const KArgs &a = src.args(w.x);
         const long long t0 = (long long)w.z * kPT;
+        constexpr bool U16OUT = Cfg::U16OUT;
+        constexpr int osz = U16OUT ? 2 : 4;
 #pragma unroll
-        for (int j = 0; j < kPDPW; ++j) {
-            const int d = w.y * kPDB + warp * kPDPW + j;
+        for (int j = 0; j < DPW; ++j) {
+            const int d = w.y * DB + warp * DPW + j;
             if (d >= a.ndms) continue;
             unsigned char *orow =
-                a.out + (size_t)(w.w * a.out_group_stride + (long long)d * a.out_stride) * 4;
+                a.out + (size_t)(w.w * a.out_group_stride + (long long)d * a.out_stride) * osz;
 #pragma unroll
-            for (int r = 0; r < kPR4; ++r) {
-                const long long t = t0 + 4 * (lane + 32 * r);
-                if (t + 3 < a.nsamp && ((((uintptr_t)orow) | (t * 4)) & 15) == 0) {
-                    if (a.out_i32)
+            for (int r = 0; r < PRW; ++r) {
+                const long long t = t0 + SPW * (lane + 32 * r);
+                const bool whole = t + SPW - 1 < a.nsamp &&
+                                   ((((uintptr_t)orow) | (t * osz)) & (SPW * osz - 1)) == 0;
+                if (whole && U16OUT) {
+                    if constexpr (SPW == 4)
+                        *reinterpret_cast<uint2 *>(orow + t * 2) =
+                            make_uint2((uint32_t)f[j][r][0] | ((uint32_t)f[j][r][1] << 16),
+                                       (uint32_t)f[j][r][2] | ((uint32_t)f[j][r][3] << 16));
+                    else
+                        *reinterpret_cast<uint32_t *>(orow + t * 2) =
+                            (uint32_t)f[j][r][0] | ((uint32_t)f[j][r][1] << 16);
+                } else if (whole && a.out_i32) {
+                    if constexpr (SPW == 4)
                         *reinterpret_cast<int4 *>(orow + t * 4) =
                             make_int4(f[j][r][0], f[j][r][1], f[j][r][2], f[j][r][3]);
                     else
+                        *reinterpret_cast<int2 *>(orow + t * 4) = make_int2(f[j][r][0], f[j][r][1]);
+                } else if (whole) {
+                    if constexpr (SPW == 4)
                         *reinterpret_cast<float4 *>(orow + t * 4) =
                             make_float4((float)f[j][r][0], (float)f[j][r][1], (float)f[j][r][2],
                                         (float)f[j][r][3]);
+                    else
+                        *reinterpret_cast<float2 *>(orow + t * 4) =
+                            make_float2((float)f[j][r][0], (float)f[j][r][1]);
                 } else {
 #pragma unroll
-                    for (int e = 0; e < 4; ++e)
-                        if (t + e < a.nsamp)
+                    for (int e = 0; e < SPW; ++e) {
+                        if (t + e >= a.nsamp) continue;
+                        if (U16OUT)
+                            reinterpret_cast<uint16_t *>(orow)[t + e] = (uint16_t)f[j][r][e];
+                        else
                             store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
+                    }
                 }
             }
         }
@@ -572,19 +633,20 @@ __device__ __forceinline__ void packed_init_barriers(unsigned char *smem)
 }
 
 // One plan: a persistent grid of at most one CTA per SM over the plan's items.
-__global__ void __launch_bounds__(kPThreads, 1)
-    k_shift_sum_u8x4(const __grid_constant__ KArgs a, int ntiles, int nitems)
+template <class Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, 1)
+    k_shift_sum_packed(const __grid_constant__ KArgs a, int ntiles, int nitems)
 {
     extern __shared__ __align__(128) unsigned char smem[];
     packed_init_barriers(smem);
     OnePlanItems src{&a, ntiles, nitems, (int)blockIdx.x};
-    packed_stream(src, smem, a.rowcap, a.ps, a.err);
+    packed_stream<Cfg>(src, smem, a.rowcap, a.ps, a.err);
 }
 
-// Several plans (beams that may differ in channels, samples and DM plan) from one work list,
-// sharing one staging geometry (rowcap, ps) so the shared-memory layout is the same for every
-// item.
-__global__ void __launch_bounds__(kPThreads, 1)
+// Several uint8 plans (beams that may differ in channels, samples and DM plan) from one work
+// list, sharing one staging geometry (rowcap, ps) so the shared-memory layout is the same for
+// every item.
+__global__ void __launch_bounds__(CfgU8::THREADS, 1)
     k_shift_sum_u8x4_batch(const KArgs *__restrict__ beams, const int4 *__restrict__ items,
                            int nitems, unsigned *__restrict__ counter, int rawcap, int ps,
                            unsigned *err)
@@ -592,7 +654,7 @@ __global__ void __launch_bounds__(kPThreads, 1)
     extern __shared__ __align__(128) unsigned char smem[];
     packed_init_barriers(smem);
     ListItems src{beams, items, nitems, counter};
-    packed_stream(src, smem, rawcap, ps, err);
+    packed_stream<CfgU8>(src, smem, rawcap, ps, err);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -688,17 +750,54 @@ int tile_tables(StageGeom &g, const std::vector<int32_t> &S)
     return maxspan;
 }
 
+template <class Cfg>
 size_t packed_smem(int rawcap, int ps)
 {
-    return 128 + (size_t)kPNR * kPCC * rawcap + (size_t)kPNR * kPCC * kPDBS * 4 +
-           (size_t)2 * kPCC * kPDBS * 4 + (size_t)2 * kPCC * 4 * ps;
+    return 128 + (size_t)kPNR * kPCC * rawcap + (size_t)kPNR * kPCC * Cfg::DBS * 4 +
+           (size_t)2 * kPCC * Cfg::DBS * 4 + (size_t)2 * kPCC * Cfg::SPW * ps;
+}
+
+// Packed tables for configuration Cfg: offsets of (c, d)'s first word inside the channel's
+// phase-expanded row (bytes), stored DBS per channel (the padding stays 0).  False if the
+// staging does not fit in shared memory.
+template <class Cfg>
+bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
+{
+    g.Db = Cfg::DB;
+    g.T = kPT;
+    g.R = Cfg::PRW * Cfg::SPW;
+    g.DPW = Cfg::DPW;
+    g.cc = kPCC;
+    g.nst = kPNR;
+    const int maxspan = tile_tables(g, S);
+    // raw row: the tile plus the span, from the 16-byte boundary below smin, in bytes
+    const int rawcap =
+        (int)(((long long)(kPT + maxspan) * Cfg::SW + 32 + 15) / 16 * 16) + 16;
+    const int ps = rawcap - 16;  // nwp = ps/4 words; the expansion reads word nwp too
+    if (packed_smem<Cfg>(rawcap, ps) > 220 * 1024) return false;
+    g.max_span = maxspan;
+    g.rowcap = rawcap;
+    g.ps = ps;
+    const int lomask = 16 / Cfg::SW - 1;  // samples before smin in its 16-byte unit
+    std::vector<int32_t> off(g.sminspan.size() / 2 * Cfg::DBS, 0);
+    for (size_t o = 0; o < g.sminspan.size() / 2; ++o) {
+        const int lo = g.sminspan[o * 2] & lomask;
+        for (int j = 0; j < g.Db; ++j) {
+            const int e = lo + g.rel[o * g.Db + j];  // samples from the staged row's start
+            off[o * Cfg::DBS + j] = (e % Cfg::SPW) * ps + (e / Cfg::SPW) * 4;
+        }
+    }
+    g.rel.swap(off);
+    g.smem_bytes = packed_smem<Cfg>(rawcap, ps);
+    g.kernel = kernel_id;
+    return true;
 }
 
 }  // namespace
 
-// Tile S[g][d][c] for the kernel.  Fails if any shift is negative.  uint8 samples use the
-// packed kernel (Db 32, T 512) unless g.kernel == 1 asks for the generic one or its staging
-// does not fit; everything else uses the generic kernel with Db 32/16/8.
+// Tile S[g][d][c] for the kernel.  Fails if any shift is negative.  uint8 and uint16 samples
+// use the packed kernels (Db 38 / 16, T 512) unless g.kernel == 1 asks for the generic one or
+// their staging does not fit; everything else uses the generic kernel with Db 32/16/8.
 mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
 {
     const int SZ = (int)dtype_size(g.in_dtype);
@@ -712,36 +811,17 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
         mx = std::max(mx, (int)S[(size_t)i]);
     }
     g.max_shift = mx;
-    if (g.in_dtype == MDSM_U8 && g.kernel != 1) {
-        g.Db = kPDB;
-        g.T = kPT;
-        g.R = kPR4 * 4;
-        g.DPW = kPDPW;
-        g.cc = kPCC;
-        g.nst = kPNR;
-        const int maxspan = tile_tables(g, S);
-        const int rawcap = (int)(((long long)kPT + maxspan + 32 + 15) / 16 * 16) + 16;
-        const int ps = rawcap - 16;  // nwp = ps/4 words; the expansion reads word nwp too
-        if (packed_smem(rawcap, ps) <= 220 * 1024) {
-            g.max_span = maxspan;
-            g.rowcap = rawcap;
-            g.ps = ps;
-            // byte offset of (c, d)'s first word inside the phase-expanded row
-            // stored kPDBS per channel (the padding stays 0)
-            std::vector<int32_t> off(g.sminspan.size() / 2 * kPDBS, 0);
-            for (size_t o = 0; o < g.sminspan.size() / 2; ++o) {
-                const int lo16 = g.sminspan[o * 2] & 15;
-                for (int j = 0; j < g.Db; ++j) {
-                    const int e = lo16 + g.rel[o * g.Db + j];
-                    off[o * kPDBS + j] = (e & 3) * ps + (e >> 2) * 4;
-                }
-            }
-            g.rel.swap(off);
-            g.smem_bytes = packed_smem(rawcap, ps);
-            g.kernel = 2;
+    // the packed kernels sum exactly in int32: only where every sum fits
+    if (g.kernel != 1) {
+        if (g.in_dtype == MDSM_U8 && (long long)g.nchans * 255 <= 0x7fffffffLL &&
+            packed_tables<CfgU8>(g, S, 2))
             return MDSM_OK;
-        }
+        if (g.in_dtype == MDSM_U16 && !g.out_u16 &&
+            (long long)g.nchans * 65535 <= 0x7fffffffLL &&
+            packed_tables<CfgU16>(g, S, 3))
+            return MDSM_OK;
     }
+    g.out_u16 = 0;  // only the uint8 packed kernel writes uint16 sums
     g.kernel = 1;
     g.R = kR;
     g.T = 32 * kR;
@@ -810,8 +890,13 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
         return fail(MDSM_EINVAL, "input row pitch must be a multiple of 16 bytes");
     if ((in_group_stride * SZ) % 16 != 0)
         return fail(MDSM_EINVAL, "input group pitch must be a multiple of 16 bytes");
-    void *fn = g.kernel == 2 ? reinterpret_cast<void *>(&k_shift_sum_u8x4)
-                             : select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
+    void *fn = select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
+    if (g.kernel == 2 && g.out_u16)
+        fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16>);
+    else if (g.kernel == 2)
+        fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8>);
+    else if (g.kernel == 3)
+        fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16>);
     MDSM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)g.smem_bytes));
     KArgs a;
@@ -833,7 +918,7 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     a.ps = g.ps;
     a.err = d_err;
     const long long ntiles = (nsamp + g.T - 1) / g.T;
-    if (g.kernel == 2) {
+    if (g.kernel == 2 || g.kernel == 3) {
         // persistent: at most one CTA per SM walks the (DM block, tile, group) items
         const long long nitems = (long long)g.nblk * ntiles * g.ngroups;
         if (nitems > 0x7fffffffLL) return fail(MDSM_EINVAL, "block too long for one launch");
@@ -843,7 +928,8 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
         int nt = (int)ntiles, ni = (int)nitems;
         void *args[] = {&a, &nt, &ni};
         const unsigned grid = (unsigned)std::min<long long>(sms, nitems);
-        MDSM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(kPThreads), args, g.smem_bytes, st));
+        const unsigned threads = g.kernel == 2 ? CfgU8::THREADS : CfgU16::THREADS;
+        MDSM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, g.smem_bytes, st));
     } else {
         if (ntiles > 65535 || g.ngroups > 65535)
             return fail(MDSM_EINVAL, "block too long for one launch");
@@ -871,7 +957,7 @@ mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams)
         }
     b.rawcap = rawcap;
     b.ps = ps;
-    b.smem = rawcap ? packed_smem(rawcap, ps) : 0;
+    b.smem = rawcap ? packed_smem<CfgU8>(rawcap, ps) : 0;
     if (b.smem > 220 * 1024) return fail(MDSM_EINVAL, "batch: common staging does not fit");
     // per packed beam: offsets re-expressed with the common phase stride
     b.d_rel.assign(beams.size(), nullptr);
@@ -978,7 +1064,7 @@ mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches
         MDSM_CUDA_TRY(cudaGetDevice(&dev));
         MDSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
         const int grid = std::min(sms, b.nitems);
-        k_shift_sum_u8x4_batch<<<grid, kPThreads, b.smem, st>>>(
+        k_shift_sum_u8x4_batch<<<grid, CfgU8::THREADS, b.smem, st>>>(
             reinterpret_cast<const KArgs *>(b.d_kargs), reinterpret_cast<const int4 *>(b.d_items),
             b.nitems, b.d_counter, b.rawcap, b.ps, b.d_err);
         MDSM_CUDA_TRY(cudaGetLastError());

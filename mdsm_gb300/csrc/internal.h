@@ -50,7 +50,8 @@ struct StageGeom {
     long long out_stride = 0, out_group_stride = 0;  // elements
     int in_dtype = MDSM_U8;
     int acc_int = 1;      // 1: int32 accumulation, 0: float
-    int out_i32 = 0;      // output element type
+    int out_i32 = 0;      // output element type: int32 (1) or float32 (0)
+    int out_u16 = 0;      // uint16 output (the uint8 packed kernel, sums that fit 16 bits)
     int Db = 32, T = 256, R = 8, DPW = 4;
     int cc = 16, nst = 3; // channels per pipeline stage, stages
     int rowcap = 0;       // elements per staged row
@@ -64,8 +65,9 @@ struct StageGeom {
     int32_t *d_rel = nullptr;
     int32_t *d_sminspan = nullptr;
     size_t smem_bytes = 0;
-    int ps = 0;           // packed kernel: bytes per phase copy of a staged row
-    int kernel = 0;       // requested (0 choose, 1 generic); after tiling: 1 generic, 2 packed u8
+    int ps = 0;           // packed kernels: bytes per phase copy of a staged row
+    int kernel = 0;       // requested (0 choose, 1 generic); after tiling: 1 generic, 2 packed
+                          // uint8, 3 packed uint16
 };
 
 // Build the blocked tables of a stage from a full shift table S[g][d][c] (row-major).  Picks

@@ -77,11 +77,16 @@ int32_t shift_of(float dms, double delay64, float lowdm, float dmstep, int idx, 
 
 namespace {
 
-int acc_is_int(int in_dtype, int acc)
+// 1: exact INT32 sums, 0: FP32, -1: INT32 asked for float samples, -2: INT32 asked for sums
+// that may not fit.  Automatic: INT32 where a sum of nchans samples always fits, else FP32.
+int acc_is_int(int in_dtype, int acc, int nchans)
 {
-    if (acc == MDSM_ACC_I32) return in_dtype == MDSM_F32 ? -1 : 1;
+    const long long maxabs = in_dtype == MDSM_U8 ? 255 : in_dtype == MDSM_U16 ? 65535
+                             : in_dtype == MDSM_I16 ? 32768 : 0;
+    const bool fits = maxabs > 0 && (long long)nchans * maxabs <= 0x7fffffffLL;
+    if (acc == MDSM_ACC_I32) return in_dtype == MDSM_F32 ? -1 : (fits ? 1 : -2);
     if (acc == MDSM_ACC_F32) return 0;
-    return in_dtype == MDSM_F32 ? 0 : 1;
+    return fits ? 1 : 0;
 }
 
 long long round_pitch(long long elems, int dtype)
@@ -153,7 +158,9 @@ mdsm_status plan_create_brute(const mdsm_brute_desc &d, Plan &p)
 {
     if (d.in_dtype < MDSM_U8 || d.in_dtype > MDSM_F32)
         return fail(MDSM_EINVAL, "brute plan: unknown input dtype");
-    const int ai = acc_is_int(d.in_dtype, d.acc);
+    const int ai = acc_is_int(d.in_dtype, d.acc, d.nchans);
+    if (ai == -2)
+        return fail(MDSM_ERANGE, "INT32 accumulation: sums of this many channels may overflow");
     if (ai < 0) return fail(MDSM_EINVAL, "INT32 accumulation needs integer samples");
     MDSM_TRY(brute_tables(d, p.dmshifts, p.S, p.dm_values));
     const int ndms = (int)p.dm_values.size();
@@ -165,7 +172,7 @@ mdsm_status plan_create_brute(const mdsm_brute_desc &d, Plan &p)
     p.tsamp = d.tsamp;
     p.in_dtype = d.in_dtype;
     p.out_dtype = d.out_dtype;
-    p.acc = d.acc;
+    p.acc = ai ? MDSM_ACC_I32 : MDSM_ACC_F32;  // the accumulation in effect
     p.ndms = ndms;
     StageGeom g;
     g.nchans = d.nchans;
@@ -261,7 +268,9 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         return fail(MDSM_EINVAL, "subband plan: nchans, nsamp, nsubs, passes, tsamp required");
     if (d.nchans % d.nsubs != 0)
         return fail(MDSM_EINVAL, "subband plan: nchans must be a multiple of nsubs");
-    const int ai = acc_is_int(d.in_dtype, d.acc);
+    const int ai = acc_is_int(d.in_dtype, d.acc, d.nchans);
+    if (ai == -2)
+        return fail(MDSM_ERANGE, "INT32 accumulation: sums of this many channels may overflow");
     if (ai < 0) return fail(MDSM_EINVAL, "INT32 accumulation needs integer samples");
     p.kind = 2;
     p.nchans = d.nchans;
@@ -271,7 +280,7 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
     p.tsamp = d.tsamp;
     p.in_dtype = d.in_dtype;
     p.out_dtype = d.out_dtype;
-    p.acc = d.acc;
+    p.acc = ai ? MDSM_ACC_I32 : MDSM_ACC_F32;  // the accumulation in effect
     p.dmshifts.resize(d.nchans);
     dmshifts_ref(d.nchans, d.fch1, d.foff, p.dmshifts.data());
     const int nsubs = d.nsubs, cps = d.nchans / d.nsubs;
@@ -303,8 +312,9 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         int m2 = 0, m1 = 0;
         for (int32_t v : S2) m2 = std::max(m2, (int)v);
         const long long n1 = (long long)nsb + m2;
-        const long long n1p = round_pitch(n1, zdtype);
-        // stage 1: groups = subbands, rows = sub-DMs
+        // stage 1: groups = subbands, rows = sub-DMs.  Sums of at most 257 uint8 channels fit
+        // uint16: the packed kernel then writes the subband series as uint16 and the second
+        // stage reads half the bytes with its packed uint16 kernel.
         StageGeom g1;
         g1.nchans = cps;
         g1.ndms = ncalls;
@@ -313,6 +323,7 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         g1.in_dtype = ds_dtype;
         g1.acc_int = ai;
         g1.out_i32 = ai;
+        g1.out_u16 = ai && ds_dtype == MDSM_U8 && (long long)cps * 255 <= 65535;
         g1.DPW = 4;
         std::vector<int32_t> S1g((size_t)nsubs * ncalls * cps);
         for (int b = 0; b < nsubs; ++b)
@@ -320,6 +331,8 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
                 for (int c = 0; c < cps; ++c)
                     S1g[((size_t)b * ncalls + j) * cps + c] = S1[(size_t)j * d.nchans + b * cps + c];
         MDSM_TRY(build_stage_tables(g1, S1g));
+        const int pz = g1.out_u16 ? MDSM_U16 : zdtype;  // the pass's subband series type
+        const long long n1p = round_pitch(n1, pz);
         m1 = g1.max_shift;
         g1.out_stride = (long long)nsubs * n1p;  // z[j][b][t]
         g1.out_group_stride = n1p;
@@ -329,10 +342,11 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         g2.ndms = calldms;
         g2.ngroups = ncalls;
         g2.nsamp = nsb;
-        g2.in_dtype = zdtype;
+        g2.in_dtype = pz;
         g2.acc_int = ai;
         g2.out_i32 = d.out_dtype == MDSM_OUT_I32;
         g2.DPW = calldms <= 8 ? 1 : (calldms <= 16 ? 2 : 4);  // DM block no wider than a call
+        if (calldms < 10) g2.kernel = 1;  // the packed uint16 kernel's blocks are 16 trials
         MDSM_TRY(build_stage_tables(g2, S2));
         g2.in_stride = n1p;
         g2.in_group_stride = (long long)nsubs * n1p;
@@ -340,7 +354,7 @@ mdsm_status plan_create_subband(const mdsm_subband_desc &d, Plan &p)
         MDSM_TRY(upload_stage(g1));
         MDSM_TRY(upload_stage(g2));
         // z is written for t < n1 and read with the stage-2 tile overrun past its last row
-        const size_t zwrite = (size_t)ncalls * nsubs * n1p * 4;
+        const size_t zwrite = (size_t)ncalls * nsubs * n1p * dtype_size(pz);
         const size_t zread = (size_t)stage_in_bytes(g2, n1p, (long long)nsubs * n1p);
         zmax = std::max(zmax, std::max(zwrite, zread) + 4096);
         // original samples read: (n1 + m1) downsampled samples of bsz each

@@ -156,6 +156,46 @@ def test_packed_u8_matches_generic_and_oracle(lib, orc, cuda, nchans, nsamp, ndm
         assert np.array_equal(_run(generic, xg, torch), want), fill
 
 
+@pytest.mark.parametrize("nchans,nsamp,ndms", [(1024, 2000, 40), (257, 511, 17), (9, 4, 1),
+                                               (600, 3333, 100), (32767, 600, 3)])
+def test_packed_u16_matches_generic_and_oracle(lib, orc, cuda, nchans, nsamp, ndms):
+    """The packed 16-bit kernel (default for uint16) against the generic kernel and the
+    oracle, including all-65535 input (lane sums up to 2^31 - 1 over 32767 channels)."""
+    import mdsm_gb300 as m
+    torch = cuda
+    segs = [(0.0, 0.5 if nchans < 10000 else 0.02, ndms)]
+    packed = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs, in_dtype="u16",
+                         out_dtype="i32")
+    generic = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs,
+                          in_dtype="u16", out_dtype="i32", kernel=1)
+    assert packed.info.kernel == 3 and generic.info.kernel == 1
+    for fill in ("random", "max"):
+        nch, stride = packed.input_shape()
+        if fill == "max":
+            x = np.full((nch, stride), 65535, np.uint16)
+        else:
+            x = np.random.default_rng(nchans).integers(0, 65536, (nch, stride), dtype=np.uint16)
+        got = _run(packed, x, torch)
+        want = orc.dedisperse(x, packed.shift_table(), nsamp)
+        assert np.array_equal(got, want), fill
+        xg = np.zeros(generic.input_shape(), np.uint16)
+        w = min(xg.shape[1], x.shape[1])
+        xg[:, :w] = x[:, :w]
+        assert np.array_equal(_run(generic, xg, torch), want), fill
+
+
+def test_int32_accumulation_refused_when_sums_may_overflow(lib):
+    import mdsm_gb300 as m
+    from mdsm_gb300 import MdsmError
+    with pytest.raises(MdsmError) as e:
+        m.BrutePlan(32769, 1500.0, -300.0 / 32769, 64e-6, 100, [(0.0, 0.01, 2)], in_dtype="u16",
+                    out_dtype="i32", acc="i32")
+    assert e.value.status == 6  # MDSM_ERANGE
+    auto = m.BrutePlan(32769, 1500.0, -300.0 / 32769, 64e-6, 100, [(0.0, 0.01, 2)],
+                       in_dtype="u16", out_dtype="f32")
+    assert auto.info.acc == 2  # automatic: FP32 (MDSM_ACC_F32) for sums that may not fit
+
+
 def test_packed_falls_back_for_wide_plans(lib, orc, cuda):
     """A DM block whose shift span does not fit the packed kernel's staging runs on the
     generic kernel, with the same exact result."""

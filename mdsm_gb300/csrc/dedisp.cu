@@ -248,6 +248,8 @@ struct PackedCfg {
 };
 using CfgU8 = PackedCfg<1, 19, 2>;
 using CfgU8to16 = PackedCfg<1, 19, 2, true>;  // the first subband stage: uint16 subband series
+using CfgU8w16 = PackedCfg<1, 16, 2>;         // 32-trial blocks, for trial counts of 32 k
+using CfgU8w16to16 = PackedCfg<1, 16, 2, true>;
 using CfgU16 = PackedCfg<2, 16, 1>;
 
 // Work items of the packed kernels are (beam, DM block, time tile, group) tiles; a CTA runs a
@@ -813,9 +815,14 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
     g.max_shift = mx;
     // the packed kernels sum exactly in int32: only where every sum fits
     if (g.kernel != 1) {
-        if (g.in_dtype == MDSM_U8 && (long long)g.nchans * 255 <= 0x7fffffffLL &&
-            packed_tables<CfgU8>(g, S, 2))
-            return MDSM_OK;
+        if (g.in_dtype == MDSM_U8 && (long long)g.nchans * 255 <= 0x7fffffffLL) {
+            // 38-trial blocks run ~5 % faster per trial than 32-trial ones; take 32 where the
+            // last 38-trial block would leave more than that idle (e.g. 64 or 128 trials)
+            const int n38 = (g.ndms + CfgU8::DB - 1) / CfgU8::DB * CfgU8::DB;
+            const int n32 = (g.ndms + CfgU8w16::DB - 1) / CfgU8w16::DB * CfgU8w16::DB;
+            if (n38 <= 1.05 * n32 && packed_tables<CfgU8>(g, S, 2)) return MDSM_OK;
+            if (packed_tables<CfgU8w16>(g, S, 2)) return MDSM_OK;
+        }
         if (g.in_dtype == MDSM_U16 && !g.out_u16 &&
             (long long)g.nchans * 65535 <= 0x7fffffffLL &&
             packed_tables<CfgU16>(g, S, 3))
@@ -891,12 +898,19 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     if ((in_group_stride * SZ) % 16 != 0)
         return fail(MDSM_EINVAL, "input group pitch must be a multiple of 16 bytes");
     void *fn = select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
-    if (g.kernel == 2 && g.out_u16)
-        fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16>);
-    else if (g.kernel == 2)
-        fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8>);
-    else if (g.kernel == 3)
+    unsigned threads = kNW * 32;
+    if (g.kernel == 2 && g.Db == CfgU8::DB) {
+        fn = g.out_u16 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16>)
+                       : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8>);
+        threads = CfgU8::THREADS;
+    } else if (g.kernel == 2) {
+        fn = g.out_u16 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8w16to16>)
+                       : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8w16>);
+        threads = CfgU8w16::THREADS;
+    } else if (g.kernel == 3) {
         fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16>);
+        threads = CfgU16::THREADS;
+    }
     MDSM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)g.smem_bytes));
     KArgs a;
@@ -928,14 +942,13 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
         int nt = (int)ntiles, ni = (int)nitems;
         void *args[] = {&a, &nt, &ni};
         const unsigned grid = (unsigned)std::min<long long>(sms, nitems);
-        const unsigned threads = g.kernel == 2 ? CfgU8::THREADS : CfgU16::THREADS;
         MDSM_CUDA_TRY(cudaLaunchKernel(fn, dim3(grid), dim3(threads), args, g.smem_bytes, st));
     } else {
         if (ntiles > 65535 || g.ngroups > 65535)
             return fail(MDSM_EINVAL, "block too long for one launch");
         dim3 grid((unsigned)g.nblk, (unsigned)ntiles, (unsigned)g.ngroups);
         void *args[] = {&a};
-        MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(kNW * 32), args, g.smem_bytes, st));
+        MDSM_CUDA_TRY(cudaLaunchKernel(fn, grid, dim3(threads), args, g.smem_bytes, st));
     }
     if (launches) *launches += 1;
     return MDSM_OK;
@@ -945,13 +958,21 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
 // batched persistent launch over several brute-force plans
 // ------------------------------------------------------------------------------------------
 
+namespace {
+// beams the persistent batch kernel (38-trial uint8 blocks) runs; others launch alone
+bool in_batch_kernel(const StageGeom &g)
+{
+    return g.kernel == 2 && g.Db == CfgU8::DB && !g.out_u16;
+}
+}  // namespace
+
 mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams)
 {
     batch_release(b);
     b.beams = beams;
     int rawcap = 0, ps = 0;
     for (const BatchBeam &bb : beams)
-        if (bb.g->kernel == 2) {
+        if (in_batch_kernel(*bb.g)) {
             rawcap = std::max(rawcap, bb.g->rowcap);
             ps = std::max(ps, bb.g->ps);
         }
@@ -963,7 +984,7 @@ mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams)
     b.d_rel.assign(beams.size(), nullptr);
     for (size_t i = 0; i < beams.size(); ++i) {
         const StageGeom &g = *beams[i].g;
-        if (g.kernel != 2) continue;
+        if (!in_batch_kernel(g)) continue;
         std::vector<int32_t> rel(g.rel.size());
         for (size_t j = 0; j < rel.size(); ++j) {
             const int a = g.rel[j] / g.ps, q4 = g.rel[j] % g.ps;
@@ -1012,21 +1033,21 @@ mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in
         a.out = static_cast<unsigned char *>(out[i]);
         a.out_stride = out_stride[i];
         a.out_group_stride = 0;
-        a.rel = g.kernel == 2 ? static_cast<const int32_t *>(b.d_rel[i]) : g.d_rel;
+        a.rel = in_batch_kernel(g) ? static_cast<const int32_t *>(b.d_rel[i]) : g.d_rel;
         a.sminspan = g.d_sminspan;
         a.nchans = g.nchans;
         a.ndms = g.ndms;
         a.nsamp = g.nsamp;
         a.nblk = g.nblk;
-        a.rowcap = g.kernel == 2 ? b.rawcap : g.rowcap;
+        a.rowcap = in_batch_kernel(g) ? b.rawcap : g.rowcap;
         a.nst = g.nst;
         a.out_i32 = g.out_i32;
-        a.ps = g.kernel == 2 ? b.ps : g.ps;
+        a.ps = in_batch_kernel(g) ? b.ps : g.ps;
             a.err = d_err;
     }
     for (int i : order) {
         const StageGeom &g = *b.beams[i].g;
-        if (g.kernel != 2) continue;
+        if (!in_batch_kernel(g)) continue;
         const int ntiles = (g.nsamp + g.T - 1) / g.T;
         if (tile_major) {
             for (int t = 0; t < ntiles; ++t)
@@ -1071,7 +1092,7 @@ mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches
         if (launches) *launches += 1;
     }
     for (const BatchBeam &bb : b.beams) {
-        if (mode == 0 && bb.g->kernel == 2) continue;
+        if (mode == 0 && in_batch_kernel(*bb.g)) continue;
         MDSM_TRY(launch_stage(*bb.g, bb.in, bb.in_stride, 0, bb.out, bb.out_stride, 0, b.d_err, st,
                               launches));
     }

@@ -612,7 +612,8 @@ def main():
                      "peak": add_peak / 1e12, "unit": "Tadd/s",
                      "frac": achieved_ops / add_peak, "traffic": traffic,
                      "peak_source": "%d SMs x 128 lanes x sm_max_mhz (%s)" % (sm_count, pk_kind),
-                     "kernel": "k_shift_sum_u8x4" if info.kernel == 2 else "k_shift_sum",
+                     "kernel": {2: "k_shift_sum_packed<uint8>", 3: "k_shift_sum_packed<uint16>"}
+                     .get(info.kernel, "k_shift_sum"),
                      "per_launch_ms": per_launch_ms,
                      "algorithmic_adds_per_launch": ops},
         "roofline_hbm": {"bound": "hbm", "achieved": hbm_achieved, "peak": pk.get("hbm_gbs"),

@@ -393,27 +393,63 @@ constexpr int kBoxTile = 2048;   // output samples per CTA
 constexpr int kBoxHaloL = 128;   // NMS radius for the widest boxcar (256/2)
 constexpr int kBoxThreads = 256;
 
-// One CTA per (DM, tile).  Region [t0 - HL, t0 + TILE + HL + wmax - 1) is staged in float.
-// Arithmetic per sample and width is FP32 (explicitly rounded, same order as the oracle); only
-// the per-DM statistics are FP64.  Each thread owns the positions tid + q * kBoxThreads: it
-// keeps their boxcar sums and their best SNR / width in registers across the widths, and
-// reads only the partner sum B[i + w/2] from shared memory, so one width costs one shared
-// load, one shared store and one barrier per position (the sums alternate between two
-// buffers).
+// Two FP32 lanes at once (Blackwell add/mul.f32x2, each lane rounded to nearest as the scalar
+// operation would be).
+__device__ __forceinline__ unsigned long long f2_bits(float2 v)
+{
+    return (unsigned long long)__float_as_uint(v.x) |
+           ((unsigned long long)__float_as_uint(v.y) << 32);
+}
+__device__ __forceinline__ float2 bits_f2(unsigned long long v)
+{
+    return make_float2(__uint_as_float((unsigned)v), __uint_as_float((unsigned)(v >> 32)));
+}
+__device__ __forceinline__ float2 add_f2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(d);
+}
+__device__ __forceinline__ float2 mul_f2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(d);
+}
+
+// Staged samples of k_boxcar for NW widths: the region [t0 - HL, t0 + TILE + HL + wmax - 1),
+// rounded up to whole pairs of positions per thread; each sum buffer has wmax floats more so
+// that partner reads past the region stay inside it (those positions feed no kept boxcar).
+template <int NW>
+struct BoxGeom {
+    static constexpr int WMAX = 1 << (NW - 1);
+    static constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
+    static constexpr int SPAN = kBoxTile + 2 * HL + WMAX;  // samples a kept boxcar can touch
+    static constexpr int NBEST = kBoxTile + 2 * HL;        // positions with a best value
+    static constexpr int PAIRS = (SPAN + 2 * kBoxThreads - 1) / (2 * kBoxThreads);  // per thread
+    // floats; even, so the second buffer and the pairs in it stay 8-byte aligned
+    static constexpr int BUF = PAIRS * 2 * kBoxThreads + (WMAX < 2 ? 2 : WMAX);
+    static_assert(BUF % 2 == 0 && NBEST % 2 == 0, "pairs of positions");
+};
+
+// One CTA per (DM, tile).  Arithmetic per sample and width is FP32 (explicitly rounded, same
+// order as the oracle); only the per-DM statistics are FP64.  Each thread owns the position
+// pairs (2 tid + 2 kBoxThreads q, +1): it keeps their boxcar sums and best SNR / width in
+// registers across the widths and reads only the partner sums B[i + w/2] from shared memory
+// (one 8-byte load per pair), so one width costs per pair one shared load, one shared store,
+// four paired FP32 operations, the best-value updates and one barrier (the sums alternate
+// between two buffers).
 template <typename T, int NW>
 __global__ void __launch_bounds__(kBoxThreads)
     k_boxcar(const T *__restrict__ y, long long n, double threshold,
              const double2 *__restrict__ musig, DevCand *__restrict__ cands,
              unsigned long long *__restrict__ count, long long cap)
 {
+    using G = BoxGeom<NW>;
+    constexpr int HL = G::HL, SPAN = G::SPAN, NBEST = G::NBEST, PAIRS = G::PAIRS;
     extern __shared__ __align__(16) unsigned char sm[];
-    constexpr int WMAX = 1 << (NW - 1);
-    constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
-    constexpr int SPAN = kBoxTile + 2 * HL + WMAX;  // staged samples
-    constexpr int NBEST = kBoxTile + 2 * HL;        // positions with a best value
-    constexpr int PER = (SPAN + kBoxThreads - 1) / kBoxThreads;
-    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + SPAN;
-    float *best_s = B1 + SPAN;
+    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
+    float *best_s = B1 + G::BUF;
     int *bw_s = reinterpret_cast<int *>(best_s + NBEST);
 
     const int d = blockIdx.y;
@@ -424,19 +460,29 @@ __global__ void __launch_bounds__(kBoxThreads)
     const long long t0 = (long long)blockIdx.x * kBoxTile;
     const long long r0 = t0 - HL;  // series index of B[0] and best[0]
     // every staged sample and every boxcar of the tile inside the series: no per-element tests
-    const bool interior = r0 >= 0 && r0 + SPAN <= n;
+    const bool interior = r0 >= 0 && r0 + PAIRS * 2 * kBoxThreads <= n;
     const T *r = y + (size_t)d * n;
-    const int tid = threadIdx.x;
-    float b[PER], best[PER];
-    int bw[PER];
+    static_assert((kBoxThreads & (kBoxThreads - 1)) == 0, "power-of-two block");
+    // (the mask tells the compiler tid < kBoxThreads, so range tests fold at compile time for
+    // all but the last pair)
+    const int tid = threadIdx.x & (kBoxThreads - 1);
+    float2 b[PAIRS], best[PAIRS];
+    int2 bw[PAIRS];
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int i = tid + q * kBoxThreads;
+    for (int q = 0; q < PAIRS; ++q) {
+        const int i = 2 * tid + 2 * kBoxThreads * q;
         const long long t = r0 + i;
-        b[q] = (i < SPAN && (interior || (t >= 0 && t < n))) ? (float)__ldg(r + t) : 0.0f;
-        if (i < SPAN) B0[i] = b[q];
-        best[q] = -INFINITY;
-        bw[q] = 0;
+        float2 v;
+        if (interior) {
+            v = make_float2((float)__ldg(r + t), (float)__ldg(r + t + 1));
+        } else {
+            v.x = (t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
+            v.y = (t + 1 >= 0 && t + 1 < n) ? (float)__ldg(r + t + 1) : 0.0f;
+        }
+        b[q] = v;
+        *reinterpret_cast<float2 *>(B0 + i) = v;
+        best[q] = make_float2(-INFINITY, -INFINITY);
+        bw[q] = make_int2(0, 0);
     }
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
     __shared__ float inv_w[NW];
@@ -452,43 +498,49 @@ __global__ void __launch_bounds__(kBoxThreads)
             const float *cur = (l & 1) ? B0 : B1;
             float *nxt = (l & 1) ? B1 : B0;
 #pragma unroll
-            for (int q = 0; q < PER; ++q) {
-                const int i = tid + q * kBoxThreads;
-                if (i < SPAN) {
-                    b[q] = (i + h < SPAN) ? __fadd_rn(b[q], cur[i + h]) : 0.0f;
-                    nxt[i] = b[q];
-                }
+            for (int q = 0; q < PAIRS; ++q) {
+                const int i = 2 * tid + 2 * kBoxThreads * q;
+                // partner sums of positions i and i + 1
+                const float2 pv = h == 1 ? make_float2(b[q].y, cur[i + 2])
+                                         : *reinterpret_cast<const float2 *>(cur + i + h);
+                b[q] = add_f2(b[q], pv);
+                *reinterpret_cast<float2 *>(nxt + i) = b[q];
             }
             __syncthreads();
         }
         const float wm = __fmul_rn((float)w, mu_f);
         const float inv = inv_w[l];
 #pragma unroll
-        for (int q = 0; q < PER; ++q) {
-            const int i = tid + q * kBoxThreads;
+        for (int q = 0; q < PAIRS; ++q) {
+            const int i = 2 * tid + 2 * kBoxThreads * q;
+            if (i >= NBEST) continue;  // i even and NBEST even: i + 1 < NBEST too
             const long long t = r0 + i;
-            if (i < NBEST && (interior || (t >= 0 && t + w <= n))) {
-                const float sv = __fmul_rn(__fsub_rn(b[q], wm), inv);
-                if (sv > best[q]) {
-                    best[q] = sv;
-                    bw[q] = w;
-                }
+            const float2 sv = mul_f2(add_f2(b[q], make_float2(-wm, -wm)), make_float2(inv, inv));
+            const bool ok0 = interior || (t >= 0 && t + w <= n);
+            const bool ok1 = interior || (t + 1 >= 0 && t + 1 + w <= n);
+            if (ok0 && sv.x > best[q].x) {
+                best[q].x = sv.x;
+                bw[q].x = w;
+            }
+            if (ok1 && sv.y > best[q].y) {
+                best[q].y = sv.y;
+                bw[q].y = w;
             }
         }
     }
     bool any = false;
 #pragma unroll
-    for (int q = 0; q < PER; ++q) {
-        const int i = tid + q * kBoxThreads;
+    for (int q = 0; q < PAIRS; ++q) {
+        const int i = 2 * tid + 2 * kBoxThreads * q;
         if (i < NBEST) {
-            best_s[i] = best[q];
-            bw_s[i] = bw[q];
-            any |= best[q] >= thr;
+            *reinterpret_cast<float2 *>(best_s + i) = best[q];
+            *reinterpret_cast<int2 *>(bw_s + i) = bw[q];
+            any |= best[q].x >= thr || best[q].y >= thr;
         }
     }
     // most tiles hold no sample over the threshold: skip the neighbourhood test there
     if (!__syncthreads_or(any)) return;
-    for (int q = tid; q < kBoxTile; q += blockDim.x) {
+    for (int q = tid; q < kBoxTile; q += kBoxThreads) {
         const long long t = t0 + q;
         if (t >= n) break;
         const int i = q + HL;
@@ -504,6 +556,7 @@ __global__ void __launch_bounds__(kBoxThreads)
         const unsigned long long at = atomicAdd(count, 1ull);
         if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw_s[i], bv};
     }
+    (void)SPAN;
 }
 
 // The boxcar search of every DM row, for 1..9 widths (a template per width count).
@@ -512,13 +565,11 @@ static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, doub
                                  const double2 *musig, DevCand *cands,
                                  unsigned long long *count, long long cap, cudaStream_t st);
 
-// Shared memory of k_boxcar: two sum buffers of span floats, best (float) and width (int) of
-// nbest positions.
-static size_t boxcar_smem(int nwidths)
+// Shared memory of k_boxcar: two sum buffers, best (float) and width (int) of NBEST positions.
+template <int NW>
+static size_t boxcar_smem()
 {
-    const int wmax = 1 << (nwidths - 1);
-    const int hl = std::max(wmax / 2, 1);
-    return (size_t)(kBoxTile + 2 * hl + wmax) * 8 + (size_t)(kBoxTile + 2 * hl) * 8;
+    return (size_t)BoxGeom<NW>::BUF * 8 + (size_t)BoxGeom<NW>::NBEST * 8;
 }
 
 template <typename T, int NW>
@@ -526,7 +577,7 @@ static cudaError_t launch_boxcar_nw(const T *y, int ndms, long long n, double th
                                     const double2 *musig, DevCand *cands,
                                     unsigned long long *count, long long cap, cudaStream_t st)
 {
-    const size_t smem = boxcar_smem(NW);
+    const size_t smem = boxcar_smem<NW>();
     cudaError_t e = cudaFuncSetAttribute(k_boxcar<T, NW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;

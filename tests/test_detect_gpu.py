@@ -49,23 +49,27 @@ def test_ref_detector_on_dedispersed_block(lib, orc, cuda):
     assert np.array_equal(cands["snr"], snr)
 
 
-@pytest.mark.parametrize("dtype", ["i32", "f32"])
-def test_boxcar_matches_oracle(lib, orc, cuda, dtype):
+@pytest.mark.parametrize("dtype,nw,n", [("i32", 9, 9000), ("f32", 9, 9000), ("i32", 1, 4097),
+                                        ("f32", 2, 2049), ("i32", 5, 301), ("i32", 9, 12289)])
+def test_boxcar_matches_oracle(lib, orc, cuda, dtype, nw, n):
+    """Interior tiles (no bounds tests) and edge tiles, 1 to 9 widths, odd lengths."""
     import mdsm_gb300 as m
     torch = cuda
-    rng = np.random.default_rng(12)
-    ndms, n = 24, 9000
+    rng = np.random.default_rng(12 + nw + n)
+    ndms = 24
     if dtype == "i32":
         y = rng.integers(-3000, 3000, (ndms, n)).astype(np.int32)
-        y[3, 1000:1064] += 900
-        y[10, 5000:5002] += 20000
-        y[20, 8990:9000] += 9000
+        y[3, min(1000, n - 70):min(1064, n - 6)] += 900
+        y[10, n // 2:n // 2 + 2] += 20000
+        y[20, n - 10:n] += 9000
+        y[21, 0:3] += 15000
     else:
         y = rng.standard_normal((ndms, n)).astype(np.float32)
-        y[3, 1000:1064] += np.float32(0.9)
-        y[10, 5000:5002] += np.float32(8.0)
-    cands, cnt = m.boxcar_detect_device(torch.from_numpy(y).cuda(), nwidths=9, threshold=6.0)
-    dm, samp, wid, snr = orc.boxcar_detect(y, 9, 6.0)
+        y[3, min(1000, n - 70):min(1064, n - 6)] += np.float32(0.9)
+        y[10, n // 2:n // 2 + 2] += np.float32(8.0)
+        y[21, 0:3] += np.float32(6.0)
+    cands, cnt = m.boxcar_detect_device(torch.from_numpy(y).cuda(), nwidths=nw, threshold=6.0)
+    dm, samp, wid, snr = orc.boxcar_detect(y, nw, 6.0)
     assert cnt == len(dm) > 0
     assert np.array_equal(cands["dm_idx"], dm)
     assert np.array_equal(cands["sample"], samp)

@@ -73,7 +73,7 @@ using namespace mdsm;
 namespace {
 
 constexpr long long kHostSegMin = 16384;  // output samples per segment, at least
-constexpr int kHostSegMax = 8;            // segments per block, at most
+constexpr int kHostSegMax = 16;           // segments per block, at most
 
 // Brute force from host buffers with the block cut into time segments: segment s's new input
 // columns are copied in on one stream, its output columns are computed on the caller's stream

@@ -390,7 +390,6 @@ __global__ void __launch_bounds__(256)
 }
 
 constexpr int kBoxTile = 2048;   // output samples per CTA
-constexpr int kBoxHaloL = 128;   // NMS radius for the widest boxcar (256/2)
 constexpr int kBoxThreads = 256;
 
 // Two FP32 lanes at once (Blackwell add/mul.f32x2, each lane rounded to nearest as the scalar
@@ -446,7 +445,7 @@ __global__ void __launch_bounds__(kBoxThreads)
              unsigned long long *__restrict__ count, long long cap)
 {
     using G = BoxGeom<NW>;
-    constexpr int HL = G::HL, SPAN = G::SPAN, NBEST = G::NBEST, PAIRS = G::PAIRS;
+    constexpr int HL = G::HL, NBEST = G::NBEST, PAIRS = G::PAIRS;
     extern __shared__ __align__(16) unsigned char sm[];
     float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
     float *best_s = B1 + G::BUF;
@@ -556,7 +555,6 @@ __global__ void __launch_bounds__(kBoxThreads)
         const unsigned long long at = atomicAdd(count, 1ull);
         if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw_s[i], bv};
     }
-    (void)SPAN;
 }
 
 // The boxcar search of every DM row, for 1..9 widths (a template per width count).

@@ -413,7 +413,9 @@ def run_batch(args):
 
 def run_precision(args):
     """Precision report: INT32 and FP32 accumulation against the FP64 oracle, per sample type
-    (uint8 mean 128 sigma 16, int16 sigma 1000, float32 N(0,1)), 4096 channels, 64 DM trials."""
+    (uint8 mean 128 sigma 16, int16 sigma 1000, float32 N(0,1)), 4096 channels, 64 DM trials;
+    and uint16 over 40000 channels, where INT32 sums could overflow and the automatic mode
+    takes FP32."""
     import torch
 
     import mdsm_gb300 as m
@@ -451,6 +453,26 @@ def run_precision(args):
                         "max_rel_value": float((err / np.maximum(np.abs(y64), 1.0)).max()),
                         "exact": bool(err.max() == 0.0)}
         out[dtype] = res
+    # uint16 samples over 40000 channels: sums reach 2.6e9 > 2^31, so the automatic mode
+    # accumulates in FP32 (exact INT32 sums per 16 channels, Kahan-compensated across them)
+    nch16, ns16, segs16 = 40000, 1024, [(0.0, 0.01, 8)]
+    plan = m.BrutePlan(nch16, FCH1, -BW / nch16, TSAMP, ns16, segs16, in_dtype="u16",
+                       out_dtype="f32")
+    nch, stride = plan.input_shape()
+    x = np.random.default_rng(3).integers(0, 65536, (nch, stride), dtype=np.uint16)
+    d_in = plan.alloc_input()
+    d_in[: x.size].copy_(torch.from_numpy(x.ravel()))
+    d_out = plan.alloc_output()
+    plan.dedisperse_device(d_in, d_out)
+    torch.cuda.synchronize()
+    y = d_out.cpu().numpy().astype(np.float64)
+    xf = x.astype(np.float32)
+    y64 = orc.dedisperse(xf, plan.shift_table(), ns16, out="f64")
+    err = np.abs(y - y64)
+    out["u16_40000ch_auto"] = {"acc": "f32" if plan.info.acc == 2 else "i32",
+                               "max_abs": float(err.max()),
+                               "max_rel_value": float((err / np.maximum(np.abs(y64), 1.0)).max()),
+                               "max_sum": float(y64.max())}
     print(json.dumps({"precision": out, "config": {"nchans": nchans, "nsamp": nsamp,
                                                    "ndms": 64}}), flush=True)
 

@@ -159,7 +159,10 @@ mdsm_status mdsm_dedisperse_device(mdsm_plan *plan, const void *d_in, long long 
                                    void *stream);
 /* The same through host buffers: h_in channel-major with pitch h_in_stride elements (the
  * reference's nsamp + maxshift), h_out [ndms][nsamp].  Copies H2D, runs, copies D2H and
- * synchronises the stream (src/mdsm/dedispersion_thread.cu:284-298,352-355). */
+ * synchronises the stream (src/mdsm/dedispersion_thread.cu:284-298,352-355).  Brute-force
+ * blocks of at least 32768 samples run in up to 16 time segments whose copy-in, kernel and
+ * copy-out overlap (two library-owned copy streams ordered by events); pinned host buffers
+ * let the copies run at full speed.  Results do not depend on the segmentation. */
 mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_in_stride,
                                  void *h_out, void *stream);
 /* Number of kernels the last dedisperse call on this plan launched. */

@@ -439,7 +439,7 @@ struct BoxGeom {
 // four paired FP32 operations, the best-value updates and one barrier (the sums alternate
 // between two buffers).
 template <typename T, int NW>
-__global__ void __launch_bounds__(kBoxThreads)
+__global__ void __launch_bounds__(kBoxThreads, 5)
     k_boxcar(const T *__restrict__ y, long long n, double threshold,
              const double2 *__restrict__ musig, DevCand *__restrict__ cands,
              unsigned long long *__restrict__ count, long long cap)

@@ -210,6 +210,32 @@ mdsm_status mdsm_ref_detect_device_noalloc(const float *d_series, int ndms, int 
                                            long long *ncand, float *mean, float *rms,
                                            void *stream);
 
+/* process_brute with caller noise statistics (dedispersion_output.cpp:135-213, mean != NULL):
+ * h_mean/h_rms hold one value per spc samples (nchunks >= (nsamp - 5) / spc + 1 values); the
+ * test is median - h_mean[t / spc] >= h_rms[t / spc] * threshold with DM > 1 and the
+ * candidate's snr is (median - mean) / rms (the reference's file line adds that chunk's mean
+ * and rms).  Candidates sorted by (dm_idx, sample), width 1. */
+mdsm_status mdsm_ref_detect_chunked_device(const float *d_series, int ndms, int nsamp,
+                                           float lowdm, float dmstep, float threshold,
+                                           const float *h_mean, const float *h_rms,
+                                           long long nchunks, int spc, mdsm_candidate *h_cands,
+                                           long long cap, long long *ncand, void *stream);
+/* process_subband (dedispersion_output.cpp:56-132) on a subband plan's float output (rows of
+ * out_stride elements; a pass with downsample b holds nsamp / b samples per row): with
+ * h_mean == NULL, per-row mean and rms from sequential double sums (:87-97), else the caller's
+ * chunk statistics as above; the test median - mean >= rms * threshold with the row's DM > 1,
+ * snr = median / rms.  Candidates carry the global row, the sample within the pass and, in
+ * width, the pass's downsample factor (the sample's time is t0 + sample * tsamp * width).
+ * Deviations, each a defect of the reference: every pass reads its own rows (the reference
+ * reads the first pass's rows for every pass), the row's DM is the plan's (the reference
+ * prints lowdm + k * dmstep, without the second stage's centring), and the per-row branch
+ * runs (the reference dereferences mean[0] first). */
+mdsm_status mdsm_ref_detect_subband_device(const mdsm_plan *plan, const float *d_series,
+                                           long long out_stride, float threshold,
+                                           const float *h_mean, const float *h_rms,
+                                           long long nchunks, int spc, mdsm_candidate *h_cands,
+                                           long long cap, long long *ncand, void *stream);
+
 /* Boxcar single-pulse search (src/prototypes/singlepulse.cpp:41-146, restated): widths
  * 1,2,4..2^(nwidths-1); per-DM mean/sigma in FP64; boxcar sums and SNR = (sum - w*mean) /
  * (sigma*sqrt(w)) in FP32, explicitly rounded in a fixed order; per-sample

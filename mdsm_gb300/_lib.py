@@ -135,6 +135,12 @@ SIGNATURES = {
     "mdsm_ref_detect_device_noalloc": (_st, [_vp, _i, _i, _f, _f, _f, ctypes.POINTER(Candidate),
                                              _ll, ctypes.POINTER(_ll), ctypes.POINTER(_f),
                                              ctypes.POINTER(_f), _vp]),
+    "mdsm_ref_detect_chunked_device": (_st, [_vp, _i, _i, _f, _f, _f, _vp, _vp, _ll, _i,
+                                             ctypes.POINTER(Candidate), _ll, ctypes.POINTER(_ll),
+                                             _vp]),
+    "mdsm_ref_detect_subband_device": (_st, [_vp, _vp, _ll, _f, _vp, _vp, _ll, _i,
+                                             ctypes.POINTER(Candidate), _ll, ctypes.POINTER(_ll),
+                                             _vp]),
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
     "mdsm_downsample_device": (_st, [_vp, _i, _i, _ll, _ll, _i, _i, _vp, _i, _ll, _vp]),

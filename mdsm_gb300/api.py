@@ -202,6 +202,45 @@ def ref_detect_device(series, lowdm, dmstep, threshold, cap=1 << 20, stream=None
     return _cands_to_array(buf, min(n.value, cap)), mean.value, rms.value, n.value
 
 
+def ref_detect_chunked_device(series, lowdm, dmstep, threshold, mean, rms, spc, cap=1 << 20,
+                              stream=None):
+    """Reference detector with caller noise statistics (one mean/rms per spc samples) on a
+    device float series [ndms][nsamp]: (cands, total)."""
+    ndms, nsamp = series.shape
+    mean = np.ascontiguousarray(mean, np.float32)
+    rms = np.ascontiguousarray(rms, np.float32)
+    buf = (Candidate * cap)()
+    n = ctypes.c_longlong()
+    check(load().mdsm_ref_detect_chunked_device(
+        ctypes.c_void_p(series.data_ptr()), ndms, nsamp, float(lowdm), float(dmstep),
+        float(threshold), mean.ctypes.data_as(ctypes.c_void_p),
+        rms.ctypes.data_as(ctypes.c_void_p), mean.size, int(spc), buf, cap, ctypes.byref(n),
+        _stream_ptr(stream)))
+    return _cands_to_array(buf, min(n.value, cap)), n.value
+
+
+def ref_detect_subband_device(plan, series, threshold, mean=None, rms=None, spc=0,
+                              cap=1 << 20, stream=None):
+    """process_subband on a subband plan's device float output [ndms][>= nsamp]: per-row
+    statistics, or the caller's chunk statistics.  (cands, total); width holds the pass's
+    downsample factor."""
+    out_stride = series.stride(0) if series.dim() == 2 else plan.info.nsamp
+    mp = rp = None
+    nch = 0
+    if mean is not None:
+        mean = np.ascontiguousarray(mean, np.float32)
+        rms = np.ascontiguousarray(rms, np.float32)
+        mp = mean.ctypes.data_as(ctypes.c_void_p)
+        rp = rms.ctypes.data_as(ctypes.c_void_p)
+        nch = mean.size
+    buf = (Candidate * cap)()
+    n = ctypes.c_longlong()
+    check(load().mdsm_ref_detect_subband_device(
+        plan._h, ctypes.c_void_p(series.data_ptr()), out_stride, float(threshold), mp, rp, nch,
+        int(spc), buf, cap, ctypes.byref(n), _stream_ptr(stream)))
+    return _cands_to_array(buf, min(n.value, cap)), n.value
+
+
 def boxcar_detect_device(series, nwidths=9, threshold=6.0, cap=1 << 20, stream=None):
     """Boxcar search on a device series [ndms][nsamp] (float32 or int32)."""
     import torch

@@ -30,11 +30,22 @@ def _pitch(s):
     return s.nsamp + s.maxshift
 
 
+_KEEP = []  # caller noise statistics stay alive until the block that uses them is processed
+
+
 def next_chunk(data_read, timestamp=0.0, blockRate=0.0, mean=None, rms=None):
-    """Returns (output [ndms][nsamp] view or None, samples)."""
+    """Returns (output [ndms][nsamp] view or None, samples).  mean/rms: the block's noise
+    statistics, one value per samplesPerChunk samples (float32 arrays), or None."""
     samples = ctypes.c_uint()
+    mp = rp = None
+    if mean is not None and rms is not None:
+        mean = np.ascontiguousarray(mean, np.float32)
+        rms = np.ascontiguousarray(rms, np.float32)
+        _KEEP[:] = [mean, rms]
+        mp = mean.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+        rp = rms.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
     p = load().mdsm_next_chunk(int(data_read), ctypes.byref(samples), float(timestamp),
-                               float(blockRate), None, None)
+                               float(blockRate), mp, rp)
     if not p:
         return None, samples.value
     return p, samples.value

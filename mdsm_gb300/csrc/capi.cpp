@@ -341,6 +341,34 @@ mdsm_status mdsm_ref_detect_device_noalloc(const float *d_series, int ndms, int 
                               ncand, mean, rms, static_cast<cudaStream_t>(stream));
 }
 
+mdsm_status mdsm_ref_detect_chunked_device(const float *d_series, int ndms, int nsamp,
+                                           float lowdm, float dmstep, float threshold,
+                                           const float *h_mean, const float *h_rms,
+                                           long long nchunks, int spc, mdsm_candidate *h_cands,
+                                           long long cap, long long *ncand, void *stream)
+{
+    if (!d_series || ndms <= 0 || nsamp < 5 || !ncand || !h_mean || !h_rms)
+        return fail(MDSM_EINVAL, "chunked detector: bad arguments");
+    return ref_detect_chunked(d_series, ndms, nsamp, lowdm, dmstep, threshold, h_mean, h_rms,
+                              nchunks, spc, h_cands, cap, ncand,
+                              static_cast<cudaStream_t>(stream));
+}
+
+mdsm_status mdsm_ref_detect_subband_device(const mdsm_plan *plan, const float *d_series,
+                                           long long out_stride, float threshold,
+                                           const float *h_mean, const float *h_rms,
+                                           long long nchunks, int spc, mdsm_candidate *h_cands,
+                                           long long cap, long long *ncand, void *stream)
+{
+    if (!plan || !d_series || !ncand) return fail(MDSM_EINVAL, "subband detector: bad arguments");
+    if (plan->p.out_dtype != MDSM_OUT_F32)
+        return fail(MDSM_EINVAL, "subband detector: the reference's detector reads float series");
+    if (out_stride < plan->p.nsamp)
+        return fail(MDSM_ERANGE, "subband detector: row pitch smaller than nsamp");
+    return ref_detect_subband(plan->p, d_series, out_stride, threshold, h_mean, h_rms, nchunks,
+                              spc, h_cands, cap, ncand, static_cast<cudaStream_t>(stream));
+}
+
 mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, int ndms,
                                       int nsamp, int nwidths, double threshold,
                                       mdsm_candidate *h_cands, long long cap, long long *ncand,

@@ -175,6 +175,7 @@ struct Instance {
     long long returned = 0;           // blocks count when next_chunk last returned output
     bool stopping = false, stopped_once = false;
     double ts = 0, rate = 0;
+    const float *cmean = nullptr, *crms = nullptr;  // caller noise statistics of the block
     std::vector<mdsm_candidate> cands;  // candidates of the last processed block
     FILE *fp = nullptr;
     long long written = 0;
@@ -182,7 +183,12 @@ struct Instance {
 
 Instance g;
 
-void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double ts, double rate)
+// Candidate lines as the reference's detectors print them: "time, DM, snr" (process_brute
+// with its own statistics, dedispersion_output.cpp:202-204; process_subband, :114-127, whose
+// time counts samples of the pass's downsample factor, held in the candidate's width), or
+// with caller statistics "time, DM, snr, mean, rms" (process_brute, :205-208).
+void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double ts, double rate,
+                      int spc)
 {
     SURVEY *s = g.survey;
     if (!g.fp || (!s->single_file_mode && g.written == 0)) {
@@ -204,8 +210,15 @@ void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double
     if (!g.fp) return;
     std::vector<float> dmv(g.plan->p.ndms);
     mdsm_plan_dm_values(g.plan, dmv.data());
-    for (long long i = 0; i < nc && i < (long long)c.size(); ++i)
-        fprintf(g.fp, "%lf, %f, %f\n", ts + c[i].sample * rate, dmv[c[i].dm_idx], c[i].snr);
+    const bool with_stats = g.plan->p.kind == 1 && g.cmean;
+    for (long long i = 0; i < nc && i < (long long)c.size(); ++i) {
+        const double t = ts + (double)c[i].sample * rate * (double)std::max(1, c[i].width);
+        if (with_stats)
+            fprintf(g.fp, "%lf, %f, %f, %f, %f  \n", t, dmv[c[i].dm_idx], c[i].snr,
+                    g.cmean[c[i].sample / spc], g.crms[c[i].sample / spc]);
+        else
+            fprintf(g.fp, "%lf, %f, %f\n", t, dmv[c[i].dm_idx], c[i].snr);
+    }
     fflush(g.fp);
     if (!s->single_file_mode) {
         g.written += g.prev_read;
@@ -257,18 +270,29 @@ mdsm_status process_block(unsigned data_read)
     MDSM_TRY(plan_run_device(p, g.d_in[cur], g.stride, g.d_in_bytes, g.d_out, ns, g.st));
     long long nc = 0;
     std::vector<mdsm_candidate> c(1 << 16);
-    if (p.kind == 1 && g.survey->useBruteForce) {
-        MDSM_TRY(ref_detect(static_cast<const float *>(g.d_out), p.ndms, (int)ns,
-                            g.survey->lowdm, g.survey->dmstep, g.survey->detection_threshold,
-                            c.data(), (long long)c.size(), &nc, nullptr, nullptr, g.st));
-    }
+    // the reference's detectors (dedispersion_output.cpp:56-213): with the caller's noise
+    // statistics of the block when next_chunk was given them, one value per samplesPerChunk
+    const int spc = g.survey->samplesPerChunk ? (int)g.survey->samplesPerChunk : (int)ns;
+    const long long nchunks = (ns - 5) / spc + 1;
+    const float *y = static_cast<const float *>(g.d_out);
+    const float thr = g.survey->detection_threshold;
+    if (p.kind == 1 && g.cmean)
+        MDSM_TRY(ref_detect_chunked(y, p.ndms, (int)ns, g.survey->lowdm, g.survey->dmstep, thr,
+                                    g.cmean, g.crms, nchunks, spc, c.data(), (long long)c.size(),
+                                    &nc, g.st));
+    else if (p.kind == 1)
+        MDSM_TRY(ref_detect(y, p.ndms, (int)ns, g.survey->lowdm, g.survey->dmstep, thr, c.data(),
+                            (long long)c.size(), &nc, nullptr, nullptr, g.st));
+    else
+        MDSM_TRY(ref_detect_subband(p, y, ns, thr, g.cmean, g.crms, nchunks, spc, c.data(),
+                                    (long long)c.size(), &nc, g.st));
     MDSM_CUDA_TRY(cudaMemcpyAsync(g.h_out[cur], g.d_out, (size_t)p.ndms * ns * 4,
                                   cudaMemcpyDeviceToHost, g.st));
     MDSM_TRY(check_err_word(p.d_err, g.st));
     c.resize((size_t)std::min<long long>(nc, (long long)c.size()));
     g.cands = c;
     g.prev_read = data_read;
-    write_candidates(c, nc, g.ts, g.rate);
+    write_candidates(c, nc, g.ts, g.rate, spc);
     g.blocks++;
     return MDSM_OK;
 }
@@ -471,12 +495,14 @@ float *mdsm_initialiseMDSM(SURVEY *s)
 float *mdsm_next_chunk(unsigned int data_read, unsigned *samples, double timestamp,
                        double blockRate, float *mean, float *rms)
 {
-    (void)mean;
-    (void)rms;
     if (!g.live) {
         set_error("next_chunk before initialiseMDSM");
         return nullptr;
     }
+    // caller-owned noise statistics of the block being handed in (one value per
+    // samplesPerChunk samples); read by the detector when the block is processed
+    g.cmean = mean && rms ? mean : nullptr;
+    g.crms = mean && rms ? rms : nullptr;
     g.pending_read = data_read;
     if (data_read == 0) g.stopping = true;
     g.survey->timestamp = timestamp;

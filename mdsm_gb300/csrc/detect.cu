@@ -188,6 +188,163 @@ mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, 
 }
 
 // ---------------------------------------------------------------------------------------------
+// The reference detectors' other forms: process_brute with caller noise statistics (one mean
+// and rms per samplesPerChunk samples, dedispersion_output.cpp:198-209) and process_subband
+// (:56-132): per-row statistics when the caller gives none, else the caller's chunk
+// statistics.  One kernel applies the median-of-five test to any set of rows.
+// ---------------------------------------------------------------------------------------------
+
+// One thread per row: dedispersion_output.cpp:87-97, sequential double sums (total += x,
+// total2 += pow(x, 2), exact for a float x) and the float mean / rms the reference keeps.
+__global__ void k_row_stats_seq(const float *__restrict__ buf, long long stride, int nrows,
+                                int nvalid, float2 *__restrict__ stats)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= nrows) return;
+    const float *r = buf + (size_t)k * stride;
+    double t1 = 0.0, t2 = 0.0;
+    for (int t = 0; t < nvalid; ++t) {
+        const double v = (double)__ldg(r + t);
+        t1 = __dadd_rn(t1, v);
+        t2 = __dadd_rn(t2, __dmul_rn(v, v));
+    }
+    const float lm = __double2float_rn(__ddiv_rn(t1, (double)nvalid));
+    const double var = __dadd_rn(__ddiv_rn(t2, (double)nvalid), -__dmul_rn((double)lm, (double)lm));
+    stats[k] = make_float2(lm, __double2float_rn(__dsqrt_rn(var)));
+}
+
+// Median-of-five test on rows [nrows][nvalid] (row pitch stride) whose DMs are dmv[row]:
+// median - mean >= rms * threshold and DM > 1, with (mean, rms) the row's (rowstats) or the
+// caller's chunk values cmean/crms[t / spc].  snr_mode 0 prints median / rms (process_subband,
+// and process_brute without caller statistics), 1 (median - mean) / rms (process_brute with
+// them).  Candidates carry the row, the sample and `width`.
+__global__ void k_median_detect(const float *__restrict__ buf, long long stride, int nrows,
+                                int nvalid, const float *__restrict__ dmv, float threshold,
+                                const float2 *__restrict__ rowstats,
+                                const float *__restrict__ cmean, const float *__restrict__ crms,
+                                int spc, int snr_mode, int width, int row0,
+                                DevCand *__restrict__ cands,
+                                unsigned long long *__restrict__ count, long long cap)
+{
+    const int k = blockIdx.y;
+    if (k >= nrows || !((double)__ldg(dmv + k) > 1.0)) return;
+    const float *r = buf + (size_t)k * stride;
+    float2 rs = make_float2(0.0f, 0.0f);
+    if (rowstats) rs = rowstats[k];
+    const unsigned nl = (unsigned)nvalid - 4u;
+    for (unsigned l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
+        const float m = median5(__ldg(r + l), __ldg(r + l + 1), __ldg(r + l + 2), __ldg(r + l + 3),
+                                __ldg(r + l + 4));
+        const float mean = rowstats ? rs.x : __ldg(cmean + l / (unsigned)spc);
+        const float rms = rowstats ? rs.y : __ldg(crms + l / (unsigned)spc);
+        if (__fsub_rn(m, mean) >= __fmul_rn(rms, threshold)) {
+            const float snr = snr_mode ? __fdiv_rn(__fsub_rn(m, mean), rms) : __fdiv_rn(m, rms);
+            const unsigned long long at = atomicAdd(count, 1ull);
+            if ((long long)at < cap) cands[at] = DevCand{row0 + k, (int32_t)l, width, snr};
+        }
+    }
+}
+
+namespace {
+
+// Work area of the median detectors: counter, DM values, row statistics, chunk statistics,
+// candidate records.
+struct MedianWork {
+    unsigned long long *count;
+    float *dmv;
+    float2 *rowstats;
+    float *cmean, *crms;
+    DevCand *cands;
+};
+
+mdsm_status median_work(int nrows, long long nchunks, long long cap, MedianWork *w)
+{
+    auto up = [](size_t b) { return (b + 255) / 256 * 256; };
+    const size_t o_dmv = 256, o_rs = o_dmv + up((size_t)nrows * 4);
+    const size_t o_cm = o_rs + up((size_t)nrows * 8), o_cr = o_cm + up((size_t)nchunks * 4);
+    const size_t o_c = o_cr + up((size_t)nchunks * 4);
+    void *sc = nullptr;
+    MDSM_TRY(scratch_get(o_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand), &sc));
+    char *b = static_cast<char *>(sc);
+    w->count = reinterpret_cast<unsigned long long *>(b);
+    w->dmv = reinterpret_cast<float *>(b + o_dmv);
+    w->rowstats = reinterpret_cast<float2 *>(b + o_rs);
+    w->cmean = reinterpret_cast<float *>(b + o_cm);
+    w->crms = reinterpret_cast<float *>(b + o_cr);
+    w->cands = reinterpret_cast<DevCand *>(b + o_c);
+    return MDSM_OK;
+}
+
+}  // namespace
+
+mdsm_status ref_detect_chunked(const float *d_series, int ndms, int nsamp, float lowdm,
+                               float dmstep, float threshold, const float *h_mean,
+                               const float *h_rms, long long nchunks, int spc,
+                               mdsm_candidate *h_cands, long long cap, long long *ncand,
+                               cudaStream_t st)
+{
+    if (spc <= 0 || nchunks < (long long)(nsamp - 5) / spc + 1)
+        return fail(MDSM_ERANGE, "chunk statistics: fewer values than (nsamp - 4) / spc");
+    if (cap < 0) cap = 0;
+    MedianWork w;
+    MDSM_TRY(median_work(ndms, nchunks, cap, &w));
+    // the reference's DM of row k: lowdm + k * dmstep in float (dedispersion_output.cpp:194)
+    std::vector<float> dmv((size_t)ndms);
+    for (int k = 0; k < ndms; ++k) dmv[(size_t)k] = (lowdm + 0.0f) + (float)(unsigned)k * dmstep;
+    MDSM_CUDA_TRY(cudaMemsetAsync(w.count, 0, sizeof(unsigned long long), st));
+    MDSM_CUDA_TRY(cudaMemcpyAsync(w.dmv, dmv.data(), dmv.size() * 4, cudaMemcpyHostToDevice, st));
+    MDSM_CUDA_TRY(cudaMemcpyAsync(w.cmean, h_mean, (size_t)nchunks * 4, cudaMemcpyHostToDevice, st));
+    MDSM_CUDA_TRY(cudaMemcpyAsync(w.crms, h_rms, (size_t)nchunks * 4, cudaMemcpyHostToDevice, st));
+    dim3 grid((unsigned)std::min<long long>((nsamp + 255) / 256, 64), (unsigned)ndms);
+    k_median_detect<<<grid, 256, 0, st>>>(d_series, nsamp, ndms, nsamp, w.dmv, threshold,
+                                          nullptr, w.cmean, w.crms, spc, 1, 1, 0, w.cands,
+                                          w.count, cap);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return fetch_cands(w.cands, w.count, cap, h_cands, ncand, st);
+}
+
+mdsm_status ref_detect_subband(const Plan &p, const float *d_series, long long out_stride,
+                               float threshold, const float *h_mean, const float *h_rms,
+                               long long nchunks, int spc, mdsm_candidate *h_cands, long long cap,
+                               long long *ncand, cudaStream_t st)
+{
+    if (p.kind != 2) return fail(MDSM_EINVAL, "subband detector: not a subband plan");
+    if (h_mean && (!h_rms || spc <= 0 || nchunks < (long long)(p.nsamp - 5) / spc + 1))
+        return fail(MDSM_ERANGE, "chunk statistics: fewer values than (nsamp - 4) / spc");
+    if (cap < 0) cap = 0;
+    MedianWork w;
+    MDSM_TRY(median_work(p.ndms, h_mean ? nchunks : 0, cap, &w));
+    MDSM_CUDA_TRY(cudaMemsetAsync(w.count, 0, sizeof(unsigned long long), st));
+    MDSM_CUDA_TRY(cudaMemcpyAsync(w.dmv, p.dm_values.data(), (size_t)p.ndms * 4,
+                                  cudaMemcpyHostToDevice, st));
+    if (h_mean) {
+        MDSM_CUDA_TRY(cudaMemcpyAsync(w.cmean, h_mean, (size_t)nchunks * 4,
+                                      cudaMemcpyHostToDevice, st));
+        MDSM_CUDA_TRY(cudaMemcpyAsync(w.crms, h_rms, (size_t)nchunks * 4,
+                                      cudaMemcpyHostToDevice, st));
+    }
+    for (size_t i = 0; i < p.pass_row0.size(); ++i) {
+        const int row0 = (int)p.pass_row0[i];
+        const int rows = (int)((i + 1 < p.pass_row0.size() ? p.pass_row0[i + 1] : p.ndms) - row0);
+        const int b = p.pass_bin[i];
+        const int nvalid = p.nsamp / b;
+        if (rows <= 0 || nvalid < 5) continue;
+        const float *rb = d_series + (size_t)row0 * out_stride;
+        float2 *rs = nullptr;
+        if (!h_mean) {
+            rs = w.rowstats + row0;
+            k_row_stats_seq<<<(rows + 127) / 128, 128, 0, st>>>(rb, out_stride, rows, nvalid, rs);
+        }
+        dim3 grid((unsigned)std::min<long long>((nvalid + 255) / 256, 64), (unsigned)rows);
+        k_median_detect<<<grid, 256, 0, st>>>(rb, out_stride, rows, nvalid, w.dmv + row0,
+                                              threshold, rs, w.cmean, w.crms, spc, 0, b, row0,
+                                              w.cands, w.count, cap);
+    }
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return fetch_cands(w.cands, w.count, cap, h_cands, ncand, st);
+}
+
+// ---------------------------------------------------------------------------------------------
 // Reference detector without allocation.
 //
 // Some callers cannot call cudaMalloc: a real-time pipeline stage that must not stall on the

@@ -172,6 +172,16 @@ mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float
                                float dmstep, float threshold, mdsm_candidate *h_cands,
                                long long cap, long long *ncand, float *mean, float *rms,
                                cudaStream_t st);
+mdsm_status ref_detect_chunked(const float *d_series, int ndms, int nsamp, float lowdm,
+                               float dmstep, float threshold, const float *h_mean,
+                               const float *h_rms, long long nchunks, int spc,
+                               mdsm_candidate *h_cands, long long cap, long long *ncand,
+                               cudaStream_t st);
+struct Plan;
+mdsm_status ref_detect_subband(const Plan &p, const float *d_series, long long out_stride,
+                               float threshold, const float *h_mean, const float *h_rms,
+                               long long nchunks, int spc, mdsm_candidate *h_cands, long long cap,
+                               long long *ncand, cudaStream_t st);
 mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
                           double threshold, mdsm_candidate *h_cands, long long cap,
                           long long *ncand, cudaStream_t st);

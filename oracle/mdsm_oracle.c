@@ -313,6 +313,69 @@ long orc_ref_detect(const float *buf, int tdms, int nsamp, float lowdm, float dm
     return n;
 }
 
+long orc_ref_detect_chunked(const float *buf, int tdms, int nsamp, float lowdm, float dmstep,
+                            float threshold, const float *mean, const float *rms, int spc,
+                            int32_t *dm_idx, int32_t *samp, float *snr, long cap)
+{
+    long n = 0;
+    for (int k = 0; k < tdms; k++) {
+        float thisdm = (lowdm + 0.0f) + (float)(unsigned)k * dmstep;
+        if (!((double)thisdm > 1.0)) continue;
+        const float *r = buf + (long)k * nsamp;
+        for (unsigned l = 0; l < (unsigned)nsamp - 4u; l++) {
+            float m = orc_median_of_five(r[l], r[l + 1], r[l + 2], r[l + 3], r[l + 4]);
+            float cm = mean[l / (unsigned)spc], cr = rms[l / (unsigned)spc];
+            float lim = cr * threshold;
+            if (m - cm >= lim) {
+                if (n < cap) {
+                    dm_idx[n] = k;
+                    samp[n] = (int32_t)l;
+                    snr[n] = (m - cm) / cr;
+                }
+                n++;
+            }
+        }
+    }
+    return n;
+}
+
+long orc_ref_detect_subband(const float *buf, long stride, int nrows, int nvalid,
+                            const float *dmv, float threshold, const float *mean,
+                            const float *rms, int spc, int32_t *dm_idx, int32_t *samp,
+                            float *snr, long cap)
+{
+    long n = 0;
+    for (int k = 0; k < nrows; k++) {
+        const float *r = buf + (long)k * stride;
+        float lm = 0.0f, lr = 0.0f;
+        if (!mean) {
+            double total = 0.0, total2 = 0.0;
+            for (int t = 0; t < nvalid; t++) {
+                total += (double)r[t];
+                total2 += (double)r[t] * (double)r[t];  /* pow(x, 2): exact for a float x */
+            }
+            lm = (float)(total / nvalid);
+            lr = (float)sqrt(total2 / nvalid - (double)lm * (double)lm);
+        }
+        if (!((double)dmv[k] > 1.0)) continue;
+        for (unsigned t = 0; t < (unsigned)nvalid - 4u; t++) {
+            float m = orc_median_of_five(r[t], r[t + 1], r[t + 2], r[t + 3], r[t + 4]);
+            float cm = mean ? mean[t / (unsigned)spc] : lm;
+            float cr = mean ? rms[t / (unsigned)spc] : lr;
+            float lim = cr * threshold;
+            if (m - cm >= lim) {
+                if (n < cap) {
+                    dm_idx[n] = k;
+                    samp[n] = (int32_t)t;
+                    snr[n] = m / cr;
+                }
+                n++;
+            }
+        }
+    }
+    return n;
+}
+
 /* ------------------------------------------------------------------------------------ */
 /* RFI clipping                                                                         */
 /* ------------------------------------------------------------------------------------ */

@@ -97,6 +97,20 @@ long orc_ref_detect(const float *buf, int tdms, int nsamp, float lowdm, float dm
                     float threshold, float mean, float rms, int32_t *dm_idx, int32_t *samp,
                     float *snr, long cap);
 
+/* process_brute (:172-211) with caller noise statistics (mean != NULL): the test uses
+ * mean[l / spc] and rms[l / spc]; the printed snr is (median - mean) / rms. */
+long orc_ref_detect_chunked(const float *buf, int tdms, int nsamp, float lowdm, float dmstep,
+                            float threshold, const float *mean, const float *rms, int spc,
+                            int32_t *dm_idx, int32_t *samp, float *snr, long cap);
+/* process_subband (:56-132) over nrows rows of nvalid samples (row pitch stride) whose DMs are
+ * dmv[row].  mean == NULL: per-row statistics (sequential double sums, :87-97) and
+ * snr = median / localrms; else chunk statistics (mean[t / spc], rms[t / spc]) and
+ * snr = median / rms. */
+long orc_ref_detect_subband(const float *buf, long stride, int nrows, int nvalid,
+                            const float *dmv, float threshold, const float *mean,
+                            const float *rms, int spc, int32_t *dm_idx, int32_t *samp,
+                            float *snr, long cap);
+
 /* ---- RFI clipping (rfi_clipper.cu:8-67, with its two defects fixed) ---- */
 /* Per-channel clip over [0, len) then per-spectrum clip over channels, in place.
  * kind: 0 = uint8, 1 = uint16, 2 = int16, 3 = float32.  k_chan/k_spec <= 0 skips that pass. */

@@ -56,6 +56,8 @@ def lib():
         _O.orc_subband_tempval.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_float, ctypes.c_float]
         _O.orc_ref_detect.restype = ctypes.c_long
+        _O.orc_ref_detect_chunked.restype = ctypes.c_long
+        _O.orc_ref_detect_subband.restype = ctypes.c_long
         _O.orc_boxcar_detect.restype = ctypes.c_long
         _O.orc_unpack.restype = ctypes.c_long
     return _O
@@ -156,6 +158,44 @@ def ref_detect(buf, lowdm, dmstep, threshold, cap=1 << 22):
                              _p(dm), _p(sa), _p(sn), ctypes.c_long(cap))
     k = min(n, cap)
     return (dm[:k].copy(), sa[:k].copy(), sn[:k].copy()), mean, rms
+
+
+def ref_detect_chunked(buf, lowdm, dmstep, threshold, mean, rms, spc, cap=1 << 22):
+    """process_brute with caller noise statistics: (dm, sample, snr)."""
+    buf = np.ascontiguousarray(buf, np.float32)
+    ndms, nsamp = buf.shape
+    mean = np.ascontiguousarray(mean, np.float32)
+    rms = np.ascontiguousarray(rms, np.float32)
+    dm = np.empty(cap, np.int32)
+    sa = np.empty(cap, np.int32)
+    sn = np.empty(cap, np.float32)
+    n = lib().orc_ref_detect_chunked(_p(buf), ndms, nsamp, ctypes.c_float(lowdm),
+                                     ctypes.c_float(dmstep), ctypes.c_float(threshold),
+                                     _p(mean), _p(rms), int(spc), _p(dm), _p(sa), _p(sn),
+                                     ctypes.c_long(cap))
+    k = min(n, cap)
+    return dm[:k].copy(), sa[:k].copy(), sn[:k].copy()
+
+
+def ref_detect_subband(rows, nvalid, dm_values, threshold, mean=None, rms=None, spc=1,
+                       cap=1 << 22):
+    """process_subband over rows [nrows][>= nvalid] with DMs dm_values: (row, sample, snr)."""
+    rows = np.ascontiguousarray(rows, np.float32)
+    nrows, stride = rows.shape
+    dmv = np.ascontiguousarray(dm_values, np.float32)
+    mp = rp = None
+    if mean is not None:
+        mean = np.ascontiguousarray(mean, np.float32)
+        rms = np.ascontiguousarray(rms, np.float32)
+        mp, rp = _p(mean), _p(rms)
+    dm = np.empty(cap, np.int32)
+    sa = np.empty(cap, np.int32)
+    sn = np.empty(cap, np.float32)
+    n = lib().orc_ref_detect_subband(_p(rows), ctypes.c_long(stride), nrows, int(nvalid),
+                                     _p(dmv), ctypes.c_float(threshold), mp, rp, int(spc),
+                                     _p(dm), _p(sa), _p(sn), ctypes.c_long(cap))
+    k = min(n, cap)
+    return dm[:k].copy(), sa[:k].copy(), sn[:k].copy()
 
 
 KIND = {np.dtype(np.uint8): 0, np.dtype(np.uint16): 1, np.dtype(np.int16): 2,

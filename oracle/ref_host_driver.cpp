@@ -16,6 +16,9 @@
 void process_brute(float *buffer, FILE *output, SURVEY *survey, int read_nsamp, size_t size,
                    double timestamp, double blockRate, time_t start_time, float *mean, float *rms);
 float medianOfFive(float n1, float n2, float n3, float n4, float n5);
+/* dedispersion_output.cpp:56-57 */
+void process_subband(float *buffer, FILE *output, SURVEY *survey, int read_nsamp, size_t size,
+                     double timestamp, double blockRate, float *mean, float *rms);
 
 extern "C" int ref_process_brute(float *buf, int tdms, int nsamp, float lowdm, float dmstep,
                                  float threshold, const char *outpath)
@@ -33,6 +36,60 @@ extern "C" int ref_process_brute(float *buf, int tdms, int nsamp, float lowdm, f
     if (!fp) return -1;
     process_brute(buf, fp, &s, nsamp, (size_t)tdms * (size_t)nsamp, 0.0, 1.0, time(NULL), NULL,
                   NULL);
+    fclose(fp);
+    return 0;
+}
+
+/* process_brute with caller noise statistics (mean != NULL, one value per spc samples). */
+extern "C" int ref_process_brute_chunked(float *buf, int tdms, int nsamp, float lowdm,
+                                         float dmstep, float threshold, int spc, float *mean,
+                                         float *rms, const char *outpath)
+{
+    SURVEY s;
+    memset(&s, 0, sizeof(s));
+    s.tdms = (unsigned)tdms;
+    s.nsamp = (unsigned)nsamp;
+    s.lowdm = lowdm;
+    s.dmstep = dmstep;
+    s.detection_threshold = threshold;
+    s.num_threads = 1;
+    s.useBruteForce = 1;
+    s.samplesPerChunk = (unsigned)spc;
+    FILE *fp = fopen(outpath, "w");
+    if (!fp) return -1;
+    process_brute(buf, fp, &s, nsamp, (size_t)tdms * (size_t)nsamp, 0.0, 1.0, time(NULL), mean,
+                  rms);
+    fclose(fp);
+    return 0;
+}
+
+/* process_subband for one pass (its pass loop reads the first pass's rows for every pass, so
+ * one pass is the case it computes as intended) with caller noise statistics; mean == NULL
+ * would dereference the null pointer at :63. */
+extern "C" int ref_process_subband_chunked(float *buf, int nsamp, float lowdm, float dmstep,
+                                           float sub_dmstep, int ncalls, int calldms,
+                                           int binsize, float threshold, int spc, float *mean,
+                                           float *rms, const char *outpath)
+{
+    SUBBAND_PASSES pass;
+    memset(&pass, 0, sizeof(pass));
+    pass.lowdm = lowdm;
+    pass.dmstep = dmstep;
+    pass.sub_dmstep = sub_dmstep;
+    pass.ncalls = ncalls;
+    pass.calldms = calldms;
+    pass.binsize = binsize;
+    SURVEY s;
+    memset(&s, 0, sizeof(s));
+    s.pass_parameters = &pass;
+    s.num_passes = 1;
+    s.num_threads = 1;
+    s.detection_threshold = threshold;
+    s.samplesPerChunk = (unsigned)spc;
+    FILE *fp = fopen(outpath, "w");
+    if (!fp) return -1;
+    const size_t rows = (size_t)ncalls * (size_t)calldms;
+    process_subband(buf, fp, &s, nsamp, rows * (size_t)(nsamp / binsize), 0.0, 1.0, mean, rms);
     fclose(fp);
     return 0;
 }

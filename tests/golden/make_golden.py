@@ -61,6 +61,46 @@ def host_fixtures():
                 rows.append((float(parts[0]), float(parts[1]), float(parts[2])))
     os.unlink(path)
     det = np.array(rows, np.float64).reshape(-1, 3)
+    # process_brute with caller noise statistics (one mean/rms per 256 samples)
+    spc = 256
+    nchunk = (cube.shape[1] - 4 + spc - 1) // spc
+    crng = np.random.default_rng(77)
+    cmean = (crng.standard_normal(nchunk) * 0.5).astype(np.float32)
+    crms = (3.0 + crng.uniform(0.0, 1.0, nchunk)).astype(np.float32)
+
+    def lines(path, nf):
+        out = []
+        with open(path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= nf:
+                    out.append(tuple(float(v) for v in parts[:nf]))
+        os.unlink(path)
+        return np.array(out, np.float64).reshape(-1, nf)
+
+    fd, path = tempfile.mkstemp(suffix=".dat")
+    os.close(fd)
+    rc = h.ref_process_brute_chunked(buf.ctypes.data_as(ctypes.c_void_p), cube.shape[0],
+                                     cube.shape[1], ctypes.c_float(0.0), ctypes.c_float(0.5),
+                                     ctypes.c_float(4.0), spc,
+                                     cmean.ctypes.data_as(ctypes.c_void_p),
+                                     crms.ctypes.data_as(ctypes.c_void_p), path.encode())
+    assert rc == 0
+    det_chunked = lines(path, 5)
+    # process_subband, one pass of 4 calls x 4 fine DMs, caller noise statistics; binsize 1
+    # and 2 (rows of nsamp / binsize samples)
+    sub = {}
+    for b in (1, 2):
+        rows = np.ascontiguousarray(cube[:, : cube.shape[1] // b])
+        fd, path = tempfile.mkstemp(suffix=".dat")
+        os.close(fd)
+        rc = h.ref_process_subband_chunked(rows.ctypes.data_as(ctypes.c_void_p), cube.shape[1],
+                                           ctypes.c_float(0.0), ctypes.c_float(0.5),
+                                           ctypes.c_float(2.0), 4, 4, b, ctypes.c_float(4.0),
+                                           spc, cmean.ctypes.data_as(ctypes.c_void_p),
+                                           crms.ctypes.data_as(ctypes.c_void_p), path.encode())
+        assert rc == 0
+        sub[b] = lines(path, 3)
     # read_block unpack for every bit width
     raw = rng.integers(0, 256, 256, dtype=np.uint8)
     fd, rpath = tempfile.mkstemp(suffix=".raw")
@@ -77,8 +117,12 @@ def host_fixtures():
     np.savez_compressed(os.path.join(HERE, "ref_host.npz"), median_in=tup, median_out=med,
                         detect_rows=det, detect_threshold=np.float32(4.0),
                         detect_lowdm=np.float32(0.0), detect_dmstep=np.float32(0.5),
+                        chunk_spc=np.int32(spc), chunk_mean=cmean, chunk_rms=crms,
+                        detect_chunked_rows=det_chunked, subband_rows_b1=sub[1],
+                        subband_rows_b2=sub[2],
                         unpack_raw=raw, **{"unpack_%d" % k: v for k, v in unpacked.items()})
-    print("wrote ref_host.npz: %d detections" % len(det))
+    print("wrote ref_host.npz: %d detections, %d with chunk statistics, %d / %d subband"
+          % (len(det), len(det_chunked), len(sub[1]), len(sub[2])))
 
 
 def gpu_fixtures(out_dir=HERE):

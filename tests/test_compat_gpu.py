@@ -103,3 +103,122 @@ def test_candidate_file_rotation(lib, orc, cuda, tmp_path):
         for ln in f:
             t = float(ln.split(",")[0])
             assert t_start + blocks[0] * block_s <= t < t_start + (blocks[-1] + 1) * block_s
+
+
+def _run_blocks(compat, survey, x, nblocks, ts0, tsamp, stats=None):
+    s = survey.contents
+    buf = compat.initialiseMDSM(survey)
+    nsamp, ms = s.nsamp, s.maxshift
+    outs = []
+    for k in range(nblocks + 2):
+        if k < nblocks:
+            if k == 0:
+                buf[:, : nsamp + ms] = x[:, : nsamp + ms]
+            else:
+                buf[:, ms: ms + nsamp] = x[:, k * nsamp + ms: (k + 1) * nsamp + ms]
+            data_read = nsamp
+        else:
+            data_read = 0
+        st = stats(k) if (stats and k < nblocks) else (None, None)
+        ptr, samples = compat.next_chunk(data_read, ts0 + k * nsamp * tsamp, tsamp, *st)
+        if ptr is not None and samples:
+            outs.append(compat.output_view(ptr, survey).copy())
+        if not compat.start_processing(data_read):
+            break
+    compat.tearDownMDSM()
+    return outs
+
+
+def test_caller_noise_statistics_lines(lib, orc, cuda, tmp_path):
+    """next_chunk's mean/rms (as the Pelican module passes them) switch process_brute to its
+    caller-statistics form: lines "time, DM, snr, mean, rms" equal to the oracle's."""
+    from mdsm_gb300 import compat, synth
+    obs = tmp_path / "obs.xml"
+    obs.write_text(OBS.format(dir=str(tmp_path)))
+    survey = compat.processSurveyParameters(obs)
+    s = survey.contents
+    s.samplesPerChunk = 512
+    tsamp, nblocks = 0.000064, 2
+    x = synth.gaussian_f32(128, nblocks * 4096 + 600, 5)
+    synth.inject(x, 1500.0, -0.78125, tsamp, [(1500, 25.0, 4, 2.0), (5500, 30.0, 4, 2.0)],
+                 K=4148.741601)
+    rng = np.random.default_rng(6)
+    stats = [((rng.standard_normal(8) * 0.2).astype(np.float32),
+              rng.uniform(8.0, 12.0, 8).astype(np.float32)) for _ in range(nblocks)]
+    outs = _run_blocks(compat, survey, x, nblocks, 100.0, tsamp, lambda k: stats[k])
+    assert len(outs) == nblocks
+    got = [tuple(float(v) for v in ln.split(",")) for ln in open(tmp_path / "cands.dat")
+           if ln.strip()]
+    want = []
+    for k, y in enumerate(outs):
+        dm, t, snr = orc.ref_detect_chunked(y, 0.0, 0.5, 6.0, stats[k][0], stats[k][1], 512)
+        for d, tt, sn in zip(dm, t, snr):
+            want.append((100.0 + k * 4096 * tsamp + tt * tsamp, 0.5 * d, sn,
+                         stats[k][0][tt // 512], stats[k][1][tt // 512]))
+    assert len(got) == len(want) > 0
+    for a, b in zip(got, want):
+        assert all(abs(u - v) <= 1e-6 * max(1.0, abs(v)) for u, v in zip(a, b)), (a, b)
+
+
+OBS_SUB = """<observation>
+    <frequencies top="1500.0" offset="-1.171875" />
+    <dm lowDM="0" numDMs="0" dmStep="0" useBruteForce="0" />
+    <samples number="4096" />
+    <channels number="256" subbands="16" />
+    <timing tsamp="0.000064" />
+    <detection threshold="5" />
+    <output filePrefix="sub" baseDirectory="{dir}" secondsPerFile="600"
+            usePCTime="0" singleFileMode="1" />
+    <passes>
+        <pass><lowDm>0.0</lowDm><highDm>32.0</highDm><deltaDm>0.5</deltaDm>
+              <downsample>1</downsample><subDm>4.0</subDm><numDms>64</numDms>
+              <dmsPerCall>8</dmsPerCall><ncalls>8</ncalls></pass>
+        <pass><lowDm>32.0</lowDm><highDm>96.0</highDm><deltaDm>2.0</deltaDm>
+              <downsample>2</downsample><subDm>16.0</subDm><numDms>32</numDms>
+              <dmsPerCall>8</dmsPerCall><ncalls>4</ncalls></pass>
+    </passes>
+</observation>
+"""
+
+
+def test_subband_stage_interface_detects(lib, orc, cuda, tmp_path):
+    """Subband mode through the stage interface: process_subband's per-row statistics branch
+    on the plan's own DMs, lines "time, DM, snr" with time counted in each pass's downsampled
+    samples, equal to the oracle's detections on the returned series."""
+    from mdsm_gb300 import compat, synth
+    obs = tmp_path / "obs.xml"
+    obs.write_text(OBS_SUB.format(dir=str(tmp_path)))
+    survey = compat.processSurveyParameters(obs)
+    tsamp, nblocks = 0.000064, 2
+    x = synth.gaussian_f32(256, nblocks * 4096 + 4000, 9)
+    synth.inject(x, 1500.0, -1.171875, tsamp, [(1000, 20.0, 6, 1.5), (6000, 60.0, 8, 1.5)],
+                 K=4148.741601)
+    outs = _run_blocks(compat, survey, x, nblocks, 50.0, tsamp)
+    assert len(outs) == nblocks
+    got = [tuple(float(v) for v in ln.split(",")) for ln in open(tmp_path / "sub.dat")
+           if ln.strip()]
+    import mdsm_gb300 as m
+    want = []
+    plan = m.SubbandPlan(256, 1500.0, -1.171875, tsamp, 4096, 16,
+                         [dict(lowdm=0.0, highdm=32.0, dmstep=0.5, sub_dmstep=4.0, ncalls=8,
+                               calldms=8),
+                          dict(lowdm=32.0, highdm=96.0, dmstep=2.0, sub_dmstep=16.0, ncalls=4,
+                               calldms=8, binsize=2)], in_dtype="f32", out_dtype="f32")
+    dm_values = plan.dm_values()
+    for k, y in enumerate(outs):
+        row0 = 0
+        for rows, b in ((64, 1), (32, 2)):
+            dm, t, snr = orc.ref_detect_subband(y[row0:row0 + rows], 4096 // b,
+                                                dm_values[row0:row0 + rows], 5.0)
+            for d, tt, sn in zip(dm, t, snr):
+                want.append((50.0 + k * 4096 * tsamp + tt * tsamp * b, dm_values[row0 + d], sn,
+                             row0 + d))
+            row0 += rows
+    # the library writes each block's candidates sorted by (row, sample)
+    want_sorted = []
+    for k in range(nblocks):
+        blk = [w for w in want if 50.0 + k * 4096 * tsamp <= w[0] < 50.0 + (k + 1) * 4096 * tsamp]
+        want_sorted += sorted(blk, key=lambda w: (w[3], w[0]))
+    assert len(got) == len(want_sorted) > 0
+    for a, b in zip(got, want_sorted):
+        assert abs(a[0] - b[0]) <= 1e-6 and abs(a[1] - b[1]) <= 1e-5 and abs(a[2] - b[2]) <= 1e-5

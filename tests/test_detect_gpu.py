@@ -94,3 +94,86 @@ def test_detrend_normalise_matches_oracle(lib, orc, cuda):
         full = (n // L) * L
         assert np.allclose(got[k, :full], want[:full], rtol=1e-5, atol=1e-5)
         assert np.array_equal(got[k, full:], y[k, full:])
+
+
+def _golden_cube():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("mk", os.path.join(GOLD, "make_golden.py"))
+    mk = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mk)
+    return mk.detector_cube()
+
+
+def test_chunked_detector_on_golden_block(lib, orc, cuda):
+    """process_brute with caller noise statistics: the reference's own lines (golden) and the
+    oracle's candidates."""
+    import mdsm_gb300 as m
+    torch = cuda
+    cube = _golden_cube()
+    g = np.load(os.path.join(GOLD, "ref_host.npz"))
+    spc, cm, cr = int(g["chunk_spc"]), g["chunk_mean"], g["chunk_rms"]
+    cands, n = m.ref_detect_chunked_device(torch.from_numpy(cube).cuda(), 0.0, 0.5, 4.0, cm, cr,
+                                           spc)
+    rows = g["detect_chunked_rows"]
+    assert n == len(rows) > 0
+    assert np.array_equal(cands["sample"].astype(np.float64), rows[:, 0])
+    assert np.allclose(cands["snr"], rows[:, 2], atol=5e-7, rtol=0)
+    dm, samp, snr = orc.ref_detect_chunked(cube, 0.0, 0.5, 4.0, cm, cr, spc)
+    assert np.array_equal(cands["dm_idx"], dm) and np.array_equal(cands["sample"], samp)
+    assert np.array_equal(cands["snr"], snr)
+
+
+def _subband_block(torch):
+    import mdsm_gb300 as m
+    from mdsm_gb300 import synth
+    nchans, nsamp, tsamp = 256, 4096, 64e-6
+    passes = [dict(lowdm=0.0, highdm=32.0, dmstep=0.5, sub_dmstep=4.0, ncalls=8, calldms=8),
+              dict(lowdm=32.0, highdm=96.0, dmstep=2.0, sub_dmstep=16.0, ncalls=4, calldms=8,
+                   binsize=2)]
+    plan = m.SubbandPlan(nchans, 1500.0, -300.0 / nchans, tsamp, nsamp, 16, passes,
+                         in_dtype="f32", out_dtype="f32")
+    nch, stride = plan.input_shape()
+    x = synth.gaussian_f32(nch, stride, 17)
+    synth.inject(x, 1500.0, -300.0 / nchans, tsamp, [(1200, 20.0, 6, 1.5), (3000, 60.0, 8, 1.5)],
+                 K=4148.741601)
+    d_in = plan.alloc_input()
+    d_in[: x.size].copy_(torch.from_numpy(x.ravel()))
+    d_out = plan.alloc_output()
+    plan.dedisperse_device(d_in, d_out)
+    torch.cuda.synchronize()
+    return plan, passes, d_out
+
+
+@pytest.mark.parametrize("chunked", [False, True])
+def test_subband_detector_matches_oracle(lib, orc, cuda, chunked):
+    """process_subband per pass (rows of nsamp / binsize samples) with per-row statistics or
+    caller chunk statistics, on the plan's own DMs, against the oracle pass by pass."""
+    import mdsm_gb300 as m
+    torch = cuda
+    plan, passes, d_out = _subband_block(torch)
+    y = d_out.cpu().numpy()
+    dmv = plan.dm_values()
+    spc = 512
+    rng = np.random.default_rng(4)
+    cm = (rng.standard_normal(8) * 0.1).astype(np.float32) if chunked else None
+    cr = (rng.uniform(1.0, 3.0, 8)).astype(np.float32) if chunked else None
+    cands, n = m.ref_detect_subband_device(plan, d_out, 5.0, cm, cr, spc)
+    want_dm, want_t, want_snr, want_w = [], [], [], []
+    row0 = 0
+    for p in passes:
+        rows = p["ncalls"] * p["calldms"]
+        b = p.get("binsize", 1)
+        nvalid = 4096 // b
+        dm, t, snr = orc.ref_detect_subband(y[row0:row0 + rows], nvalid, dmv[row0:row0 + rows],
+                                            5.0, cm, cr, spc)
+        want_dm += (dm + row0).tolist()
+        want_t += t.tolist()
+        want_snr += snr.tolist()
+        want_w += [b] * len(dm)
+        row0 += rows
+    order = np.lexsort((np.array(want_t), np.array(want_dm)))
+    assert n == len(want_dm) > 0
+    assert np.array_equal(cands["dm_idx"], np.array(want_dm)[order])
+    assert np.array_equal(cands["sample"], np.array(want_t)[order])
+    assert np.array_equal(cands["width"], np.array(want_w)[order])
+    assert np.array_equal(cands["snr"], np.array(want_snr, np.float32)[order])

@@ -45,6 +45,58 @@ def test_reference_detector_matches_reference(orc, host_gold):
     assert np.allclose(rows[:, 2], snr, atol=5e-7, rtol=0)
 
 
+def test_chunked_detector_matches_reference(orc, host_gold):
+    """process_brute with caller noise statistics (one mean/rms per 256 samples): the reference
+    prints time, DM, (median - mean)/rms, mean and rms."""
+    cube = _detector_cube()
+    spc = int(host_gold["chunk_spc"])
+    cm, cr = host_gold["chunk_mean"], host_gold["chunk_rms"]
+    dm, samp, snr = orc.ref_detect_chunked(cube, 0.0, 0.5, 4.0, cm, cr, spc)
+    rows = host_gold["detect_chunked_rows"]
+    assert len(rows) == len(dm) > 0
+    assert np.array_equal(rows[:, 0], samp.astype(np.float64))
+    assert np.allclose(rows[:, 1], dm.astype(np.float32) * np.float32(0.5), atol=5e-7)
+    assert np.allclose(rows[:, 2], snr, atol=5e-7, rtol=0)
+    assert np.allclose(rows[:, 3], cm[samp // spc], atol=5e-7, rtol=0)
+    assert np.allclose(rows[:, 4], cr[samp // spc], atol=5e-7, rtol=0)
+
+
+@pytest.mark.parametrize("binsize", [1, 2])
+def test_subband_detector_matches_reference(orc, host_gold, binsize):
+    """process_subband, one pass of 16 rows with caller noise statistics: time is
+    t * binsize, DM lowdm + row * dmstep, snr median / rms."""
+    cube = _detector_cube()
+    n = cube.shape[1] // binsize
+    rows_in = np.ascontiguousarray(cube[:, :n])
+    dmv = np.float32(0.0) + np.arange(16, dtype=np.float32) * np.float32(0.5)
+    spc = int(host_gold["chunk_spc"])
+    dm, samp, snr = orc.ref_detect_subband(rows_in, n, dmv, 4.0, host_gold["chunk_mean"],
+                                           host_gold["chunk_rms"], spc)
+    rows = host_gold["subband_rows_b%d" % binsize]
+    assert len(rows) == len(dm) > 0
+    assert np.array_equal(rows[:, 0], (samp * binsize).astype(np.float64))
+    assert np.allclose(rows[:, 1], dmv[dm], atol=5e-7)
+    assert np.allclose(rows[:, 2], snr, atol=5e-7, rtol=0)
+
+
+def test_subband_row_statistics(orc):
+    """The per-row statistics branch of process_subband (mean == NULL), which the reference
+    cannot run (it prints mean[0] first): restated, checked against numpy's FP64 sums."""
+    rng = np.random.default_rng(8)
+    rows = (rng.standard_normal((6, 1000)) * 2.0 + 1.0).astype(np.float32)
+    rows[4, 500:503] += np.float32(30.0)
+    dmv = np.array([0.5, 1.5, 2.5, 3.5, 4.5, 5.5], np.float32)
+    dm, samp, snr = orc.ref_detect_subband(rows, 1000, dmv, 5.0)
+    assert len(dm) > 0 and set(dm.tolist()) == {4}
+    r = rows[4].astype(np.float64)
+    lm = np.float32(r.sum() / 1000)
+    lr = np.float32(np.sqrt((r * r).sum() / 1000 - np.float64(lm) ** 2))
+    med = np.median(np.lib.stride_tricks.sliding_window_view(rows[4], 5), axis=1)
+    want = np.nonzero(med.astype(np.float32) - lm >= lr * np.float32(5.0))[0]
+    assert np.array_equal(samp, want)
+    assert np.allclose(snr, med[want].astype(np.float32) / lr, rtol=1e-7)
+
+
 def test_unpack_matches_reference(orc, host_gold):
     raw = host_gold["unpack_raw"]
     for nbits in (1, 2, 4, 8, 16):

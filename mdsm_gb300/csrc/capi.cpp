@@ -74,6 +74,7 @@ namespace {
 
 constexpr long long kHostSegMin = 16384;  // output samples per segment, at least
 constexpr int kHostSegMax = 16;           // segments per block, at most
+constexpr long long kHostSegEdge = 4096;  // first and last segment of a long block
 
 // Brute force from host buffers with the block cut into time segments: segment s's new input
 // columns are copied in on one stream, its output columns are computed on the caller's stream
@@ -88,10 +89,23 @@ mdsm_status dedisperse_host_pipelined(Plan &p, const void *h_in, long long h_in_
     const StageGeom &g = p.stages[0];
     const long long SZ = (long long)dtype_size(p.in_dtype);
     const long long row = (long long)p.nsamp + p.maxshift;
-    long long nseg = std::min<long long>(kHostSegMax, p.nsamp / kHostSegMin);
-    long long seg = (p.nsamp + nseg - 1) / nseg;
-    seg = (seg + 511) / 512 * 512;  // whole tiles of either kernel; 16-byte aligned offsets
-    nseg = (p.nsamp + seg - 1) / seg;
+    // Segment starts, multiples of 512 (whole tiles of either kernel, 16-byte aligned
+    // offsets).  Long blocks get short first and last segments (kHostSegEdge samples): the
+    // first copy-in and the last copy-out are the parts nothing overlaps.
+    std::vector<long long> starts{0};
+    long long m_lo = 0, m_hi = p.nsamp;  // the uniformly cut middle
+    if (p.nsamp >= 2 * kHostSegEdge + 2 * kHostSegMin) {
+        m_lo = kHostSegEdge;
+        m_hi = (p.nsamp - kHostSegEdge) / 512 * 512;
+        starts.push_back(m_lo);
+    }
+    const long long nmid = std::max<long long>(
+        1, std::min<long long>(kHostSegMax - (long long)starts.size() - (m_hi < p.nsamp),
+                               (m_hi - m_lo) / kHostSegMin));
+    const long long seg = ((m_hi - m_lo + nmid - 1) / nmid + 511) / 512 * 512;
+    for (long long t = m_lo + seg; t < m_hi; t += seg) starts.push_back(t);
+    if (m_hi < p.nsamp) starts.push_back(m_hi);
+    const long long nseg = (long long)starts.size();
     if (!p.s_in) MDSM_CUDA_TRY(cudaStreamCreateWithFlags(&p.s_in, cudaStreamNonBlocking));
     if (!p.s_out) MDSM_CUDA_TRY(cudaStreamCreateWithFlags(&p.s_out, cudaStreamNonBlocking));
     while ((long long)p.seg_ev.size() < 2 * nseg + 2) {
@@ -110,8 +124,8 @@ mdsm_status dedisperse_host_pipelined(Plan &p, const void *h_in, long long h_in_
     long long done = 0;  // input columns copied so far
     p.last_launches = 0;
     for (long long s = 0; s < nseg; ++s) {
-        const long long t0 = s * seg;
-        const long long len = std::min(seg, (long long)p.nsamp - t0);
+        const long long t0 = starts[(size_t)s];
+        const long long len = (s + 1 < nseg ? starts[(size_t)s + 1] : (long long)p.nsamp) - t0;
         const long long hi_col = s == nseg - 1 ? row : std::min(row, t0 + len + p.maxshift);
         if (hi_col > done) {
             MDSM_CUDA_TRY(cudaMemcpy2DAsync(di + done * SZ, (size_t)(p.in_stride * SZ),

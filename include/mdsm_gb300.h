@@ -12,8 +12,10 @@
  *   Dedispersed output is DM-major [ndms][nsamp] (src/mdsm/dedispersion_kernel.cu:46,75).
  *
  * Thread safety: different plans may be used from different threads concurrently; one plan is
- * used by one thread at a time.  The compatibility functions at the end keep the reference's
- * single global instance (src/mdsm/dedispersion_manager.cpp:14-34).
+ * used by one thread at a time.  The detector entry points may be called from several threads
+ * (calls on one device take turns on its work area; the no-allocation detector is the
+ * exception, see there).  The compatibility functions at the end keep the reference's single
+ * global instance (src/mdsm/dedispersion_manager.cpp:14-34).
  */
 #ifndef MDSM_GB300_H_
 #define MDSM_GB300_H_

@@ -13,6 +13,8 @@
 
 #include <algorithm>
 #include <cstring>
+#include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -22,25 +24,40 @@
 namespace mdsm {
 
 // ---------------------------------------------------------------------------------------------
-// scratch: one grow-only device buffer per process for detector work arrays
+// scratch: one grow-only device buffer per device for the detectors' work arrays.  A call
+// holds its device's buffer (a lock) until it returns, so detector calls from several threads
+// take turns; every such call synchronises its stream before returning.
 // ---------------------------------------------------------------------------------------------
 namespace {
-std::mutex g_scratch_mu;
-void *g_scratch = nullptr;
-size_t g_scratch_bytes = 0;
+struct ScratchSlot {
+    std::mutex mu;
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+std::mutex g_slots_mu;
+std::map<int, std::unique_ptr<ScratchSlot>> g_slots;
 }  // namespace
 
-static mdsm_status scratch_get(size_t bytes, void **out)
+static mdsm_status scratch_get(size_t bytes, void **out, std::unique_lock<std::mutex> *lease)
 {
-    std::lock_guard<std::mutex> lk(g_scratch_mu);
-    if (g_scratch_bytes < bytes) {
-        if (g_scratch) cudaFree(g_scratch);
-        g_scratch = nullptr;
-        g_scratch_bytes = 0;
-        MDSM_CUDA_TRY(cudaMalloc(&g_scratch, bytes));
-        g_scratch_bytes = bytes;
+    int dev = 0;
+    MDSM_CUDA_TRY(cudaGetDevice(&dev));
+    ScratchSlot *slot = nullptr;
+    {
+        std::lock_guard<std::mutex> lk(g_slots_mu);
+        std::unique_ptr<ScratchSlot> &u = g_slots[dev];
+        if (!u) u.reset(new ScratchSlot());
+        slot = u.get();
     }
-    *out = g_scratch;
+    *lease = std::unique_lock<std::mutex>(slot->mu);
+    if (slot->bytes < bytes) {
+        if (slot->p) cudaFree(slot->p);
+        slot->p = nullptr;
+        slot->bytes = 0;
+        MDSM_CUDA_TRY(cudaMalloc(&slot->p, bytes));
+        slot->bytes = bytes;
+    }
+    *out = slot->p;
     return MDSM_OK;
 }
 
@@ -166,7 +183,8 @@ mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, 
     const size_t off_c = off_sums + ((size_t)nchunks * sizeof(double2) + 255) / 256 * 256;
     const size_t bytes = off_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand);
     void *sc = nullptr;
-    MDSM_TRY(scratch_get(bytes, &sc));
+    std::unique_lock<std::mutex> lease;
+    MDSM_TRY(scratch_get(bytes, &sc, &lease));
     char *base = static_cast<char *>(sc);
     auto *d_count = reinterpret_cast<unsigned long long *>(base + off_cnt);
     auto *d_stats = reinterpret_cast<float *>(base + off_stats);
@@ -257,14 +275,16 @@ struct MedianWork {
     DevCand *cands;
 };
 
-mdsm_status median_work(int nrows, long long nchunks, long long cap, MedianWork *w)
+mdsm_status median_work(int nrows, long long nchunks, long long cap, MedianWork *w,
+                        std::unique_lock<std::mutex> *lease)
 {
     auto up = [](size_t b) { return (b + 255) / 256 * 256; };
     const size_t o_dmv = 256, o_rs = o_dmv + up((size_t)nrows * 4);
     const size_t o_cm = o_rs + up((size_t)nrows * 8), o_cr = o_cm + up((size_t)nchunks * 4);
     const size_t o_c = o_cr + up((size_t)nchunks * 4);
     void *sc = nullptr;
-    MDSM_TRY(scratch_get(o_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand), &sc));
+    MDSM_TRY(scratch_get(o_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand), &sc,
+                         lease));
     char *b = static_cast<char *>(sc);
     w->count = reinterpret_cast<unsigned long long *>(b);
     w->dmv = reinterpret_cast<float *>(b + o_dmv);
@@ -287,7 +307,8 @@ mdsm_status ref_detect_chunked(const float *d_series, int ndms, int nsamp, float
         return fail(MDSM_ERANGE, "chunk statistics: fewer values than (nsamp - 4) / spc");
     if (cap < 0) cap = 0;
     MedianWork w;
-    MDSM_TRY(median_work(ndms, nchunks, cap, &w));
+    std::unique_lock<std::mutex> lease;
+    MDSM_TRY(median_work(ndms, nchunks, cap, &w, &lease));
     // the reference's DM of row k: lowdm + k * dmstep in float (dedispersion_output.cpp:194)
     std::vector<float> dmv((size_t)ndms);
     for (int k = 0; k < ndms; ++k) dmv[(size_t)k] = (lowdm + 0.0f) + (float)(unsigned)k * dmstep;
@@ -313,7 +334,8 @@ mdsm_status ref_detect_subband(const Plan &p, const float *d_series, long long o
         return fail(MDSM_ERANGE, "chunk statistics: fewer values than (nsamp - 4) / spc");
     if (cap < 0) cap = 0;
     MedianWork w;
-    MDSM_TRY(median_work(p.ndms, h_mean ? nchunks : 0, cap, &w));
+    std::unique_lock<std::mutex> lease;
+    MDSM_TRY(median_work(p.ndms, h_mean ? nchunks : 0, cap, &w, &lease));
     MDSM_CUDA_TRY(cudaMemsetAsync(w.count, 0, sizeof(unsigned long long), st));
     MDSM_CUDA_TRY(cudaMemcpyAsync(w.dmv, p.dm_values.data(), (size_t)p.ndms * 4,
                                   cudaMemcpyHostToDevice, st));
@@ -768,7 +790,8 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
     const size_t off_c = off_ms + ((size_t)ndms * sizeof(double2) + 255) / 256 * 256;
     const size_t bytes = off_c + (size_t)std::max<long long>(cap, 1) * sizeof(DevCand);
     void *sc = nullptr;
-    MDSM_TRY(scratch_get(bytes, &sc));
+    std::unique_lock<std::mutex> lease;
+    MDSM_TRY(scratch_get(bytes, &sc, &lease));
     char *base = static_cast<char *>(sc);
     auto *d_count = reinterpret_cast<unsigned long long *>(base + off_cnt);
     auto *d_part = reinterpret_cast<double2 *>(base + off_part);

@@ -177,3 +177,44 @@ def test_subband_detector_matches_oracle(lib, orc, cuda, chunked):
     assert np.array_equal(cands["sample"], np.array(want_t)[order])
     assert np.array_equal(cands["width"], np.array(want_w)[order])
     assert np.array_equal(cands["snr"], np.array(want_snr, np.float32)[order])
+
+
+def test_detectors_from_several_threads(lib, cuda):
+    """Detector calls from four threads at once (each its own stream and series) return what
+    the same calls return one after another."""
+    import threading
+    import mdsm_gb300 as m
+    torch = cuda
+    rng = np.random.default_rng(31)
+    series = []
+    for i in range(4):
+        y = rng.integers(-3000, 3000, (16, 6000)).astype(np.int32)
+        y[i + 2, 1000 + 100 * i: 1010 + 100 * i] += 20000
+        series.append(torch.from_numpy(y).cuda())
+    fseries = [s.float() for s in series]
+    torch.cuda.synchronize()
+
+    def run(i):
+        st = torch.cuda.Stream()
+        a = m.boxcar_detect_device(series[i], nwidths=7, threshold=6.0, stream=st)
+        b = m.ref_detect_device(fseries[i], 0.0, 0.5, 5.0, stream=st)
+        st.synchronize()
+        return a, b
+
+    serial = [run(i) for i in range(4)]
+    out = [None] * 4
+
+    def worker(i):
+        for _ in range(5):
+            out[i] = run(i)
+
+    th = [threading.Thread(target=worker, args=(i,)) for i in range(4)]
+    for t in th:
+        t.start()
+    for t in th:
+        t.join()
+    for i in range(4):
+        (ca, na), (cb, mb, rb, nb) = out[i]
+        (sa, sna), (sb, smb, srb, snb) = serial[i]
+        assert na == sna > 0 and np.array_equal(ca, sa)
+        assert nb == snb and np.array_equal(cb, sb) and (mb, rb) == (smb, srb)

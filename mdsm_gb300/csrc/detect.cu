@@ -90,7 +90,7 @@ __global__ void k_ref_chunk_sums(const float *__restrict__ buf, unsigned mod, un
     for (unsigned j = 0; j < mod; ++j) {
         const double v = (double)__ldg(p + j);
         t1 = __dadd_rn(t1, v);
-        t2 = __dadd_rn(t2, __dmul_rn(v, v));
+        t2 = __fma_rn(v, v, t2);  // v*v exact: same as dmul + dadd
     }
     sums[i] = make_double2(t1, t2);
 }
@@ -224,7 +224,7 @@ __global__ void k_row_stats_seq(const float *__restrict__ buf, long long stride,
     for (int t = 0; t < nvalid; ++t) {
         const double v = (double)__ldg(r + t);
         t1 = __dadd_rn(t1, v);
-        t2 = __dadd_rn(t2, __dmul_rn(v, v));
+        t2 = __fma_rn(v, v, t2);  // v*v exact: same as dmul + dadd
     }
     const float lm = __double2float_rn(__ddiv_rn(t1, (double)nvalid));
     const double var = __dadd_rn(__ddiv_rn(t2, (double)nvalid), -__dmul_rn((double)lm, (double)lm));
@@ -504,7 +504,7 @@ __global__ void k_series_chunk_sums(const T *__restrict__ y, long long n, int nc
     for (long long i = c0; i < c1; ++i) {
         const double v = ld_d(r, i);
         p1 = __dadd_rn(p1, v);
-        p2 = __dadd_rn(p2, __dmul_rn(v, v));
+        p2 = __fma_rn(v, v, p2);  // v*v exact: same as dmul + dadd
     }
     part[(size_t)d * nch + ch] = make_double2(p1, p2);
 }
@@ -610,16 +610,69 @@ struct BoxGeom {
     static_assert(BUF % 2 == 0 && NBEST % 2 == 0, "pairs of positions");
 };
 
-// One CTA per (DM, tile).  Arithmetic per sample and width is FP32 (explicitly rounded, same
-// order as the oracle); only the per-DM statistics are FP64.  Each thread owns the position
-// pairs (2 tid + 2 kBoxThreads q, +1): it keeps their boxcar sums and best SNR / width in
-// registers across the widths and reads only the partner sums B[i + w/2] from shared memory
-// (one 8-byte load per pair), so one width costs per pair one shared load, one shared store,
-// four paired FP32 operations, the best-value updates and one barrier (the sums alternate
-// between two buffers).
+// Best SNR over the widths 1, 2, ..., 2^(NW-1) at series position t (0 <= t < n) and the first
+// width reaching it, for a position that passed the threshold.  The sums are formed in the
+// order of the tile loop (B_w[t] = B_{w/2}[t] + B_{w/2}[t + w/2]): a pairwise sum over the
+// samples in order, merging equal-sized partial sums as a binary counter carries, completes
+// the width-w sum exactly when w samples have been added.
+template <typename T, int NW>
+__device__ __noinline__ void box_best_at(const T *__restrict__ r, long long t, long long n,
+                                         float mu_f, const float *inv_w, float *bv, int *bw)
+{
+    float st[NW];
+    int sp = 0;
+    float best = -INFINITY;
+    int width = 0;
+    for (int j = 0; j < (1 << (NW - 1)) && t + j < n; ++j) {
+        st[sp++] = (float)__ldg(r + t + j);
+        for (int k = j + 1; (k & 1) == 0; k >>= 1) {
+            st[sp - 2] = __fadd_rn(st[sp - 2], st[sp - 1]);
+            --sp;
+        }
+        if (((j + 1) & j) == 0) {  // j + 1 = w, a power of two: st[0] is the width-w sum
+            const int w = j + 1;
+            const int l = 31 - __clz(w);
+            const float sv = __fmul_rn(__fadd_rn(st[0], -__fmul_rn((float)w, mu_f)), inv_w[l]);
+            if (sv > best) {
+                best = sv;
+                width = w;
+            }
+        }
+    }
+    *bv = best;
+    *bw = width;
+}
+
+// Samples of one tile into registers: the pairs (r0 + 2 tid + 2 kBoxThreads q, +1), zero
+// outside the series.
+template <typename T, int PAIRS>
+__device__ __forceinline__ void box_load(float2 (&v)[PAIRS], const T *__restrict__ r,
+                                         long long r0, long long n, int tid, bool interior)
+{
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q) {
+        const long long t = r0 + 2 * tid + 2 * kBoxThreads * q;
+        if (interior) {
+            v[q] = make_float2((float)__ldg(r + t), (float)__ldg(r + t + 1));
+        } else {
+            v[q].x = (t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
+            v[q].y = (t + 1 >= 0 && t + 1 < n) ? (float)__ldg(r + t + 1) : 0.0f;
+        }
+    }
+}
+
+// One CTA per (DM, run of `tpc` consecutive tiles); the samples of the next tile are loaded
+// into registers while the current one is searched.  Arithmetic per sample and width is FP32
+// (explicitly rounded, same order as the oracle); only the per-DM statistics are FP64.  Each
+// thread owns the position pairs (2 tid + 2 kBoxThreads q, +1): it keeps their boxcar sums and
+// best SNR in registers across the widths and reads only the partner sums B[i + w/2] from
+// shared memory (one 8-byte load per pair), so one width costs per pair one shared load, one
+// shared store, three paired FP32 operations, two maxima and one barrier (the sums alternate
+// between two buffers).  Which width gave the best SNR is needed only where the best passes
+// the threshold (few positions): there box_best_at forms it again, with the same sums.
 template <typename T, int NW>
 __global__ void __launch_bounds__(kBoxThreads, 5)
-    k_boxcar(const T *__restrict__ y, long long n, double threshold,
+    k_boxcar(const T *__restrict__ y, long long n, int tpc, double threshold,
              const double2 *__restrict__ musig, DevCand *__restrict__ cands,
              unsigned long long *__restrict__ count, long long cap)
 {
@@ -628,111 +681,114 @@ __global__ void __launch_bounds__(kBoxThreads, 5)
     extern __shared__ __align__(16) unsigned char sm[];
     float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
     float *best_s = B1 + G::BUF;
-    int *bw_s = reinterpret_cast<int *>(best_s + NBEST);
 
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
     if (!(sig > 0.0)) return;
     const float mu_f = __double2float_rn(mu);
     const float thr = __double2float_rn(threshold);
-    const long long t0 = (long long)blockIdx.x * kBoxTile;
-    const long long r0 = t0 - HL;  // series index of B[0] and best[0]
-    // every staged sample and every boxcar of the tile inside the series: no per-element tests
-    const bool interior = r0 >= 0 && r0 + PAIRS * 2 * kBoxThreads <= n;
     const T *r = y + (size_t)d * n;
     static_assert((kBoxThreads & (kBoxThreads - 1)) == 0, "power-of-two block");
     // (the mask tells the compiler tid < kBoxThreads, so range tests fold at compile time for
     // all but the last pair)
     const int tid = threadIdx.x & (kBoxThreads - 1);
-    float2 b[PAIRS], best[PAIRS];
-    int2 bw[PAIRS];
-#pragma unroll
-    for (int q = 0; q < PAIRS; ++q) {
-        const int i = 2 * tid + 2 * kBoxThreads * q;
-        const long long t = r0 + i;
-        float2 v;
-        if (interior) {
-            v = make_float2((float)__ldg(r + t), (float)__ldg(r + t + 1));
-        } else {
-            v.x = (t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
-            v.y = (t + 1 >= 0 && t + 1 < n) ? (float)__ldg(r + t + 1) : 0.0f;
-        }
-        b[q] = v;
-        *reinterpret_cast<float2 *>(B0 + i) = v;
-        best[q] = make_float2(-INFINITY, -INFINITY);
-        bw[q] = make_int2(0, 0);
-    }
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
     __shared__ float inv_w[NW];
     if (tid < NW)
         inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
-    __syncthreads();
+
+    const long long ntiles = (n + kBoxTile - 1) / kBoxTile;
+    const long long tile_lo = (long long)blockIdx.x * tpc;
+    const long long tile_hi = tile_lo + tpc < ntiles ? tile_lo + tpc : ntiles;
+    // every staged sample and every boxcar of the tile inside the series: no per-element tests
+    auto inside = [&](long long tile) {
+        const long long r0 = tile * kBoxTile - HL;
+        return r0 >= 0 && r0 + PAIRS * 2 * kBoxThreads <= n;
+    };
+    float2 nx[PAIRS];
+    box_load<T, PAIRS>(nx, r, tile_lo * kBoxTile - HL, n, tid, inside(tile_lo));
+    for (long long tile = tile_lo; tile < tile_hi; ++tile) {
+        const long long t0 = tile * kBoxTile;
+        const long long r0 = t0 - HL;  // series index of B[0] and best[0]
+        const bool interior = inside(tile);
+        float2 b[PAIRS], best[PAIRS];
 #pragma unroll
-    for (int l = 0; l < NW; ++l) {
-        const int w = 1 << l;
-        if (l > 0) {
-            // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
-            const int h = w >> 1;
-            const float *cur = (l & 1) ? B0 : B1;
-            float *nxt = (l & 1) ? B1 : B0;
+        for (int q = 0; q < PAIRS; ++q) {
+            b[q] = nx[q];
+            *reinterpret_cast<float2 *>(B0 + 2 * tid + 2 * kBoxThreads * q) = b[q];
+            best[q] = make_float2(-INFINITY, -INFINITY);
+        }
+        if (tile + 1 < tile_hi)  // in flight while this tile is searched
+            box_load<T, PAIRS>(nx, r, r0 + kBoxTile, n, tid, inside(tile + 1));
+        __syncthreads();
+#pragma unroll
+        for (int l = 0; l < NW; ++l) {
+            const int w = 1 << l;
+            if (l > 0) {
+                // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
+                const int h = w >> 1;
+                const float *cur = (l & 1) ? B0 : B1;
+                float *nxt = (l & 1) ? B1 : B0;
+#pragma unroll
+                for (int q = 0; q < PAIRS; ++q) {
+                    const int i = 2 * tid + 2 * kBoxThreads * q;
+                    // partner sums of positions i and i + 1
+                    const float2 pv = h == 1 ? make_float2(b[q].y, cur[i + 2])
+                                             : *reinterpret_cast<const float2 *>(cur + i + h);
+                    b[q] = add_f2(b[q], pv);
+                    *reinterpret_cast<float2 *>(nxt + i) = b[q];
+                }
+                __syncthreads();
+            }
+            const float wm = __fmul_rn((float)w, mu_f);
+            const float inv = inv_w[l];
 #pragma unroll
             for (int q = 0; q < PAIRS; ++q) {
                 const int i = 2 * tid + 2 * kBoxThreads * q;
-                // partner sums of positions i and i + 1
-                const float2 pv = h == 1 ? make_float2(b[q].y, cur[i + 2])
-                                         : *reinterpret_cast<const float2 *>(cur + i + h);
-                b[q] = add_f2(b[q], pv);
-                *reinterpret_cast<float2 *>(nxt + i) = b[q];
+                if (i >= NBEST) continue;  // i even and NBEST even: i + 1 < NBEST too
+                const long long t = r0 + i;
+                const float2 sv = mul_f2(add_f2(b[q], make_float2(-wm, -wm)), make_float2(inv, inv));
+                if (interior) {
+                    best[q].x = fmaxf(best[q].x, sv.x);
+                    best[q].y = fmaxf(best[q].y, sv.y);
+                } else {
+                    if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
+                    if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
+                }
             }
-            __syncthreads();
         }
-        const float wm = __fmul_rn((float)w, mu_f);
-        const float inv = inv_w[l];
+        bool any = false;
+#pragma unroll
+        for (int q = 0; q < PAIRS; ++q)
+            if (2 * tid + 2 * kBoxThreads * q < NBEST) any |= best[q].x >= thr || best[q].y >= thr;
+        // most tiles hold no sample over the threshold: skip the neighbourhood test there
+        if (!__syncthreads_or(any)) continue;
 #pragma unroll
         for (int q = 0; q < PAIRS; ++q) {
             const int i = 2 * tid + 2 * kBoxThreads * q;
-            if (i >= NBEST) continue;  // i even and NBEST even: i + 1 < NBEST too
-            const long long t = r0 + i;
-            const float2 sv = mul_f2(add_f2(b[q], make_float2(-wm, -wm)), make_float2(inv, inv));
-            const bool ok0 = interior || (t >= 0 && t + w <= n);
-            const bool ok1 = interior || (t + 1 >= 0 && t + 1 + w <= n);
-            if (ok0 && sv.x > best[q].x) {
-                best[q].x = sv.x;
-                bw[q].x = w;
-            }
-            if (ok1 && sv.y > best[q].y) {
-                best[q].y = sv.y;
-                bw[q].y = w;
-            }
+            if (i < NBEST) *reinterpret_cast<float2 *>(best_s + i) = best[q];
         }
-    }
-    bool any = false;
-#pragma unroll
-    for (int q = 0; q < PAIRS; ++q) {
-        const int i = 2 * tid + 2 * kBoxThreads * q;
-        if (i < NBEST) {
-            *reinterpret_cast<float2 *>(best_s + i) = best[q];
-            *reinterpret_cast<int2 *>(bw_s + i) = bw[q];
-            any |= best[q].x >= thr || best[q].y >= thr;
+        __syncthreads();
+        for (int q = tid; q < kBoxTile; q += kBoxThreads) {
+            const long long t = t0 + q;
+            if (t >= n) break;
+            const int i = q + HL;
+            const float bv = best_s[i];
+            if (!(bv >= thr)) continue;
+            float snr;
+            int width;
+            box_best_at<T, NW>(r, t, n, mu_f, inv_w, &snr, &width);
+            const int h = max(width / 2, 1);
+            bool keep = true;
+            for (int u = 1; u <= h && keep; ++u)
+                if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
+            for (int u = 1; u <= h && keep; ++u)
+                if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
+            if (!keep) continue;
+            const unsigned long long at = atomicAdd(count, 1ull);
+            if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, width, snr};
         }
-    }
-    // most tiles hold no sample over the threshold: skip the neighbourhood test there
-    if (!__syncthreads_or(any)) return;
-    for (int q = tid; q < kBoxTile; q += kBoxThreads) {
-        const long long t = t0 + q;
-        if (t >= n) break;
-        const int i = q + HL;
-        const float bv = best_s[i];
-        if (!(bv >= thr)) continue;
-        const int h = max(bw_s[i] / 2, 1);
-        bool keep = true;
-        for (int u = 1; u <= h && keep; ++u)
-            if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
-        for (int u = 1; u <= h && keep; ++u)
-            if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
-        if (!keep) continue;
-        const unsigned long long at = atomicAdd(count, 1ull);
-        if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, bw_s[i], bv};
+        // (the next tile writes best_s only after its own barriers)
     }
 }
 
@@ -742,11 +798,11 @@ static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, doub
                                  const double2 *musig, DevCand *cands,
                                  unsigned long long *count, long long cap, cudaStream_t st);
 
-// Shared memory of k_boxcar: two sum buffers, best (float) and width (int) of NBEST positions.
+// Shared memory of k_boxcar: two sum buffers and the best SNR of NBEST positions.
 template <int NW>
 static size_t boxcar_smem()
 {
-    return (size_t)BoxGeom<NW>::BUF * 8 + (size_t)BoxGeom<NW>::NBEST * 8;
+    return (size_t)BoxGeom<NW>::BUF * 8 + (size_t)BoxGeom<NW>::NBEST * 4;
 }
 
 template <typename T, int NW>
@@ -758,8 +814,12 @@ static cudaError_t launch_boxcar_nw(const T *y, int ndms, long long n, double th
     cudaError_t e = cudaFuncSetAttribute(k_boxcar<T, NW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    dim3 g3((unsigned)((n + kBoxTile - 1) / kBoxTile), (unsigned)ndms);
-    k_boxcar<T, NW><<<g3, kBoxThreads, smem, st>>>(y, n, threshold, musig, cands, count, cap);
+    // runs of up to 8 tiles per CTA while that leaves >= 8192 CTAs (several waves of 5 per SM)
+    const long long ntiles = (n + kBoxTile - 1) / kBoxTile;
+    int tpc = (int)std::min<long long>(8, std::max<long long>(1, ntiles * ndms / 8192));
+    tpc = (int)std::min<long long>(tpc, ntiles);
+    dim3 g3((unsigned)((ntiles + tpc - 1) / tpc), (unsigned)ndms);
+    k_boxcar<T, NW><<<g3, kBoxThreads, smem, st>>>(y, n, tpc, threshold, musig, cands, count, cap);
     return cudaGetLastError();
 }
 

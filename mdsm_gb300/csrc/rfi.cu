@@ -98,7 +98,7 @@ __global__ void __launch_bounds__(256)
             for (long long i = c0; i < c1; ++i) {
                 const double v = (double)row[i];
                 p1 = __dadd_rn(p1, v);
-                p2 = __dadd_rn(p2, __dmul_rn(v, v));
+                p2 = __fma_rn(v, v, p2);  // v*v exact: same as dmul + dadd
             }
             part[c] = make_double2(p1, p2);
         }
@@ -148,7 +148,7 @@ __global__ void k_clip_spectra(T *__restrict__ x, int nchans, long long stride, 
             for (int c = c0; c < c1; ++c) {
                 const double v = (double)x[(size_t)c * stride + t];
                 p1 = __dadd_rn(p1, v);
-                p2 = __dadd_rn(p2, __dmul_rn(v, v));
+                p2 = __fma_rn(v, v, p2);  // v*v exact: same as dmul + dadd
             }
             s1 = __dadd_rn(s1, p1);
             s2 = __dadd_rn(s2, p2);

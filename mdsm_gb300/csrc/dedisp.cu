@@ -245,6 +245,7 @@ struct PackedCfg {
     static_assert(NW >= kPCC, "one compute warp per staged row expands it");
     static_assert(NW * 32 >= kPCC * DB, "the compute threads copy a chunk's offsets");
     static_assert(DPW == 1 || DPW == 2, "one or two DM trials per warp");
+    static_assert(!U16OUT || SW == 1, "uint16 output from uint8 samples");
 };
 using CfgU8 = PackedCfg<1, 19, 2>;
 using CfgU8to16 = PackedCfg<1, 19, 2, true>;  // the first subband stage: uint16 subband series
@@ -481,8 +482,9 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
 #pragma unroll
                 for (int r = 0; r < PRW; ++r) {
                     A[j][r] = O[j][r] = 0u;
+                    if constexpr (!Cfg::U16OUT)
 #pragma unroll
-                    for (int e = 0; e < SPW; ++e) f[j][r][e] = 0;
+                        for (int e = 0; e < SPW; ++e) f[j][r][e] = 0;
                 }
         }
         const unsigned char *pbase =
@@ -544,7 +546,8 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 }
         }
         const bool last = (m.w & kChunkLast) != 0;
-        if (((m.y + 1) & 15) == 0 || last) {
+        // (uint16 output: an item has at most 257 channels, so its 16-bit lane sums are final)
+        if (!Cfg::U16OUT && (((m.y + 1) & 15) == 0 || last)) {
             // A = E + 2^(8 SW) O (mod 2^32): E and O hold the lane sums exactly
 #pragma unroll
             for (int j = 0; j < DPW; ++j)
@@ -582,15 +585,22 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 const long long t = t0 + SPW * (lane + 32 * r);
                 const bool whole = t + SPW - 1 < a.nsamp &&
                                    ((((uintptr_t)orow) | (t * osz)) & (SPW * osz - 1)) == 0;
-                if (whole && U16OUT) {
-                    if constexpr (SPW == 4)
-                        *reinterpret_cast<uint2 *>(orow + t * 2) =
-                            make_uint2((uint32_t)f[j][r][0] | ((uint32_t)f[j][r][1] << 16),
-                                       (uint32_t)f[j][r][2] | ((uint32_t)f[j][r][3] << 16));
-                    else
-                        *reinterpret_cast<uint32_t *>(orow + t * 2) =
-                            (uint32_t)f[j][r][0] | ((uint32_t)f[j][r][1] << 16);
-                } else if (whole && a.out_i32) {
+                if constexpr (U16OUT) {
+                    // samples 0 and 2 are E's lanes, 1 and 3 O's
+                    const uint32_t E = A[j][r] - (O[j][r] << 8);
+                    const uint32_t w01 = __byte_perm(E, O[j][r], 0x5410);
+                    const uint32_t w23 = __byte_perm(E, O[j][r], 0x7632);
+                    if (whole) {
+                        *reinterpret_cast<uint2 *>(orow + t * 2) = make_uint2(w01, w23);
+                    } else {
+                        const uint32_t v[4] = {w01 & 0xFFFFu, w01 >> 16, w23 & 0xFFFFu, w23 >> 16};
+#pragma unroll
+                        for (int e = 0; e < 4; ++e)
+                            if (t + e < a.nsamp) reinterpret_cast<uint16_t *>(orow)[t + e] = (uint16_t)v[e];
+                    }
+                    continue;
+                }
+                if (whole && a.out_i32) {
                     if constexpr (SPW == 4)
                         *reinterpret_cast<int4 *>(orow + t * 4) =
                             make_int4(f[j][r][0], f[j][r][1], f[j][r][2], f[j][r][3]);
@@ -606,13 +616,8 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                             make_float2((float)f[j][r][0], (float)f[j][r][1]);
                 } else {
 #pragma unroll
-                    for (int e = 0; e < SPW; ++e) {
-                        if (t + e >= a.nsamp) continue;
-                        if (U16OUT)
-                            reinterpret_cast<uint16_t *>(orow)[t + e] = (uint16_t)f[j][r][e];
-                        else
-                            store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
-                    }
+                    for (int e = 0; e < SPW; ++e)
+                        if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
                 }
             }
         }

@@ -90,7 +90,7 @@ typedef struct {
     int out_dtype;   /* MDSM_OUT_F32 / MDSM_OUT_I32                                 */
     int acc;         /* MDSM_ACC_*                                                  */
     int dm_block;    /* DM trials per CTA tile; 0 = choose                          */
-    int kernel;      /* 0 = choose, 1 = generic smem kernel, 2 = packed 8-bit kernel */
+    int kernel;      /* 0 = choose (packed kernel where it applies), 1 = generic kernel */
 } mdsm_brute_desc;
 
 /* Two-stage subband plan, one or more passes.  Replaces the subband set-up of initialiseMDSM
@@ -117,7 +117,8 @@ typedef struct {
     long long in_bytes;   /* device input bytes the device entry points may read            */
     long long out_bytes;  /* ndms * nsamp * output element size                              */
     int in_dtype, out_dtype, acc;
-    int dm_block, time_tile, kernel;
+    int dm_block, time_tile;
+    int kernel;           /* 1 generic, 2 packed 8-bit, 3 packed 16-bit                     */
     int nstages;          /* 1 brute force, 2 subband                                       */
     long long work_bytes; /* plan-owned device scratch (subband intermediate)               */
 } mdsm_plan_info;

@@ -904,6 +904,7 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
         return fail(MDSM_EINVAL, "input group pitch must be a multiple of 16 bytes");
     void *fn = select_kernel(g.in_dtype, g.acc_int, g.DPW, g.cc);
     unsigned threads = kNW * 32;
+    bool persistent = true;  // the packed kernels: a persistent grid over (block, tile, group)
     if (g.kernel == 2 && g.Db == CfgU8::DB) {
         fn = g.out_u16 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16>)
                        : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8>);
@@ -915,6 +916,8 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     } else if (g.kernel == 3) {
         fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16>);
         threads = CfgU16::THREADS;
+    } else {
+        persistent = false;
     }
     MDSM_CUDA_TRY(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)g.smem_bytes));
@@ -937,8 +940,8 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     a.ps = g.ps;
     a.err = d_err;
     const long long ntiles = (nsamp + g.T - 1) / g.T;
-    if (g.kernel == 2 || g.kernel == 3) {
-        // persistent: at most one CTA per SM walks the (DM block, tile, group) items
+    if (persistent) {
+        // at most one CTA per SM walks the (DM block, tile, group) items
         const long long nitems = (long long)g.nblk * ntiles * g.ngroups;
         if (nitems > 0x7fffffffLL) return fail(MDSM_EINVAL, "block too long for one launch");
         int dev = 0, sms = 0;

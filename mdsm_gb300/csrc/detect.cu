@@ -17,9 +17,11 @@
 #include <memory>
 #include <mutex>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "internal.h"
+#include "ptx.cuh"
 
 namespace mdsm {
 
@@ -643,26 +645,37 @@ __device__ __noinline__ void box_best_at(const T *__restrict__ r, long long t, l
     *bw = width;
 }
 
-// Samples of one tile into registers: the pairs (r0 + 2 tid + 2 kBoxThreads q, +1), zero
-// outside the series.
+// Asynchronous copy of one tile's samples into NB: this thread's pairs
+// (r0 + 2 tid + 2 kBoxThreads q, +1), zero outside the series.  Only the issuing thread reads
+// them back, so its own wait is the only synchronisation.
 template <typename T, int PAIRS>
-__device__ __forceinline__ void box_load(float2 (&v)[PAIRS], const T *__restrict__ r,
-                                         long long r0, long long n, int tid, bool interior)
+__device__ __forceinline__ void box_prefetch(uint32_t *NB, const T *__restrict__ r, long long r0,
+                                             long long n, int tid)
 {
+    static_assert(sizeof(T) == 4, "4-byte samples");
 #pragma unroll
-    for (int q = 0; q < PAIRS; ++q) {
-        const long long t = r0 + 2 * tid + 2 * kBoxThreads * q;
-        if (interior) {
-            v[q] = make_float2((float)__ldg(r + t), (float)__ldg(r + t + 1));
-        } else {
-            v[q].x = (t >= 0 && t < n) ? (float)__ldg(r + t) : 0.0f;
-            v[q].y = (t + 1 >= 0 && t + 1 < n) ? (float)__ldg(r + t + 1) : 0.0f;
+    for (int q = 0; q < PAIRS; ++q)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int i = 2 * tid + 2 * kBoxThreads * q + e;
+            const long long t = r0 + i;
+            const bool in = t >= 0 && t < n;
+            cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
         }
-    }
+    cp_async_commit();
 }
 
-// One CTA per (DM, run of `tpc` consecutive tiles); the samples of the next tile are loaded
-// into registers while the current one is searched.  Arithmetic per sample and width is FP32
+template <typename T>
+__device__ __forceinline__ float box_value(uint32_t raw)
+{
+    if constexpr (std::is_same<T, float>::value)
+        return __uint_as_float(raw);
+    else
+        return (float)(int32_t)raw;
+}
+
+// One CTA per (DM, run of `tpc` consecutive tiles); the samples of the next tile are copied
+// into shared memory (cp.async) while the current one is searched.  Arithmetic per sample and width is FP32
 // (explicitly rounded, same order as the oracle); only the per-DM statistics are FP64.  Each
 // thread owns the position pairs (2 tid + 2 kBoxThreads q, +1): it keeps their boxcar sums and
 // best SNR in registers across the widths and reads only the partner sums B[i + w/2] from
@@ -681,6 +694,7 @@ __global__ void __launch_bounds__(kBoxThreads, 5)
     extern __shared__ __align__(16) unsigned char sm[];
     float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
     float *best_s = B1 + G::BUF;
+    uint32_t *NB = reinterpret_cast<uint32_t *>(best_s + NBEST);  // next tile's samples
 
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
@@ -705,21 +719,22 @@ __global__ void __launch_bounds__(kBoxThreads, 5)
         const long long r0 = tile * kBoxTile - HL;
         return r0 >= 0 && r0 + PAIRS * 2 * kBoxThreads <= n;
     };
-    float2 nx[PAIRS];
-    box_load<T, PAIRS>(nx, r, tile_lo * kBoxTile - HL, n, tid, inside(tile_lo));
+    box_prefetch<T, PAIRS>(NB, r, tile_lo * kBoxTile - HL, n, tid);
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
         const long long t0 = tile * kBoxTile;
         const long long r0 = t0 - HL;  // series index of B[0] and best[0]
         const bool interior = inside(tile);
         float2 b[PAIRS], best[PAIRS];
+        cp_async_wait_all();
 #pragma unroll
         for (int q = 0; q < PAIRS; ++q) {
-            b[q] = nx[q];
-            *reinterpret_cast<float2 *>(B0 + 2 * tid + 2 * kBoxThreads * q) = b[q];
+            const int i = 2 * tid + 2 * kBoxThreads * q;
+            b[q] = make_float2(box_value<T>(NB[i]), box_value<T>(NB[i + 1]));
+            *reinterpret_cast<float2 *>(B0 + i) = b[q];
             best[q] = make_float2(-INFINITY, -INFINITY);
         }
         if (tile + 1 < tile_hi)  // in flight while this tile is searched
-            box_load<T, PAIRS>(nx, r, r0 + kBoxTile, n, tid, inside(tile + 1));
+            box_prefetch<T, PAIRS>(NB, r, r0 + kBoxTile, n, tid);
         __syncthreads();
 #pragma unroll
         for (int l = 0; l < NW; ++l) {
@@ -798,11 +813,13 @@ static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, doub
                                  const double2 *musig, DevCand *cands,
                                  unsigned long long *count, long long cap, cudaStream_t st);
 
-// Shared memory of k_boxcar: two sum buffers and the best SNR of NBEST positions.
+// Shared memory of k_boxcar: two sum buffers, the best SNR of NBEST positions and the next
+// tile's samples.
 template <int NW>
 static size_t boxcar_smem()
 {
-    return (size_t)BoxGeom<NW>::BUF * 8 + (size_t)BoxGeom<NW>::NBEST * 4;
+    using G = BoxGeom<NW>;
+    return (size_t)G::BUF * 8 + (size_t)G::NBEST * 4 + (size_t)G::PAIRS * 2 * kBoxThreads * 4;
 }
 
 template <typename T, int NW>

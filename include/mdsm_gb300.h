@@ -119,7 +119,7 @@ typedef struct {
     int in_dtype, out_dtype, acc;
     int dm_block, time_tile;
     int kernel;           /* 1 generic, 2 packed 8-bit, 3 packed 16-bit                     */
-    int nstages;          /* 1 brute force, 2 subband                                       */
+    int nstages;          /* 1 brute force; subband: 2 per pass (mdsm_plan_stage_info)       */
     long long work_bytes; /* plan-owned device scratch (subband intermediate)               */
 } mdsm_plan_info;
 
@@ -132,6 +132,16 @@ mdsm_status mdsm_brute_plan_create(const mdsm_brute_desc *desc, mdsm_plan **out)
 mdsm_status mdsm_subband_plan_create(const mdsm_subband_desc *desc, mdsm_plan **out);
 void mdsm_plan_destroy(mdsm_plan *plan);
 mdsm_status mdsm_plan_get_info(const mdsm_plan *plan, mdsm_plan_info *info);
+
+/* One launch stage of a plan (brute force: stage 0; subband pass i: stages 2i and 2i+1): the
+ * kernel it runs (1 generic, 2 packed 8-bit, 3 packed 16-bit), its DM block and time tile,
+ * and whether it writes uint16 subband series. */
+typedef struct {
+    int kernel, dm_block, time_tile, out_u16;
+    int nchans, ndms, ngroups, nsamp;
+    long long smem_bytes;
+} mdsm_stage_info;
+mdsm_status mdsm_plan_stage_info(const mdsm_plan *plan, int stage, mdsm_stage_info *info);
 /* Integer shifts, row-major [ndms][nchans] (brute) or stage tables (subband: stage 1
  * [ncalls][nchans] of the first pass when which = 1, stage 2 [ndms][nsubs] when which = 2). */
 mdsm_status mdsm_plan_shift_table(const mdsm_plan *plan, int which, int32_t *out);

@@ -86,6 +86,12 @@ class PlanInfo(ctypes.Structure):
                 ("work_bytes", ctypes.c_longlong)]
 
 
+class StageInfo(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_int) for n in ("kernel", "dm_block", "time_tile", "out_u16",
+                                            "nchans", "ndms", "ngroups", "nsamp")] + \
+               [("smem_bytes", ctypes.c_longlong)]
+
+
 class SigprocHeader(ctypes.Structure):
     _fields_ = [(n, ctypes.c_int) for n in ("nchans", "nbits", "nifs", "machine_id",
                                             "telescope_id", "data_type", "nbeams", "ibeam",
@@ -119,6 +125,7 @@ SIGNATURES = {
     "mdsm_subband_plan_create": (_st, [ctypes.POINTER(SubbandDesc), ctypes.POINTER(_vp)]),
     "mdsm_plan_destroy": (None, [_vp]),
     "mdsm_plan_get_info": (_st, [_vp, ctypes.POINTER(PlanInfo)]),
+    "mdsm_plan_stage_info": (_st, [_vp, ctypes.c_int, ctypes.POINTER(StageInfo)]),
     "mdsm_plan_shift_table": (_st, [_vp, _i, _vp]),
     "mdsm_plan_dm_values": (_st, [_vp, _vp]),
     "mdsm_plan_dmshifts": (_st, [_vp, _vp]),

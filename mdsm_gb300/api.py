@@ -9,7 +9,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import (ACC, DTYPES, OUT_DTYPES, SHIFT_MODES, BruteDesc, Candidate, PlanInfo,
-                   Segment, SubbandDesc, SUBBAND_PASSES, check, load)
+                   Segment, StageInfo, SubbandDesc, SUBBAND_PASSES, check, load)
 
 _NP_OF = {"u8": np.uint8, "u16": np.uint16, "i16": np.int16, "f32": np.float32,
           "i32": np.int32}
@@ -41,6 +41,12 @@ class _PlanBase:
     def info(self):
         i = PlanInfo()
         check(load().mdsm_plan_get_info(self._h, ctypes.byref(i)))
+        return i
+
+    def stage_info(self, stage):
+        """Launch stage `stage` (brute force: 0; subband pass i: 2i, 2i+1)."""
+        i = StageInfo()
+        check(load().mdsm_plan_stage_info(self._h, int(stage), ctypes.byref(i)))
         return i
 
     @property

@@ -223,6 +223,25 @@ mdsm_status mdsm_plan_get_info(const mdsm_plan *plan, mdsm_plan_info *info)
     return MDSM_OK;
 }
 
+mdsm_status mdsm_plan_stage_info(const mdsm_plan *plan, int stage, mdsm_stage_info *info)
+{
+    if (!plan || !info) return fail(MDSM_EINVAL, "null argument");
+    const Plan &p = plan->p;
+    if (stage < 0 || stage >= (int)p.stages.size()) return fail(MDSM_EINVAL, "no such stage");
+    const StageGeom &g = p.stages[(size_t)stage];
+    std::memset(info, 0, sizeof(*info));
+    info->kernel = g.kernel;
+    info->dm_block = g.Db;
+    info->time_tile = g.T;
+    info->out_u16 = g.out_u16;
+    info->nchans = g.nchans;
+    info->ndms = g.ndms;
+    info->ngroups = g.ngroups;
+    info->nsamp = (int)g.nsamp;
+    info->smem_bytes = (long long)g.smem_bytes;
+    return MDSM_OK;
+}
+
 mdsm_status mdsm_plan_shift_table(const mdsm_plan *plan, int which, int32_t *out)
 {
     if (!plan || !out) return fail(MDSM_EINVAL, "null argument");

@@ -229,16 +229,17 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
 // ------------------------------------------------------------------------------------------
 constexpr int kPCC = 16;         // channels per stage
 constexpr int kPNR = 3;          // raw stages in flight
-constexpr int kPT = 512;         // samples per tile
+constexpr int kPT = 512;         // samples per tile (the uint16-output configurations: 1024)
 
-template <int SW_, int NW_, int DPW_, bool U16OUT_ = false>
+template <int SW_, int NW_, int DPW_, bool U16OUT_ = false, int PT_ = kPT>
 struct PackedCfg {
     static constexpr bool U16OUT = U16OUT_;       // store the sums as uint16
     static constexpr int SW = SW_;                // bytes per sample
     static constexpr int SPW = 4 / SW;            // samples per word = phase copies
     static constexpr int NW = NW_;                // compute warps (the producer is warp NW)
     static constexpr int DPW = DPW_;              // DM trials per compute warp
-    static constexpr int PRW = kPT / (32 * SPW);  // words per lane per DM trial
+    static constexpr int PT = PT_;                // samples per tile
+    static constexpr int PRW = PT / (32 * SPW);   // words per lane per DM trial
     static constexpr int DB = NW * DPW;           // DM trials per tile
     static constexpr int DBS = (DB + 3) / 4 * 4;  // offsets per channel as stored (16-byte rows)
     static constexpr int THREADS = (NW + 1) * 32;
@@ -246,11 +247,15 @@ struct PackedCfg {
     static_assert(NW * 32 >= kPCC * DB, "the compute threads copy a chunk's offsets");
     static_assert(DPW == 1 || DPW == 2, "one or two DM trials per warp");
     static_assert(!U16OUT || SW == 1, "uint16 output from uint8 samples");
+    static_assert(PT % (32 * SPW) == 0, "whole words per lane");
 };
 using CfgU8 = PackedCfg<1, 19, 2>;
-using CfgU8to16 = PackedCfg<1, 19, 2, true>;  // the first subband stage: uint16 subband series
 using CfgU8w16 = PackedCfg<1, 16, 2>;         // 32-trial blocks, for trial counts of 32 k
-using CfgU8w16to16 = PackedCfg<1, 16, 2, true>;
+// The first subband stage (uint16 subband series): without the int32 flush registers there
+// is room for 1024-sample tiles, which halve the per-chunk costs per add; 768- or 512-sample
+// tiles where the wider staging does not fit in shared memory.
+template <int NW, int PT>
+using CfgU8to16T = PackedCfg<1, NW, 2, true, PT>;
 using CfgU16 = PackedCfg<2, 16, 1>;
 
 // Work items of the packed kernels are (beam, DM block, time tile, group) tiles; a CTA runs a
@@ -374,7 +379,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 return;
             }
             const KArgs &a = src.args(p_w.x);
-            const long long t0 = (long long)p_w.z * kPT;
+            const long long t0 = (long long)p_w.z * Cfg::PT;
             const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
             const int c0 = p_k * kPCC;
             const int nc = min(kPCC, a.nchans - c0);
@@ -383,7 +388,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             if (lane < nc) {
                 const int c = c0 + lane;
                 const long long start = t0 + p_ss.x;
-                const long long end = start + kPT + p_ss.y;
+                const long long end = start + Cfg::PT + p_ss.y;
                 const long long sb = (start * SW) & ~15LL;  // bytes
                 const long long eb = (end * SW + 15) & ~15LL;
                 bytes = (unsigned)(eb - sb);
@@ -571,7 +576,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         // series of the first stage, uint16)
         const int4 w = src.item(m.x);
         const KArgs &a = src.args(w.x);
-        const long long t0 = (long long)w.z * kPT;
+        const long long t0 = (long long)w.z * Cfg::PT;
         constexpr bool U16OUT = Cfg::U16OUT;
         constexpr int osz = U16OUT ? 2 : 4;
 #pragma unroll
@@ -771,7 +776,7 @@ template <class Cfg>
 bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
 {
     g.Db = Cfg::DB;
-    g.T = kPT;
+    g.T = Cfg::PT;
     g.R = Cfg::PRW * Cfg::SPW;
     g.DPW = Cfg::DPW;
     g.cc = kPCC;
@@ -779,7 +784,7 @@ bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
     const int maxspan = tile_tables(g, S);
     // raw row: the tile plus the span, from the 16-byte boundary below smin, in bytes
     const int rawcap =
-        (int)(((long long)(kPT + maxspan) * Cfg::SW + 32 + 15) / 16 * 16) + 16;
+        (int)(((long long)(Cfg::PT + maxspan) * Cfg::SW + 32 + 15) / 16 * 16) + 16;
     const int ps = rawcap - 16;  // nwp = ps/4 words; the expansion reads word nwp too
     if (packed_smem<Cfg>(rawcap, ps) > 220 * 1024) return false;
     g.max_span = maxspan;
@@ -825,8 +830,20 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
             // last 38-trial block would leave more than that idle (e.g. 64 or 128 trials)
             const int n38 = (g.ndms + CfgU8::DB - 1) / CfgU8::DB * CfgU8::DB;
             const int n32 = (g.ndms + CfgU8w16::DB - 1) / CfgU8w16::DB * CfgU8w16::DB;
-            if (n38 <= 1.05 * n32 && packed_tables<CfgU8>(g, S, 2)) return MDSM_OK;
-            if (packed_tables<CfgU8w16>(g, S, 2)) return MDSM_OK;
+            const bool w38 = n38 <= 1.05 * n32;
+            if (g.out_u16) {
+                if (w38 && (packed_tables<CfgU8to16T<19, 1024>>(g, S, 2) ||
+                            packed_tables<CfgU8to16T<19, 768>>(g, S, 2) ||
+                            packed_tables<CfgU8to16T<19, 512>>(g, S, 2)))
+                    return MDSM_OK;
+                if (packed_tables<CfgU8to16T<16, 1024>>(g, S, 2) ||
+                    packed_tables<CfgU8to16T<16, 768>>(g, S, 2) ||
+                    packed_tables<CfgU8to16T<16, 512>>(g, S, 2))
+                    return MDSM_OK;
+            } else {
+                if (w38 && packed_tables<CfgU8>(g, S, 2)) return MDSM_OK;
+                if (packed_tables<CfgU8w16>(g, S, 2)) return MDSM_OK;
+            }
         }
         if (g.in_dtype == MDSM_U16 && !g.out_u16 &&
             (long long)g.nchans * 65535 <= 0x7fffffffLL &&
@@ -906,12 +923,16 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     unsigned threads = kNW * 32;
     bool persistent = true;  // the packed kernels: a persistent grid over (block, tile, group)
     if (g.kernel == 2 && g.Db == CfgU8::DB) {
-        fn = g.out_u16 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16>)
-                       : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8>);
+        fn = !g.out_u16     ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8>)
+             : g.T == 1024 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<19, 1024>>)
+             : g.T == 768  ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<19, 768>>)
+                           : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<19, 512>>);
         threads = CfgU8::THREADS;
     } else if (g.kernel == 2) {
-        fn = g.out_u16 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8w16to16>)
-                       : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8w16>);
+        fn = !g.out_u16     ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8w16>)
+             : g.T == 1024 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<16, 1024>>)
+             : g.T == 768  ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<16, 768>>)
+                           : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<16, 512>>);
         threads = CfgU8w16::THREADS;
     } else if (g.kernel == 3) {
         fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16>);

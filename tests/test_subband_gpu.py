@@ -83,3 +83,30 @@ def test_subband_recovers_injected_pulse(lib, orc, cuda):
     z = (y - y.mean(axis=1, keepdims=True)) / y.std(axis=1, keepdims=True)
     d, t = np.unravel_index(np.argmax(z), z.shape)
     assert abs(dms[d] - 150.0) < 2.0 and abs(t - 3000) < 10
+
+
+def test_subband_first_stage_tile_widths(lib, orc, cuda):
+    """The uint16 first stage takes 1024-, 768- or 512-sample tiles as its staging fits shared
+    memory (wider sub-DM steps widen the shift span); every width, and the int32 fallback past
+    them, against the oracle."""
+    import mdsm_gb300 as m
+    torch = cuda
+    nchans, nsubs, tsamp, fch1, foff = 1024, 16, 64e-6, 1500.0, -300.0 / 1024
+    nsamp = 3000
+    seen = set()
+    for sub_dmstep in (2.0, 6.0, 12.0, 40.0):
+        p = dict(lowdm=0.0, highdm=32 * sub_dmstep, dmstep=sub_dmstep / 16, sub_dmstep=sub_dmstep,
+                 ncalls=32, calldms=16)
+        plan = m.SubbandPlan(nchans, fch1, foff, tsamp, nsamp, nsubs, [p], in_dtype="u8",
+                             out_dtype="i32")
+        s1 = plan.stage_info(0)
+        seen.add(s1.time_tile if s1.out_u16 else 0)
+        nch, stride = plan.input_shape()
+        x = np.random.default_rng(int(sub_dmstep)).integers(0, 256, (nch, stride), dtype=np.uint8)
+        got = _run(plan, x, torch)
+        S1, S2 = plan.stage_tables()
+        n1 = nsamp + int(S2.max())
+        _, want = orc.subband_dedisperse(x.astype(np.float32), S1, S2, nsubs, nsamp, n1,
+                                         p["calldms"])
+        assert np.array_equal(got.astype(np.float32), want), sub_dmstep
+    assert {1024, 768, 512} <= seen, seen

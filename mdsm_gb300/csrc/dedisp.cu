@@ -256,7 +256,10 @@ using CfgU8w16 = PackedCfg<1, 16, 2>;         // 32-trial blocks, for trial coun
 // tiles where the wider staging does not fit in shared memory.
 template <int NW, int PT>
 using CfgU8to16T = PackedCfg<1, NW, 2, true, PT>;
-using CfgU16 = PackedCfg<2, 16, 1>;
+// uint16 samples (no flush registers either): 768- or 512-sample tiles as the staging fits
+// shared memory (1024-sample rows of uint16 never fit with their two phase copies).
+template <int PT>
+using CfgU16T = PackedCfg<2, 16, 1, false, PT>;
 
 // Work items of the packed kernels are (beam, DM block, time tile, group) tiles; a CTA runs a
 // stream of them.  The producer warp stages the stream's chunks (16 channels of one item) into
@@ -436,6 +439,10 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
     uint32_t A[DPW][PRW];        // raw words summed mod 2^32 (<= 256 channels)
     uint32_t O[DPW][PRW];        // odd lanes summed (<= 256 channels)
     int32_t f[DPW][PRW][SPW];    // int32 sums
+    // The lane sums are final (no int32 flush) for uint16 output (an item has at most 257
+    // channels, so the 16-bit lanes do not carry) and for uint16 samples (E and O are then
+    // 32-bit sums, exact while nchans * 65535 < 2^31, which the host checks).
+    constexpr bool kDirect = Cfg::U16OUT || SW == 2;
 
     unsigned gk = 0;  // chunk sequence number
     bool aborted = false;
@@ -487,7 +494,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
 #pragma unroll
                 for (int r = 0; r < PRW; ++r) {
                     A[j][r] = O[j][r] = 0u;
-                    if constexpr (!Cfg::U16OUT)
+                    if constexpr (!kDirect)
 #pragma unroll
                         for (int e = 0; e < SPW; ++e) f[j][r][e] = 0;
                 }
@@ -551,8 +558,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 }
         }
         const bool last = (m.w & kChunkLast) != 0;
-        // (uint16 output: an item has at most 257 channels, so its 16-bit lane sums are final)
-        if (!Cfg::U16OUT && (((m.y + 1) & 15) == 0 || last)) {
+        if (!kDirect && (((m.y + 1) & 15) == 0 || last)) {
             // A = E + 2^(8 SW) O (mod 2^32): E and O hold the lane sums exactly
 #pragma unroll
             for (int j = 0; j < DPW; ++j)
@@ -564,9 +570,6 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                         f[j][r][2] += (int32_t)(E >> 16);
                         f[j][r][1] += (int32_t)(O[j][r] & 0xFFFFu);
                         f[j][r][3] += (int32_t)(O[j][r] >> 16);
-                    } else {
-                        f[j][r][0] += (int32_t)E;
-                        f[j][r][1] += (int32_t)O[j][r];
                     }
                     A[j][r] = O[j][r] = 0u;
                 }
@@ -605,24 +608,30 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                     }
                     continue;
                 }
+                int32_t v[SPW];
+                if constexpr (SW == 2) {
+                    v[0] = (int32_t)(A[j][r] - (O[j][r] << 16));
+                    v[SPW - 1] = (int32_t)O[j][r];
+                } else {
+#pragma unroll
+                    for (int e = 0; e < SPW; ++e) v[e] = f[j][r][e];
+                }
                 if (whole && a.out_i32) {
                     if constexpr (SPW == 4)
-                        *reinterpret_cast<int4 *>(orow + t * 4) =
-                            make_int4(f[j][r][0], f[j][r][1], f[j][r][2], f[j][r][3]);
+                        *reinterpret_cast<int4 *>(orow + t * 4) = make_int4(v[0], v[1], v[2], v[3]);
                     else
-                        *reinterpret_cast<int2 *>(orow + t * 4) = make_int2(f[j][r][0], f[j][r][1]);
+                        *reinterpret_cast<int2 *>(orow + t * 4) = make_int2(v[0], v[SPW - 1]);
                 } else if (whole) {
                     if constexpr (SPW == 4)
                         *reinterpret_cast<float4 *>(orow + t * 4) =
-                            make_float4((float)f[j][r][0], (float)f[j][r][1], (float)f[j][r][2],
-                                        (float)f[j][r][3]);
+                            make_float4((float)v[0], (float)v[1], (float)v[2], (float)v[3]);
                     else
                         *reinterpret_cast<float2 *>(orow + t * 4) =
-                            make_float2((float)f[j][r][0], (float)f[j][r][1]);
+                            make_float2((float)v[0], (float)v[SPW - 1]);
                 } else {
 #pragma unroll
                     for (int e = 0; e < SPW; ++e)
-                        if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), f[j][r][e], a.out_i32);
+                        if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), v[e], a.out_i32);
                 }
             }
         }
@@ -847,7 +856,7 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
         }
         if (g.in_dtype == MDSM_U16 && !g.out_u16 &&
             (long long)g.nchans * 65535 <= 0x7fffffffLL &&
-            packed_tables<CfgU16>(g, S, 3))
+            (packed_tables<CfgU16T<768>>(g, S, 3) || packed_tables<CfgU16T<512>>(g, S, 3)))
             return MDSM_OK;
     }
     g.out_u16 = 0;  // only the uint8 packed kernel writes uint16 sums
@@ -935,8 +944,9 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
                            : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<16, 512>>);
         threads = CfgU8w16::THREADS;
     } else if (g.kernel == 3) {
-        fn = reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16>);
-        threads = CfgU16::THREADS;
+        fn = g.T == 768 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16T<768>>)
+                        : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16T<512>>);
+        threads = CfgU16T<512>::THREADS;
     } else {
         persistent = false;
     }

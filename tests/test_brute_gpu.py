@@ -219,3 +219,27 @@ def test_packed_u8_float_output(lib, orc, cuda):
     got = _run(plan, x, torch)
     assert got.dtype == np.float32
     assert np.array_equal(got, orc.dedisperse(x, plan.shift_table(), 1500).astype(np.float32))
+
+
+def test_packed_u16_tile_widths(lib, orc, cuda):
+    """The packed 16-bit kernel takes 768- or 512-sample tiles as its staging fits shared memory
+    (larger DM steps widen the staged rows); each width exact against the oracle, with
+    all-65535 rows included."""
+    import mdsm_gb300 as m
+    torch = cuda
+    nchans, nsamp = 512, 2500
+    seen = set()
+    for dmstep in (0.25, 0.5, 1.0, 1.5, 4.0):
+        plan = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, [(0.0, dmstep, 40)],
+                           in_dtype="u16", out_dtype="i32")
+        st = plan.stage_info(0)
+        if st.kernel != 3:
+            continue
+        seen.add(st.time_tile)
+        nch, stride = plan.input_shape()
+        x = np.random.default_rng(int(dmstep * 10)).integers(0, 65536, (nch, stride),
+                                                              dtype=np.uint16)
+        x[::7] = 65535
+        got = _run(plan, x, torch)
+        assert np.array_equal(got, orc.dedisperse(x, plan.shift_table(), nsamp)), dmstep
+    assert {768, 512} <= seen, seen

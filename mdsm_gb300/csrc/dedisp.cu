@@ -338,6 +338,9 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
     constexpr int DB = Cfg::DB, DBS = Cfg::DBS;
     const int nwp = ps >> 2;  // words per phase copy
     const int nq = nwp >> 2;  // 16-byte quads per phase copy
+    // ceil(2^20 / nq): (q * nq_inv) >> 20 == q / nq for q < 16 nq, nq < 256 (the host keeps
+    // rows below 4096 bytes)
+    const unsigned nq_inv = ((1u << 20) + (unsigned)nq - 1) / (unsigned)nq;
     uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
     int4 *meta = reinterpret_cast<int4 *>(smem + 64);  // kPNR entries
     unsigned char *raw = smem + 128;
@@ -453,16 +456,19 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         const bool ok = mbar_wait_bounded(&bars[s], par, err, ERR_WAIT_TIMEOUT);
         const int4 m = ok ? meta[s] : make_int4(-1, 0, 0, 0);
         if (ok) {
-            // Expand staged row `warp` into its phase copies (16-byte loads and stores).
-            // P[pb] was last read for chunk gk-2, before the barrier of chunk gk-1.  All 16
-            // rows are expanded whatever the chunk holds (rows past its channels, or the whole
-            // stage at the end of the stream, hold earlier data nobody reads), so the
-            // expansion does not wait for the chunk's entry.  Warps past the 16 rows idle here.
-            if (warp < kPCC) {
+            // Expand the staged rows into their phase copies (16-byte loads and stores), the
+            // 16 rows' quads spread over all compute threads.  P[pb] was last read for chunk
+            // gk-2, before the barrier of chunk gk-1.  All 16 rows are expanded whatever the
+            // chunk holds (rows past its channels, or the whole stage at the end of the
+            // stream, hold earlier data nobody reads), so the expansion does not wait for the
+            // chunk's entry.
+            for (int q = tid; q < kPCC * nq; q += NW * 32) {
+                const int row = (int)(((unsigned)q * nq_inv) >> 20);  // q / nq
+                const int i = q - row * nq;
                 const uint32_t *W =
-                    reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + warp) * rawcap);
-                uint32_t *Pr = P + ((size_t)pb * kPCC + warp) * SPW * nwp;
-                for (int i = lane; i < nq; i += 32) {
+                    reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + row) * rawcap);
+                uint32_t *Pr = P + ((size_t)pb * kPCC + row) * SPW * nwp;
+                {
                     const uint4 w = reinterpret_cast<const uint4 *>(W)[i];
                     const uint32_t w4 = W[4 * i + 4];
                     reinterpret_cast<uint4 *>(Pr)[i] = w;
@@ -795,7 +801,7 @@ bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
     const int rawcap =
         (int)(((long long)(Cfg::PT + maxspan) * Cfg::SW + 32 + 15) / 16 * 16) + 16;
     const int ps = rawcap - 16;  // nwp = ps/4 words; the expansion reads word nwp too
-    if (packed_smem<Cfg>(rawcap, ps) > 220 * 1024) return false;
+    if (packed_smem<Cfg>(rawcap, ps) > 220 * 1024 || ps >= 4096) return false;
     g.max_span = maxspan;
     g.rowcap = rawcap;
     g.ps = ps;

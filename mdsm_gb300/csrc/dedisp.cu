@@ -521,8 +521,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         // Two channels per step: A += wa + wz and O += odd(wa) + odd(wz) are one 3-input
         // integer add each.
         auto pair = [&](int c) {
-            const unsigned char *pa = pbase + (size_t)c * SPW * ps;
-            const unsigned char *pz = pa + SPW * ps;
+            const unsigned char *pa = pbase, *pz = pbase;  // the offsets select the rows
             int oa[DPW], oz[DPW];
             offs(c, oa);
             offs(c + 1, oz);
@@ -551,7 +550,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             for (; ci + 1 < nc; ci += 2) pair(ci);
         }
         if (ci < nc) {  // odd channel count: the last channel alone
-            const unsigned char *pa = pbase + (size_t)ci * SPW * ps;
+            const unsigned char *pa = pbase;
             int oa[DPW];
             offs(ci, oa);
 #pragma unroll
@@ -784,8 +783,9 @@ size_t packed_smem(int rawcap, int ps)
            (size_t)2 * kPCC * Cfg::DBS * 4 + (size_t)2 * kPCC * Cfg::SPW * ps;
 }
 
-// Packed tables for configuration Cfg: offsets of (c, d)'s first word inside the channel's
-// phase-expanded row (bytes), stored DBS per channel (the padding stays 0).  False if the
+// Packed tables for configuration Cfg: offsets (bytes) of (c, d)'s first word from the start
+// of the chunk's phase-expanded rows (row c % 16, its phase copy, the word), stored DBS per
+// channel (the padding stays 0).  False if the
 // staging does not fit in shared memory.
 template <class Cfg>
 bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
@@ -809,9 +809,10 @@ bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
     std::vector<int32_t> off(g.sminspan.size() / 2 * Cfg::DBS, 0);
     for (size_t o = 0; o < g.sminspan.size() / 2; ++o) {
         const int lo = g.sminspan[o * 2] & lomask;
+        const int row = (int)(o % (size_t)g.nchans) % kPCC;  // the channel's row in its chunk
         for (int j = 0; j < g.Db; ++j) {
             const int e = lo + g.rel[o * g.Db + j];  // samples from the staged row's start
-            off[o * Cfg::DBS + j] = (e % Cfg::SPW) * ps + (e / Cfg::SPW) * 4;
+            off[o * Cfg::DBS + j] = (row * Cfg::SPW + e % Cfg::SPW) * ps + (e / Cfg::SPW) * 4;
         }
     }
     g.rel.swap(off);

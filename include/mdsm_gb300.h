@@ -402,6 +402,9 @@ int mdsm_start_processing(unsigned int data_read);
 void mdsm_tearDownMDSM(void);
 /* Candidates found for the block returned by the last next_chunk (detector output). */
 long long mdsm_compat_candidates(mdsm_candidate *out, long long cap);
+/* Blocks since initialiseMDSM whose float input was all integers 0..255 and so ran on the
+ * 8-bit kernels (same output bit for bit: every partial sum is an integer below 2^24). */
+long long mdsm_compat_blocks_8bit(void);
 void mdsm_free_survey(SURVEY *survey);
 
 #ifdef __cplusplus

@@ -173,6 +173,7 @@ SIGNATURES = {
     "mdsm_start_processing": (_i, [ctypes.c_uint]),
     "mdsm_tearDownMDSM": (None, []),
     "mdsm_compat_candidates": (_ll, [ctypes.POINTER(Candidate), _ll]),
+    "mdsm_compat_blocks_8bit": (_ll, []),
     "mdsm_free_survey": (None, [ctypes.POINTER(SURVEY)]),
 }
 

@@ -64,6 +64,11 @@ def tearDownMDSM():
     load().mdsm_tearDownMDSM()
 
 
+def blocks_8bit():
+    """Blocks that ran on the 8-bit kernels (their float input was all integers 0..255)."""
+    return load().mdsm_compat_blocks_8bit()
+
+
 def candidates(cap=1 << 16):
     buf = (Candidate * cap)()
     n = load().mdsm_compat_candidates(buf, cap)

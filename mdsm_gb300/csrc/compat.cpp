@@ -179,6 +179,15 @@ struct Instance {
     std::vector<mdsm_candidate> cands;  // candidates of the last processed block
     FILE *fp = nullptr;
     long long written = 0;
+    // 8-bit path: a uint8 plan of the same geometry, run when a block's floats are all
+    // integers 0..255 (then every partial sum is an integer below 2^24, exact in float in any
+    // order, so the packed kernels give the float kernels' output bit for bit)
+    mdsm_plan *plan8 = nullptr;
+    void *d_in8 = nullptr;
+    size_t d_in8_bytes = 0;
+    long long stride8 = 0;
+    unsigned *d_flag = nullptr, *h_flag = nullptr;
+    long long blocks8 = 0;
 };
 
 Instance g;
@@ -234,6 +243,10 @@ void release()
 {
     if (g.fp) fclose(g.fp);
     if (g.plan) mdsm_plan_destroy(g.plan);
+    if (g.plan8) mdsm_plan_destroy(g.plan8);
+    if (g.d_in8) cudaFree(g.d_in8);
+    if (g.d_flag) cudaFree(g.d_flag);
+    if (g.h_flag) cudaFreeHost(g.h_flag);
     if (g.h_in) cudaFreeHost(g.h_in);
     for (int i = 0; i < 2; ++i) {
         if (g.h_out[i]) cudaFreeHost(g.h_out[i]);
@@ -242,6 +255,74 @@ void release()
     if (g.d_out) cudaFree(g.d_out);
     if (g.st) cudaStreamDestroy(g.st);
     g = Instance();
+}
+
+// The 8-bit path where it gives the float plan's output exactly: float sums of integers
+// 0..255 over at most 65793 channels stay below 2^24 (exact), and passes without
+// downsampling (a downsampled pass averages samples into fractions).  Set-up failures leave
+// the float path alone.
+void setup_8bit(const SURVEY *s)
+{
+    const Plan &p = g.plan->p;
+    if ((long long)p.nchans * 255 >= (1LL << 24)) return;
+    mdsm_status st;
+    if (s->useBruteForce) {
+        mdsm_segment seg{s->lowdm, s->dmstep, (int)s->tdms};
+        mdsm_brute_desc d;
+        memset(&d, 0, sizeof d);
+        d.nchans = (int)s->nchans;
+        d.fch1 = s->fch1;
+        d.foff = s->foff;
+        d.tsamp = s->tsamp;
+        d.nsamp = (int)s->nsamp;
+        d.segs = &seg;
+        d.nsegs = 1;
+        d.shift_mode = s->useL1Cache ? MDSM_SHIFT_L1 : MDSM_SHIFT_OPT;
+        d.in_dtype = MDSM_U8;
+        d.out_dtype = MDSM_OUT_F32;
+        st = mdsm_brute_plan_create(&d, &g.plan8);
+    } else {
+        for (unsigned i = 0; i < s->num_passes; ++i)
+            if (s->pass_parameters[i].binsize > 1) return;
+        mdsm_subband_desc d;
+        memset(&d, 0, sizeof d);
+        d.nchans = (int)s->nchans;
+        d.fch1 = s->fch1;
+        d.foff = s->foff;
+        d.tsamp = s->tsamp;
+        d.nsamp = (int)s->nsamp;
+        d.nsubs = (int)s->nsubs;
+        d.passes = s->pass_parameters;
+        d.npasses = (int)s->num_passes;
+        d.use_fma = 1;
+        d.in_dtype = MDSM_U8;
+        d.out_dtype = MDSM_OUT_F32;
+        st = mdsm_subband_plan_create(&d, &g.plan8);
+    }
+    if (st != MDSM_OK) {
+        g.plan8 = nullptr;
+        return;
+    }
+    const Plan &q = g.plan8->p;
+    long long need = 0;
+    const bool same = q.nchans == p.nchans && q.ndms == p.ndms && q.nsamp == p.nsamp &&
+                      q.maxshift == p.maxshift && q.S == p.S && q.S1 == p.S1 && q.S2 == p.S2;
+    if (!same || plan_in_requirements(q, q.in_stride, &need) != MDSM_OK ||
+        cudaMalloc(&g.d_in8, (size_t)need + 256) != cudaSuccess ||
+        cudaMalloc((void **)&g.d_flag, sizeof(unsigned)) != cudaSuccess ||
+        cudaHostAlloc((void **)&g.h_flag, sizeof(unsigned), 0) != cudaSuccess) {
+        if (g.plan8) mdsm_plan_destroy(g.plan8);
+        if (g.d_in8) cudaFree(g.d_in8);
+        if (g.d_flag) cudaFree(g.d_flag);
+        if (g.h_flag) cudaFreeHost(g.h_flag);
+        g.plan8 = nullptr;
+        g.d_in8 = nullptr;
+        g.d_flag = g.h_flag = nullptr;
+        return;
+    }
+    cudaMemset(g.d_in8, 0, (size_t)need + 256);
+    g.d_in8_bytes = (size_t)need + 256;
+    g.stride8 = q.in_stride;
 }
 
 // One block through the device: tail carry, H2D of the new samples, dedispersion, detection,
@@ -265,9 +346,26 @@ mdsm_status process_block(unsigned data_read)
                                         g.h_in + ms, g.hstride * 4, (size_t)ns * 4, p.nchans,
                                         cudaMemcpyHostToDevice, g.st));
     }
+    bool eight = false;
+    if (g.plan8) {
+        // all of the block's input (tail and new samples) integers 0..255?
+        MDSM_CUDA_TRY(cudaMemsetAsync(g.d_flag, 0, sizeof(unsigned), g.st));
+        MDSM_TRY(pack_u8_rows(static_cast<const float *>(g.d_in[cur]), g.stride, p.nchans, ns + ms,
+                              static_cast<uint8_t *>(g.d_in8), g.stride8, g.d_flag, g.st));
+        MDSM_CUDA_TRY(cudaMemcpyAsync(g.h_flag, g.d_flag, sizeof(unsigned),
+                                      cudaMemcpyDeviceToHost, g.st));
+    }
     // The host input buffer may be refilled once the copies above have run.
     MDSM_CUDA_TRY(cudaStreamSynchronize(g.st));
-    MDSM_TRY(plan_run_device(p, g.d_in[cur], g.stride, g.d_in_bytes, g.d_out, ns, g.st));
+    eight = g.plan8 && *g.h_flag == 0;
+    if (eight) {
+        MDSM_TRY(plan_run_device(g.plan8->p, g.d_in8, g.stride8, g.d_in8_bytes, g.d_out, ns,
+                                 g.st));
+        MDSM_TRY(check_err_word(g.plan8->p.d_err, g.st));
+        g.blocks8++;
+    } else {
+        MDSM_TRY(plan_run_device(p, g.d_in[cur], g.stride, g.d_in_bytes, g.d_out, ns, g.st));
+    }
     long long nc = 0;
     std::vector<mdsm_candidate> c(1 << 16);
     // the reference's detectors (dedispersion_output.cpp:56-213): with the caller's noise
@@ -487,6 +585,7 @@ float *mdsm_initialiseMDSM(SURVEY *s)
     cudaMemset(g.d_in[1], 0, (size_t)need + 256);
     memset(g.h_in, 0, (size_t)g.hstride * p.nchans * 4);
     g.d_in_bytes = (size_t)need + 256;
+    setup_8bit(s);
     g.live = true;
     return g.h_in;
 }
@@ -544,5 +643,7 @@ long long mdsm_compat_candidates(mdsm_candidate *out, long long cap)
     for (long long i = 0; i < n && i < cap; ++i) out[i] = g.cands[i];
     return n;
 }
+
+long long mdsm_compat_blocks_8bit(void) { return g.blocks8; }
 
 }  // extern "C"

@@ -156,6 +156,12 @@ mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size
                             void *d_out, long long out_stride, cudaStream_t st);
 mdsm_status check_err_word(unsigned *d_err, cudaStream_t st);
 
+// Float rows [nrows][in_stride] -> uint8 rows [nrows][out_stride] over columns [0, ncols):
+// every value that is bit for bit an integer 0..255 is stored as that integer; any other
+// value (fractions, negatives, -0, NaN, > 255) sets *flag.  Asynchronous on st.
+mdsm_status pack_u8_rows(const float *in, long long in_stride, int nrows, long long ncols,
+                         uint8_t *out, long long out_stride, unsigned *flag, cudaStream_t st);
+
 // host shift formulas (the reference's arithmetic, evaluated on the host)
 float dmdelay_ref(float f1, float f2);
 void dmshifts_ref(int nchans, float fch1, float foff, float *out);

@@ -18,6 +18,56 @@
 
 namespace mdsm {
 
+// Float rows to uint8 rows where every value is an integer 0..255 (the float blocks of the
+// stage interface usually hold 8-bit samples): four columns per thread, float4 loads and
+// 4-byte stores where the row allows.
+__global__ void __launch_bounds__(256)
+    k_pack_u8_rows(const float *__restrict__ in, long long in_stride, int nrows, long long ncols,
+                   uint8_t *__restrict__ out, long long out_stride, unsigned *__restrict__ flag)
+{
+    const int r = blockIdx.y;
+    const long long t = ((long long)blockIdx.x * blockDim.x + threadIdx.x) * 4;
+    if (r >= nrows || t >= ncols) return;
+    const float *row = in + (size_t)r * in_stride;
+    float v[4];
+    if (t + 3 < ncols) {
+        const float4 q = *reinterpret_cast<const float4 *>(row + t);
+        v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+    } else {
+        for (int e = 0; e < 4; ++e) v[e] = t + e < ncols ? row[t + e] : 0.0f;
+    }
+    uint32_t packed = 0;
+    bool bad = false;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        const unsigned u = __float2uint_rz(v[e]);
+        // bit-exact round trip: rejects fractions, -0, NaN and values past 255
+        bad |= u > 255u || __float_as_uint(v[e]) != __float_as_uint(__uint2float_rn(u));
+        packed |= (u & 0xFFu) << (8 * e);
+    }
+    if (bad) atomicOr(flag, 1u);
+    uint8_t *orow = out + (size_t)r * out_stride;
+    if (t + 3 < ncols) {
+        *reinterpret_cast<uint32_t *>(orow + t) = packed;
+    } else {
+        for (int e = 0; e < 4 && t + e < ncols; ++e) orow[t + e] = (uint8_t)(packed >> (8 * e));
+    }
+}
+
+mdsm_status pack_u8_rows(const float *in, long long in_stride, int nrows, long long ncols,
+                         uint8_t *out, long long out_stride, unsigned *flag, cudaStream_t st)
+{
+    if (nrows <= 0 || ncols <= 0) return MDSM_OK;
+    if (((uintptr_t)in & 15) || (in_stride & 3) || ((uintptr_t)out & 3) || (out_stride & 3))
+        return fail(MDSM_EINVAL, "pack_u8_rows: rows must be 16-byte (float) / 4-byte aligned");
+    const long long quads = (ncols + 3) / 4;
+    if (nrows > 65535) return fail(MDSM_EINVAL, "pack_u8_rows: too many rows");
+    dim3 grid((unsigned)((quads + 255) / 256), (unsigned)nrows);
+    k_pack_u8_rows<<<grid, 256, 0, st>>>(in, in_stride, nrows, ncols, out, out_stride, flag);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return MDSM_OK;
+}
+
 // One CTA moves a tile of 32 spectra x 32 channels: loads walk channels (consecutive in the
 // raw stream), stores walk time (consecutive in the output rows).
 template <int NBITS, typename TOut>

@@ -105,7 +105,7 @@ def test_candidate_file_rotation(lib, orc, cuda, tmp_path):
             assert t_start + blocks[0] * block_s <= t < t_start + (blocks[-1] + 1) * block_s
 
 
-def _run_blocks(compat, survey, x, nblocks, ts0, tsamp, stats=None):
+def _run_blocks(compat, survey, x, nblocks, ts0, tsamp, stats=None, before_teardown=None):
     s = survey.contents
     buf = compat.initialiseMDSM(survey)
     nsamp, ms = s.nsamp, s.maxshift
@@ -125,6 +125,8 @@ def _run_blocks(compat, survey, x, nblocks, ts0, tsamp, stats=None):
             outs.append(compat.output_view(ptr, survey).copy())
         if not compat.start_processing(data_read):
             break
+    if before_teardown:
+        before_teardown()
     compat.tearDownMDSM()
     return outs
 
@@ -222,3 +224,60 @@ def test_subband_stage_interface_detects(lib, orc, cuda, tmp_path):
     assert len(got) == len(want_sorted) > 0
     for a, b in zip(got, want_sorted):
         assert abs(a[0] - b[0]) <= 1e-6 and abs(a[1] - b[1]) <= 1e-5 and abs(a[2] - b[2]) <= 1e-5
+
+
+def test_integer_blocks_take_8bit_kernels(lib, orc, cuda, tmp_path):
+    """Float blocks whose samples are all integers 0..255 (8-bit data handed in as floats, as
+    the reference's file reader does) run on the 8-bit kernels with the float path's output
+    bit for bit; a block holding one fraction runs on the float kernels."""
+    from mdsm_gb300 import compat
+    obs = tmp_path / "obs.xml"
+    obs.write_text(OBS.format(dir=str(tmp_path)))
+    survey = compat.processSurveyParameters(obs)
+    nsamp, tsamp, nblocks = 4096, 0.000064, 3
+    S = orc.shift_table(128, 1500.0, -0.78125, tsamp, [(0.0, 0.5, 96)], mode="l1")
+    ms = int(S.max())
+    x = np.random.default_rng(5).integers(0, 256, (128, nblocks * nsamp + ms)).astype(np.float32)
+    x[:3, :50] = 255.0
+    x[7, nsamp + ms + 10] = 3.5  # among block 1's new samples, not in block 2's tail
+    seen = {}
+    outs = _run_blocks(compat, survey, x, nblocks, 0.0, tsamp,
+                       before_teardown=lambda: seen.setdefault("n", compat.blocks_8bit()))
+    assert seen["n"] == nblocks - 1
+    assert len(outs) == nblocks
+    for k, y in enumerate(outs):
+        assert np.array_equal(y, orc.dedisperse(x[:, k * nsamp:], S, nsamp)), k
+
+
+OBS_SUB1 = OBS_SUB.replace("""        <pass><lowDm>32.0</lowDm><highDm>96.0</highDm><deltaDm>2.0</deltaDm>
+              <downsample>2</downsample><subDm>16.0</subDm><numDms>32</numDms>
+              <dmsPerCall>8</dmsPerCall><ncalls>4</ncalls></pass>
+""", "")
+
+
+def test_integer_blocks_take_8bit_kernels_subband(lib, orc, cuda, tmp_path):
+    """The same for a subband plan without downsampled passes: the 8-bit stages (uint16
+    subband series) give the float stages' output bit for bit."""
+    import mdsm_gb300 as m
+    from mdsm_gb300 import compat
+    assert OBS_SUB1 != OBS_SUB
+    obs = tmp_path / "obs.xml"
+    obs.write_text(OBS_SUB1.format(dir=str(tmp_path)))
+    survey = compat.processSurveyParameters(obs)
+    nsamp, tsamp, nblocks = 4096, 0.000064, 2
+    pas = dict(lowdm=0.0, highdm=32.0, dmstep=0.5, sub_dmstep=4.0, ncalls=8, calldms=8)
+    plan = m.SubbandPlan(256, 1500.0, -1.171875, tsamp, nsamp, 16, [pas], in_dtype="f32",
+                         out_dtype="f32")
+    S1, S2 = plan.stage_tables()
+    nch, stride = plan.input_shape()
+    x = np.random.default_rng(6).integers(0, 256, (256, nblocks * nsamp + stride)).astype(
+        np.float32)
+    seen = {}
+    outs = _run_blocks(compat, survey, x, nblocks, 0.0, tsamp,
+                       before_teardown=lambda: seen.setdefault("n", compat.blocks_8bit()))
+    assert seen["n"] == nblocks and len(outs) == nblocks
+    n1 = nsamp + int(S2.max())
+    for k, y in enumerate(outs):
+        _, want = orc.subband_dedisperse(x[:, k * nsamp: k * nsamp + stride], S1, S2, 16, nsamp,
+                                         n1, pas["calldms"])
+        assert np.array_equal(y, want), k

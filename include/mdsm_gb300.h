@@ -400,7 +400,7 @@ float *mdsm_next_chunk(unsigned int data_read, unsigned *samples, double timesta
                        double blockRate, float *mean, float *rms);
 int mdsm_start_processing(unsigned int data_read);
 void mdsm_tearDownMDSM(void);
-/* Candidates found for the block returned by the last next_chunk (detector output). */
+/* Candidates of the last block handed to start_processing (waits for its processing). */
 long long mdsm_compat_candidates(mdsm_candidate *out, long long cap);
 /* Blocks since initialiseMDSM whose float input was all integers 0..255 and so ran on the
  * 8-bit kernels (same output bit for bit: every partial sum is an integer below 2^24). */

@@ -17,9 +17,11 @@
 //    and the second start_processing(0) returns 0;
 //  * candidates of every block are written as text "time, dm, snr" to the reference's output
 //    files (dedispersion_output.cpp:194-196,233-302).
-// GB300 design: no worker threads and barriers.  The overlap tail stays on the device and is
-// moved there with one device-to-device copy (no host memcpy per channel), only the new
-// samples cross the host link, the input/output buffers are pinned, and detection runs on the
+// GB300 design: one worker thread runs a block's dedispersion, detection and copy-out while
+// the caller reads the next block (the reference's dedispersion and output threads), joined
+// by the next call instead of barriers.  The overlap tail stays on the device and is moved
+// there with one device-to-device copy (no host memcpy per channel), only the new samples
+// cross the host link, the input/output buffers are pinned, and detection runs on the
 // device.  Errors set mdsm_last_error() and return NULL / 0 instead of exit(0).
 #include <cctype>
 #include <cmath>
@@ -30,6 +32,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "internal.h"
@@ -188,6 +191,21 @@ struct Instance {
     long long stride8 = 0;
     unsigned *d_flag = nullptr, *h_flag = nullptr;
     long long blocks8 = 0;
+    // The block after its copies runs on a worker thread, as the reference's dedispersion and
+    // output threads do, so the caller reads the next block meanwhile; next_chunk,
+    // start_processing and tearDown wait for it.
+    std::thread worker;
+    mdsm_status wstatus = MDSM_OK;
+    std::string werror;
+};
+
+// One block handed to the worker: what next_chunk gave for it, captured when it is submitted.
+struct Job {
+    unsigned data_read = 0;
+    int cur = 0, device = 0;
+    bool eight = false;
+    double ts = 0, rate = 0;
+    std::vector<float> mean, rms;  // caller noise statistics (empty: the detector's own)
 };
 
 Instance g;
@@ -197,7 +215,7 @@ Instance g;
 // time counts samples of the pass's downsample factor, held in the candidate's width), or
 // with caller statistics "time, DM, snr, mean, rms" (process_brute, :205-208).
 void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double ts, double rate,
-                      int spc)
+                      int spc, const float *cmean, const float *crms)
 {
     SURVEY *s = g.survey;
     if (!g.fp || (!s->single_file_mode && g.written == 0)) {
@@ -219,12 +237,12 @@ void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double
     if (!g.fp) return;
     std::vector<float> dmv(g.plan->p.ndms);
     mdsm_plan_dm_values(g.plan, dmv.data());
-    const bool with_stats = g.plan->p.kind == 1 && g.cmean;
+    const bool with_stats = g.plan->p.kind == 1 && cmean;
     for (long long i = 0; i < nc && i < (long long)c.size(); ++i) {
         const double t = ts + (double)c[i].sample * rate * (double)std::max(1, c[i].width);
         if (with_stats)
             fprintf(g.fp, "%lf, %f, %f, %f, %f  \n", t, dmv[c[i].dm_idx], c[i].snr,
-                    g.cmean[c[i].sample / spc], g.crms[c[i].sample / spc]);
+                    cmean[c[i].sample / spc], crms[c[i].sample / spc]);
         else
             fprintf(g.fp, "%lf, %f, %f\n", t, dmv[c[i].dm_idx], c[i].snr);
     }
@@ -241,6 +259,7 @@ void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double
 
 void release()
 {
+    if (g.worker.joinable()) g.worker.join();
     if (g.fp) fclose(g.fp);
     if (g.plan) mdsm_plan_destroy(g.plan);
     if (g.plan8) mdsm_plan_destroy(g.plan8);
@@ -325,13 +344,24 @@ void setup_8bit(const SURVEY *s)
     g.stride8 = q.in_stride;
 }
 
-// One block through the device: tail carry, H2D of the new samples, dedispersion, detection,
-// D2H of the series.
-mdsm_status process_block(unsigned data_read)
+// Wait for the block on the worker; its failure becomes this thread's error.
+mdsm_status join_worker()
+{
+    if (g.worker.joinable()) g.worker.join();
+    const mdsm_status st = g.wstatus;
+    if (st != MDSM_OK) set_error(g.werror);
+    g.wstatus = MDSM_OK;
+    return st;
+}
+
+// A block's first half, on the caller's thread: tail carry and H2D of the new samples (the
+// caller may refill its buffer once this returns), and the 8-bit check.
+mdsm_status stage_block(Job &j)
 {
     Plan &p = g.plan->p;
     const long long ms = p.maxshift, ns = p.nsamp;
     const int cur = (int)(g.blocks & 1), prv = cur ^ 1;
+    j.cur = cur;
     if (g.blocks == 0) {
         MDSM_CUDA_TRY(cudaMemcpy2DAsync(g.d_in[cur], g.stride * 4, g.h_in, g.hstride * 4,
                                         (size_t)(ns + ms) * 4, p.nchans, cudaMemcpyHostToDevice,
@@ -346,7 +376,6 @@ mdsm_status process_block(unsigned data_read)
                                         g.h_in + ms, g.hstride * 4, (size_t)ns * 4, p.nchans,
                                         cudaMemcpyHostToDevice, g.st));
     }
-    bool eight = false;
     if (g.plan8) {
         // all of the block's input (tail and new samples) integers 0..255?
         MDSM_CUDA_TRY(cudaMemsetAsync(g.d_flag, 0, sizeof(unsigned), g.st));
@@ -355,16 +384,26 @@ mdsm_status process_block(unsigned data_read)
         MDSM_CUDA_TRY(cudaMemcpyAsync(g.h_flag, g.d_flag, sizeof(unsigned),
                                       cudaMemcpyDeviceToHost, g.st));
     }
-    // The host input buffer may be refilled once the copies above have run.
     MDSM_CUDA_TRY(cudaStreamSynchronize(g.st));
-    eight = g.plan8 && *g.h_flag == 0;
-    if (eight) {
+    j.eight = g.plan8 && *g.h_flag == 0;
+    MDSM_CUDA_TRY(cudaGetDevice(&j.device));
+    return MDSM_OK;
+}
+
+// A block's second half, on the worker: dedispersion, detection, D2H of the series and the
+// candidate lines.
+mdsm_status finish_block(const Job &j)
+{
+    MDSM_CUDA_TRY(cudaSetDevice(j.device));
+    Plan &p = g.plan->p;
+    const long long ns = p.nsamp;
+    if (j.eight) {
         MDSM_TRY(plan_run_device(g.plan8->p, g.d_in8, g.stride8, g.d_in8_bytes, g.d_out, ns,
                                  g.st));
         MDSM_TRY(check_err_word(g.plan8->p.d_err, g.st));
         g.blocks8++;
     } else {
-        MDSM_TRY(plan_run_device(p, g.d_in[cur], g.stride, g.d_in_bytes, g.d_out, ns, g.st));
+        MDSM_TRY(plan_run_device(p, g.d_in[j.cur], g.stride, g.d_in_bytes, g.d_out, ns, g.st));
     }
     long long nc = 0;
     std::vector<mdsm_candidate> c(1 << 16);
@@ -372,26 +411,52 @@ mdsm_status process_block(unsigned data_read)
     // statistics of the block when next_chunk was given them, one value per samplesPerChunk
     const int spc = g.survey->samplesPerChunk ? (int)g.survey->samplesPerChunk : (int)ns;
     const long long nchunks = (ns - 5) / spc + 1;
+    const float *cmean = j.mean.empty() ? nullptr : j.mean.data();
+    const float *crms = j.rms.empty() ? nullptr : j.rms.data();
     const float *y = static_cast<const float *>(g.d_out);
     const float thr = g.survey->detection_threshold;
-    if (p.kind == 1 && g.cmean)
+    if (p.kind == 1 && cmean)
         MDSM_TRY(ref_detect_chunked(y, p.ndms, (int)ns, g.survey->lowdm, g.survey->dmstep, thr,
-                                    g.cmean, g.crms, nchunks, spc, c.data(), (long long)c.size(),
+                                    cmean, crms, nchunks, spc, c.data(), (long long)c.size(),
                                     &nc, g.st));
     else if (p.kind == 1)
         MDSM_TRY(ref_detect(y, p.ndms, (int)ns, g.survey->lowdm, g.survey->dmstep, thr, c.data(),
                             (long long)c.size(), &nc, nullptr, nullptr, g.st));
     else
-        MDSM_TRY(ref_detect_subband(p, y, ns, thr, g.cmean, g.crms, nchunks, spc, c.data(),
+        MDSM_TRY(ref_detect_subband(p, y, ns, thr, cmean, crms, nchunks, spc, c.data(),
                                     (long long)c.size(), &nc, g.st));
-    MDSM_CUDA_TRY(cudaMemcpyAsync(g.h_out[cur], g.d_out, (size_t)p.ndms * ns * 4,
+    MDSM_CUDA_TRY(cudaMemcpyAsync(g.h_out[j.cur], g.d_out, (size_t)p.ndms * ns * 4,
                                   cudaMemcpyDeviceToHost, g.st));
     MDSM_TRY(check_err_word(p.d_err, g.st));
     c.resize((size_t)std::min<long long>(nc, (long long)c.size()));
     g.cands = c;
-    g.prev_read = data_read;
-    write_candidates(c, nc, g.ts, g.rate, spc);
+    g.prev_read = j.data_read;
+    write_candidates(c, nc, j.ts, j.rate, spc, cmean, crms);
     g.blocks++;
+    return MDSM_OK;
+}
+
+// Hand one block in: its copies here, the rest on the worker.
+mdsm_status submit_block(unsigned data_read)
+{
+    MDSM_TRY(join_worker());
+    Job j;
+    j.data_read = data_read;
+    j.ts = g.ts;
+    j.rate = g.rate;
+    if (g.cmean) {
+        // the caller's arrays hold one value per samplesPerChunk samples of this block
+        const long long ns = g.plan->p.nsamp;
+        const int spc = g.survey->samplesPerChunk ? (int)g.survey->samplesPerChunk : (int)ns;
+        const long long nchunks = (ns - 5) / spc + 1;
+        j.mean.assign(g.cmean, g.cmean + nchunks);
+        j.rms.assign(g.crms, g.crms + nchunks);
+    }
+    MDSM_TRY(stage_block(j));
+    g.worker = std::thread([j]() {
+        g.wstatus = finish_block(j);
+        if (g.wstatus != MDSM_OK) g.werror = mdsm_last_error();
+    });
     return MDSM_OK;
 }
 
@@ -598,6 +663,11 @@ float *mdsm_next_chunk(unsigned int data_read, unsigned *samples, double timesta
         set_error("next_chunk before initialiseMDSM");
         return nullptr;
     }
+    // the block handed in by the last start_processing is the one reported here
+    if (join_worker() != MDSM_OK) {
+        if (samples) *samples = 0;
+        return nullptr;
+    }
     // caller-owned noise statistics of the block being handed in (one value per
     // samplesPerChunk samples); read by the detector when the block is processed
     g.cmean = mean && rms ? mean : nullptr;
@@ -627,23 +697,29 @@ int mdsm_start_processing(unsigned int data_read)
         return 0;
     }
     if (data_read == 0) {
+        if (join_worker() != MDSM_OK) return 0;
         if (g.stopped_once) return 0;
         g.stopped_once = true;
         return (int)(g.blocks + 1);
     }
-    if (process_block(data_read) != MDSM_OK) return 0;
-    return (int)g.blocks;
+    if (submit_block(data_read) != MDSM_OK) return 0;
+    return (int)(g.blocks + 1);  // the block now in flight counted
 }
 
 void mdsm_tearDownMDSM(void) { release(); }
 
 long long mdsm_compat_candidates(mdsm_candidate *out, long long cap)
 {
+    if (join_worker() != MDSM_OK) return 0;
     const long long n = (long long)g.cands.size();
     for (long long i = 0; i < n && i < cap; ++i) out[i] = g.cands[i];
     return n;
 }
 
-long long mdsm_compat_blocks_8bit(void) { return g.blocks8; }
+long long mdsm_compat_blocks_8bit(void)
+{
+    join_worker();
+    return g.blocks8;
+}
 
 }  // extern "C"

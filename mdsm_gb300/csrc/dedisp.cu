@@ -466,14 +466,16 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 const int i = q - row * nq;
                 const uint32_t *W =
                     reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + row) * rawcap);
-                uint32_t *Pr = P + ((size_t)pb * kPCC + row) * SPW * nwp;
+                // phase-major: copy a of row r at (a * 16 + r) * nwp, so a warp whose quads
+                // cross from one row into the next stores to consecutive addresses
+                uint32_t *Pr = P + ((size_t)pb * SPW * kPCC + row) * nwp;
                 {
                     const uint4 w = reinterpret_cast<const uint4 *>(W)[i];
                     const uint32_t w4 = W[4 * i + 4];
                     reinterpret_cast<uint4 *>(Pr)[i] = w;
 #pragma unroll
                     for (int a = 1; a < SPW; ++a)
-                        reinterpret_cast<uint4 *>(Pr + a * nwp)[i] =
+                        reinterpret_cast<uint4 *>(Pr + a * kPCC * nwp)[i] =
                             make_uint4(__funnelshift_r(w.x, w.y, 8 * SW * a),
                                        __funnelshift_r(w.y, w.z, 8 * SW * a),
                                        __funnelshift_r(w.z, w.w, 8 * SW * a),
@@ -783,8 +785,8 @@ size_t packed_smem(int rawcap, int ps)
 }
 
 // Packed tables for configuration Cfg: offsets (bytes) of (c, d)'s first word from the start
-// of the chunk's phase-expanded rows (row c % 16, its phase copy, the word), stored DBS per
-// channel (the padding stays 0).  False if the
+// of the chunk's phase-expanded rows (phase copy, row c % 16, the word; the copies are stored
+// phase-major), stored DBS per channel (the padding stays 0).  False if the
 // staging does not fit in shared memory.
 template <class Cfg>
 bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
@@ -811,7 +813,7 @@ bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
         const int row = (int)(o % (size_t)g.nchans) % kPCC;  // the channel's row in its chunk
         for (int j = 0; j < g.Db; ++j) {
             const int e = lo + g.rel[o * g.Db + j];  // samples from the staged row's start
-            off[o * Cfg::DBS + j] = (row * Cfg::SPW + e % Cfg::SPW) * ps + (e / Cfg::SPW) * 4;
+            off[o * Cfg::DBS + j] = ((e % Cfg::SPW) * kPCC + row) * ps + (e / Cfg::SPW) * 4;
         }
     }
     g.rel.swap(off);

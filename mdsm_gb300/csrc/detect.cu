@@ -536,30 +536,53 @@ __global__ void __launch_bounds__(256)
     const int d = blockIdx.x;
     const int32_t *r = y + (size_t)d * n;
     long long s1 = 0;
-    unsigned long long lo = 0, hi = 0;
-    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
-        const long long v = __ldg(r + i);
+    unsigned long long lo = 0, hi = 0;  // sum of squares, 128 bits
+    auto acc = [&](long long v) {
         s1 += v;
-        const unsigned long long q = (unsigned long long)(v * v);
-        const unsigned long long nl = lo + q;
+        const unsigned long long nl = lo + (unsigned long long)(v * v);
         hi += (nl < lo);
         lo = nl;
-    }
-    __shared__ long long a1[256];
-    __shared__ unsigned long long alo[256], ahi[256];
-    a1[threadIdx.x] = s1;
-    alo[threadIdx.x] = lo;
-    ahi[threadIdx.x] = hi;
-    __syncthreads();
-    for (int o = 128; o > 0; o >>= 1) {
-        if ((int)threadIdx.x < o) {
-            a1[threadIdx.x] += a1[threadIdx.x + o];
-            const unsigned long long nl = alo[threadIdx.x] + alo[threadIdx.x + o];
-            ahi[threadIdx.x] += ahi[threadIdx.x + o] + (nl < alo[threadIdx.x]);
-            alo[threadIdx.x] = nl;
+    };
+    long long i0 = 0;
+    if ((reinterpret_cast<uintptr_t>(r) & 15) == 0) {  // 16-byte loads, 4 values each
+        const long long n4 = n >> 2;
+        const int4 *r4 = reinterpret_cast<const int4 *>(r);
+        for (long long i = threadIdx.x; i < n4; i += blockDim.x) {
+            const int4 v = __ldg(r4 + i);
+            acc(v.x);
+            acc(v.y);
+            acc(v.z);
+            acc(v.w);
         }
-        __syncthreads();
+        i0 = n4 << 2;
     }
+    for (long long i = i0 + threadIdx.x; i < n; i += blockDim.x) acc(__ldg(r + i));
+    // warp shuffles, then the 8 warps' partials through shared memory
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long s1o = __shfl_down_sync(0xffffffffu, s1, o);
+        const unsigned long long loo = __shfl_down_sync(0xffffffffu, lo, o);
+        const unsigned long long hio = __shfl_down_sync(0xffffffffu, hi, o);
+        s1 += s1o;
+        const unsigned long long nl = lo + loo;
+        hi += hio + (nl < lo);
+        lo = nl;
+    }
+    __shared__ long long a1[8];
+    __shared__ unsigned long long alo[8], ahi[8];
+    const int warp = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        a1[warp] = s1;
+        alo[warp] = lo;
+        ahi[warp] = hi;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) {
+            a1[0] += a1[w];
+            const unsigned long long nl = alo[0] + alo[w];
+            ahi[0] += ahi[w] + (nl < alo[0]);
+            alo[0] = nl;
+        }
     if (threadIdx.x == 0) {
         const double e2 = __ddiv_rn(__dadd_rn(__dmul_rn((double)ahi[0], 18446744073709551616.0),
                                               (double)alo[0]),

@@ -288,7 +288,8 @@ mdsm_status mdsm_sigproc_write_series_header(const char *path, double fch1, doub
                                              double tsamp, double tstart);
 /* Unpack nspectra time-major spectra of nchans nbits-bit samples (1/2/4 least significant
  * field first, 16-bit unsigned, 32-bit float: file_handler.cpp:193-290) on the device and
- * write them channel-major into d_out (uint8, uint16 or float32) at columns
+ * write them channel-major into d_out (uint8, uint16, float32, or int16, which reads 16-bit
+ * samples as two's-complement signed) at columns
  * [col0, col0 + nspectra) of rows of out_stride elements; invert reverses the channel order
  * (the corner turns of src/MDSM.cpp:100-125 and MdsmModule.cpp:135-151). */
 mdsm_status mdsm_unpack_device(const void *d_raw, long long nspectra, int nchans, int nbits,

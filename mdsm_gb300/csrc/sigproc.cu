@@ -13,6 +13,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <type_traits>
 
 #include "internal.h"
 
@@ -90,7 +91,10 @@ __global__ void __launch_bounds__(256)
                 v = (TOut)raw[idx];
             } else if constexpr (NBITS == 16) {
                 const uint16_t s = (uint16_t)(raw[2 * idx] | ((uint16_t)raw[2 * idx + 1] << 8));
-                v = (TOut)s;
+                if constexpr (std::is_same<TOut, int16_t>::value)
+                    v = (int16_t)((int32_t)s - ((s & 0x8000u) ? 65536 : 0));  // two's complement
+                else
+                    v = (TOut)s;
             } else if constexpr (NBITS == 32) {
                 float f;
                 memcpy(&f, raw + 4 * idx, 4);
@@ -132,12 +136,17 @@ static mdsm_status launch_unpack(const void *raw, long long nspectra, int nchans
         k_unpack_transpose<NBITS, uint16_t><<<grid, block, 0, st>>>(
             r, nspectra, nchans, invert, static_cast<uint16_t *>(out), out_stride, col0);
         break;
+    case MDSM_I16:  // 16-bit samples read as two's-complement int16 (the int16 data form)
+        if (NBITS == 32) return fail(MDSM_EINVAL, "unpack: float samples to int16 output");
+        k_unpack_transpose<NBITS, int16_t><<<grid, block, 0, st>>>(
+            r, nspectra, nchans, invert, static_cast<int16_t *>(out), out_stride, col0);
+        break;
     case MDSM_F32:
         k_unpack_transpose<NBITS, float><<<grid, block, 0, st>>>(
             r, nspectra, nchans, invert, static_cast<float *>(out), out_stride, col0);
         break;
     default:
-        return fail(MDSM_EINVAL, "unpack: output must be uint8, uint16 or float32");
+        return fail(MDSM_EINVAL, "unpack: output must be uint8, uint16, int16 or float32");
     }
     MDSM_CUDA_TRY(cudaGetLastError());
     return MDSM_OK;

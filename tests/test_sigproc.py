@@ -124,3 +124,25 @@ def test_device_unpack_corner_turn(lib, orc, cuda, nbits, invert):
     got = out.cpu().numpy()
     assert np.array_equal(got[:, col0:col0 + nspec].astype(np.float32), want)
     assert not got[:, :col0].any() and not got[:, col0 + nspec:].any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("invert", [0, 1])
+def test_device_unpack_signed_int16(lib, cuda, invert):
+    """16-bit samples unpacked to int16 read as two's-complement signed (the int16 data form),
+    little-endian as the file stores them."""
+    from mdsm_gb300 import sigproc
+    torch = cuda
+    nchans, nspec, stride, col0 = 80, 777, 900, 5
+    raw = np.random.default_rng(16).integers(0, 256, nchans * nspec * 2, dtype=np.uint8)
+    raw[:4] = [0x00, 0x80, 0xFF, 0x7F]  # -32768 and 32767
+    want = raw.view("<i2").reshape(nspec, nchans).T
+    if invert:
+        want = want[::-1]
+    out = torch.zeros((nchans, stride), dtype=torch.int16, device="cuda")
+    sigproc.unpack_device(torch.from_numpy(raw).cuda(), nspec, nchans, 16, out, "i16", stride,
+                          col0, invert=bool(invert))
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert np.array_equal(got[:, col0:col0 + nspec], want)
+    assert not got[:, :col0].any() and not got[:, col0 + nspec:].any()

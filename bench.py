@@ -258,6 +258,8 @@ def run_serve(args):
     srv.close()
     units = sum(beams[b][2].ndms * nsamp for _, b, _ in order)
     adds = sum(block_adds(args.algo, beams[b][1], nsamp) for _, b, _ in order)
+    # brute-force equivalent: the adds a brute-force search of the same trials would take
+    brute_adds = sum(block_adds("brute", beams[b][1], nsamp) for _, b, _ in order)
     data_s = len(order) * block_s
     line = {"metric": METRIC, "value": units / wall, "unit": METRIC, "n_gpus": 1,
             "steps": len(order), "warmup": 0, "ms_per_step": wall * 1e3 / len(order),
@@ -273,6 +275,7 @@ def run_serve(args):
                         "max_s": st["max_latency_s"]},
             "admission": {"admitted": st["admitted"], "deferred_submits": delayed},
             "algorithmic_adds_per_unit": adds / units, "add_rate_tadd_s": adds / wall / 1e12,
+            "brute_equivalent_tadd_s": brute_adds / wall / 1e12,
             "slowest_blocks": [[r["beam"], r["block"], r["ticket"], round(r["latency_s"], 4)]
                                for r in sorted(got, key=lambda r: -r["latency_s"])[:6]],
             "candidates": int(sum(r["ncand"] for r in got))}
@@ -325,11 +328,13 @@ def run_serve_plain(args):
     ncand = 0
     units = 0
     adds = 0
+    brute_adds = 0
     for b, k in order:
         nch = 1024 if b % 10 == 9 else 4096
         ncand += one(nch)
         units += plans[nch].info.ndms * nsamp
         adds += block_adds(args.algo, nch, nsamp)
+        brute_adds += block_adds("brute", nch, nsamp)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     line = {"metric": METRIC, "value": units / wall, "unit": METRIC, "n_gpus": 1,
@@ -341,7 +346,8 @@ def run_serve_plain(args):
                                    "0-2000, %s, one block at a time" % (nbeams, args.algo),
                        "blocks_per_beam": args.serve_blocks},
             "real_time_factor": len(order) * block_s / wall, "candidates": int(ncand),
-            "algorithmic_adds_per_unit": adds / units, "add_rate_tadd_s": adds / wall / 1e12}
+            "algorithmic_adds_per_unit": adds / units, "add_rate_tadd_s": adds / wall / 1e12,
+            "brute_equivalent_tadd_s": brute_adds / wall / 1e12}
     print(json.dumps(line), flush=True)
 
 

@@ -191,10 +191,9 @@ struct Instance {
     long long stride8 = 0;
     unsigned *d_flag = nullptr, *h_flag = nullptr;
     long long blocks8 = 0;
-    // The block after its copies runs on a worker thread, as the reference's dedispersion and
-    // output threads do, so the caller reads the next block meanwhile; next_chunk,
-    // start_processing and tearDown wait for it.
-    std::thread worker;
+    // The block after its copies runs on a worker thread (g_worker), as the reference's
+    // dedispersion and output threads do, so the caller reads the next block meanwhile;
+    // next_chunk, start_processing and tearDown wait for it.
     mdsm_status wstatus = MDSM_OK;
     std::string werror;
 };
@@ -209,6 +208,16 @@ struct Job {
 };
 
 Instance g;
+
+// The worker of the block in flight; joined at exit too, if a caller never tears down.
+struct Worker {
+    std::thread t;
+    ~Worker()
+    {
+        if (t.joinable()) t.join();
+    }
+};
+Worker g_worker;
 
 // Candidate lines as the reference's detectors print them: "time, DM, snr" (process_brute
 // with its own statistics, dedispersion_output.cpp:202-204; process_subband, :114-127, whose
@@ -259,7 +268,7 @@ void write_candidates(const std::vector<mdsm_candidate> &c, long long nc, double
 
 void release()
 {
-    if (g.worker.joinable()) g.worker.join();
+    if (g_worker.t.joinable()) g_worker.t.join();
     if (g.fp) fclose(g.fp);
     if (g.plan) mdsm_plan_destroy(g.plan);
     if (g.plan8) mdsm_plan_destroy(g.plan8);
@@ -347,7 +356,7 @@ void setup_8bit(const SURVEY *s)
 // Wait for the block on the worker; its failure becomes this thread's error.
 mdsm_status join_worker()
 {
-    if (g.worker.joinable()) g.worker.join();
+    if (g_worker.t.joinable()) g_worker.t.join();
     const mdsm_status st = g.wstatus;
     if (st != MDSM_OK) set_error(g.werror);
     g.wstatus = MDSM_OK;
@@ -453,7 +462,7 @@ mdsm_status submit_block(unsigned data_read)
         j.rms.assign(g.crms, g.crms + nchunks);
     }
     MDSM_TRY(stage_block(j));
-    g.worker = std::thread([j]() {
+    g_worker.t = std::thread([j]() {
         g.wstatus = finish_block(j);
         if (g.wstatus != MDSM_OK) g.werror = mdsm_last_error();
     });

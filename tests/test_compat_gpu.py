@@ -281,3 +281,26 @@ def test_integer_blocks_take_8bit_kernels_subband(lib, orc, cuda, tmp_path):
         _, want = orc.subband_dedisperse(x[:, k * nsamp: k * nsamp + stride], S1, S2, 16, nsamp,
                                          n1, pas["calldms"])
         assert np.array_equal(y, want), k
+
+
+def test_exit_with_a_block_in_flight(lib, cuda, tmp_path):
+    """A caller that exits right after start_processing, without tearDownMDSM, exits cleanly
+    (the block's worker is joined at exit)."""
+    import subprocess
+    import sys
+    obs = tmp_path / "obs.xml"
+    obs.write_text(OBS.format(dir=str(tmp_path)))
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = (
+        "import numpy as np\n"
+        "from mdsm_gb300 import compat\n"
+        f"s = compat.processSurveyParameters({str(obs)!r})\n"
+        "buf = compat.initialiseMDSM(s)\n"
+        "buf[:] = 1.0\n"
+        "compat.next_chunk(s.contents.nsamp, 0.0, 0.000064)\n"
+        "assert compat.start_processing(s.contents.nsamp) == 1\n"
+        "print('submitted', flush=True)\n")
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, capture_output=True, text=True,
+                       timeout=300)
+    assert r.returncode == 0, r.stderr[-2000:]
+    assert "submitted" in r.stdout

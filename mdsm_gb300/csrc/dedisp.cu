@@ -231,9 +231,12 @@ constexpr int kPCC = 16;         // channels per stage
 constexpr int kPNR = 3;          // raw stages in flight
 constexpr int kPT = 512;         // samples per tile (wider where no flush registers are kept)
 
-template <int SW_, int NW_, int DPW_, bool U16OUT_ = false, int PT_ = kPT>
+template <int SW_, int NW_, int DPW_, bool U16OUT_ = false, int PT_ = kPT, bool SIGNED_ = false>
 struct PackedCfg {
     static constexpr bool U16OUT = U16OUT_;       // store the sums as uint16
+    // int16 samples: the expansion flips each sample's sign bit (x + 32768, offset binary), the
+    // store takes 32768 per channel off again
+    static constexpr bool SIGNED = SIGNED_;
     static constexpr int SW = SW_;                // bytes per sample
     static constexpr int SPW = 4 / SW;            // samples per word = phase copies
     static constexpr int NW = NW_;                // compute warps (the producer is warp NW)
@@ -247,6 +250,7 @@ struct PackedCfg {
     static_assert(DPW == 1 || DPW == 2, "one or two DM trials per warp");
     static_assert(!U16OUT || SW == 1, "uint16 output from uint8 samples");
     static_assert(PT % (32 * SPW) == 0, "whole words per lane");
+    static_assert(!SIGNED || (SW == 2 && !U16OUT), "signed samples are int16");
 };
 using CfgU8 = PackedCfg<1, 19, 2>;
 using CfgU8w16 = PackedCfg<1, 16, 2>;         // 32-trial blocks, for trial counts of 32 k
@@ -259,6 +263,8 @@ using CfgU8to16T = PackedCfg<1, NW, 2, true, PT>;
 // shared memory (1024-sample rows of uint16 never fit with their two phase copies).
 template <int PT>
 using CfgU16T = PackedCfg<2, 16, 1, false, PT>;
+template <int PT>
+using CfgI16T = PackedCfg<2, 16, 1, false, PT, true>;
 
 // Work items of the packed kernels are (beam, DM block, time tile, group) tiles; a CTA runs a
 // stream of them.  The producer warp stages the stream's chunks (16 channels of one item) into
@@ -470,8 +476,15 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 // cross from one row into the next stores to consecutive addresses
                 uint32_t *Pr = P + ((size_t)pb * SPW * kPCC + row) * nwp;
                 {
-                    const uint4 w = reinterpret_cast<const uint4 *>(W)[i];
-                    const uint32_t w4 = W[4 * i + 4];
+                    uint4 w = reinterpret_cast<const uint4 *>(W)[i];
+                    uint32_t w4 = W[4 * i + 4];
+                    if constexpr (Cfg::SIGNED) {
+                        w.x ^= 0x80008000u;
+                        w.y ^= 0x80008000u;
+                        w.z ^= 0x80008000u;
+                        w.w ^= 0x80008000u;
+                        w4 ^= 0x80008000u;
+                    }
                     reinterpret_cast<uint4 *>(Pr)[i] = w;
 #pragma unroll
                     for (int a = 1; a < SPW; ++a)
@@ -616,8 +629,11 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 }
                 int32_t v[SPW];
                 if constexpr (SW == 2) {
-                    v[0] = (int32_t)(A[j][r] - (O[j][r] << 16));
-                    v[SPW - 1] = (int32_t)O[j][r];
+                    // offset-binary sums less 32768 per channel (exact: the host keeps
+                    // nchans * 65535 below 2^31)
+                    const uint32_t bias = Cfg::SIGNED ? 32768u * (uint32_t)a.nchans : 0u;
+                    v[0] = (int32_t)(A[j][r] - (O[j][r] << 16) - bias);
+                    v[SPW - 1] = (int32_t)(O[j][r] - bias);
                 } else {
 #pragma unroll
                     for (int e = 0; e < SPW; ++e) v[e] = f[j][r][e];
@@ -862,7 +878,7 @@ mdsm_status build_stage_tables(StageGeom &g, const std::vector<int32_t> &S)
                 if (packed_tables<CfgU8w16>(g, S, 2)) return MDSM_OK;
             }
         }
-        if (g.in_dtype == MDSM_U16 && !g.out_u16 &&
+        if ((g.in_dtype == MDSM_U16 || g.in_dtype == MDSM_I16) && !g.out_u16 &&
             (long long)g.nchans * 65535 <= 0x7fffffffLL &&
             (packed_tables<CfgU16T<768>>(g, S, 3) || packed_tables<CfgU16T<512>>(g, S, 3)))
             return MDSM_OK;
@@ -952,8 +968,11 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
                            : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU8to16T<16, 512>>);
         threads = CfgU8w16::THREADS;
     } else if (g.kernel == 3) {
-        fn = g.T == 768 ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16T<768>>)
-                        : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16T<512>>);
+        const bool sgn = g.in_dtype == MDSM_I16;
+        fn = g.T == 768 ? (sgn ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgI16T<768>>)
+                               : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16T<768>>))
+                        : (sgn ? reinterpret_cast<void *>(&k_shift_sum_packed<CfgI16T<512>>)
+                               : reinterpret_cast<void *>(&k_shift_sum_packed<CfgU16T<512>>));
         threads = CfgU16T<512>::THREADS;
     } else {
         persistent = false;

@@ -243,3 +243,25 @@ def test_packed_u16_tile_widths(lib, orc, cuda):
         got = _run(plan, x, torch)
         assert np.array_equal(got, orc.dedisperse(x, plan.shift_table(), nsamp)), dmstep
     assert {768, 512} <= seen, seen
+
+
+@pytest.mark.parametrize("nchans,nsamp,ndms", [(48, 3000, 70), (600, 2222, 40), (32767, 600, 3)])
+def test_packed_i16_matches_oracle(lib, orc, cuda, nchans, nsamp, ndms):
+    """int16 samples on the packed 16-bit kernel (offset binary in shared memory, 32768 per
+    channel taken off at the store): exact against the oracle, with rows of -32768 and of
+    32767 throughout (sums down to -32768 * 32767)."""
+    import mdsm_gb300 as m
+    torch = cuda
+    segs = [(0.0, 0.5 if nchans < 10000 else 0.02, ndms)]
+    plan = m.BrutePlan(nchans, 1500.0, -300.0 / nchans, 64e-6, nsamp, segs, in_dtype="i16",
+                       out_dtype="i32")
+    assert plan.info.kernel == 3
+    nch, stride = plan.input_shape()
+    for fill in ("random", "min", "max"):
+        if fill == "random":
+            x = np.random.default_rng(nchans).integers(-32768, 32768, (nch, stride),
+                                                       dtype=np.int16)
+        else:
+            x = np.full((nch, stride), -32768 if fill == "min" else 32767, np.int16)
+        got = _run(plan, x, torch)
+        assert np.array_equal(got, orc.dedisperse(x, plan.shift_table(), nsamp)), fill

@@ -417,6 +417,66 @@ def run_batch(args):
     batch.close()
 
 
+def run_stage(args):
+    """The reference's stage interface (processSurveyParameters, initialiseMDSM, next_chunk,
+    start_processing, tearDownMDSM) driven as src/MDSM.cpp drives it: float blocks of 8-bit
+    samples (as its file reader fills them; they take the 8-bit kernels) and, for comparison,
+    the same blocks with fractional values (the float kernels).  Wall time per block with the
+    caller's buffer fill inside the loop; brute force, 4096 ch x 2^16 samples x 1024 DM trials
+    0-250, process_brute detection."""
+    import tempfile
+
+    from mdsm_gb300 import compat
+    nch, nsamp, ndms, step = 4096, 1 << 16, 1024, 0.244140625
+    xml = ("<observation><frequencies top=\"%.1f\" offset=\"%.10f\" />"
+           "<dm lowDM=\"0\" numDMs=\"%d\" dmStep=\"%.9f\" useBruteForce=\"1\" useL1Cache=\"1\" />"
+           "<samples number=\"%d\" /><channels number=\"%d\" subbands=\"64\" />"
+           "<timing tsamp=\"%g\" /><detection threshold=\"6\" />"
+           "<output filePrefix=\"stage\" baseDirectory=\"%s\" secondsPerFile=\"600\" "
+           "usePCTime=\"0\" singleFileMode=\"1\" /><gpus ids=\"0\" /></observation>")
+    out = {}
+    with tempfile.TemporaryDirectory() as d:
+        obs = os.path.join(d, "obs.xml")
+        with open(obs, "w") as f:
+            f.write(xml % (FCH1, -BW / nch, ndms, step, nsamp, nch, TSAMP, d))
+        for kind in ("8bit", "float"):
+            survey = compat.processSurveyParameters(obs)
+            buf = compat.initialiseMDSM(survey)
+            ms = survey.contents.maxshift
+            rng = np.random.default_rng(5)
+            src = rng.integers(96, 160, buf.shape).astype(np.float32)
+            if kind == "float":
+                src += 0.25
+            buf[:] = src
+            times = []
+            nblocks = args.warmup + args.steps
+            for k in range(nblocks):
+                t0 = time.perf_counter()
+                if k:
+                    buf[:, ms:] = src[:, ms:]  # the caller's read of the next block
+                compat.next_chunk(nsamp, k * nsamp * TSAMP, TSAMP)
+                compat.start_processing(nsamp)
+                times.append(time.perf_counter() - t0)
+            compat.next_chunk(0, nblocks * nsamp * TSAMP, TSAMP)
+            n8 = compat.blocks_8bit()
+            compat.tearDownMDSM()
+            per = float(np.mean(times[args.warmup:]))
+            out[kind] = {"value": ndms * nsamp / per, "ms_per_block": per * 1e3,
+                         "blocks_on_8bit_kernels": int(n8)}
+    line = {"metric": METRIC, "value": out["8bit"]["value"], "unit": METRIC, "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out["8bit"]["ms_per_block"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "float32 in, int32 sums",
+            "data": "synthetic 8-bit samples (uniform 96-159) handed in as float32",
+            "config": {"workload": "stage interface (next_chunk / start_processing), brute force "
+                                   "4096 ch x 2^16 samples x 1024 DM trials 0-250, "
+                                   "process_brute detection, caller fill in the loop"},
+            "real_time_factor": nsamp * TSAMP / (out["8bit"]["ms_per_block"] / 1e3),
+            "blocks_on_8bit_kernels": out["8bit"]["blocks_on_8bit_kernels"],
+            "fractional_floats": out["float"]}
+    print(json.dumps(line), flush=True)
+
+
 def run_precision(args):
     """Precision report: INT32 and FP32 accumulation against the FP64 oracle, per sample type
     (uint8 mean 128 sigma 16, int16 sigma 1000, float32 N(0,1)), 4096 channels, 64 DM trials;
@@ -492,7 +552,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--case", default="full",
-                    choices=["full", "small", "serve", "batch", "precision"],
+                    choices=["full", "small", "serve", "batch", "precision", "stage"],
                     help="small: 2048 ch x 2^16 samples x 512 DM trials (profiling case); "
                          "serve: the multi-beam serving form")
     ap.add_argument("--algo", default="subband", choices=["subband", "brute"])
@@ -513,6 +573,8 @@ def main():
         return run_batch(args)
     if args.case == "precision":
         return run_precision(args)
+    if args.case == "stage":
+        return run_stage(args)
 
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

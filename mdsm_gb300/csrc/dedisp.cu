@@ -793,6 +793,24 @@ int tile_tables(StageGeom &g, const std::vector<int32_t> &S)
     return maxspan;
 }
 
+// Dynamic shared memory a packed CTA may take: the device's opt-in limit per block (227 KB on
+// GB300; the packed kernels declare no static shared memory), 220 KB if it cannot be read.
+size_t packed_smem_limit()
+{
+    static size_t lim = 0;
+    if (!lim) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&v, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) ==
+                cudaSuccess &&
+            v > 0)
+            lim = (size_t)v;
+        else
+            lim = 220 * 1024;
+    }
+    return lim;
+}
+
 template <class Cfg>
 size_t packed_smem(int rawcap, int ps)
 {
@@ -818,7 +836,7 @@ bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
     const int rawcap =
         (int)(((long long)(Cfg::PT + maxspan) * Cfg::SW + 32 + 15) / 16 * 16) + 16;
     const int ps = rawcap - 16;  // nwp = ps/4 words; the expansion reads word nwp too
-    if (packed_smem<Cfg>(rawcap, ps) > 220 * 1024 || ps >= 4096) return false;
+    if (packed_smem<Cfg>(rawcap, ps) > packed_smem_limit() || ps >= 4096) return false;
     g.max_span = maxspan;
     g.rowcap = rawcap;
     g.ps = ps;
@@ -1045,7 +1063,8 @@ mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams)
     b.rawcap = rawcap;
     b.ps = ps;
     b.smem = rawcap ? packed_smem<CfgU8>(rawcap, ps) : 0;
-    if (b.smem > 220 * 1024) return fail(MDSM_EINVAL, "batch: common staging does not fit");
+    if (b.smem > packed_smem_limit())
+        return fail(MDSM_EINVAL, "batch: common staging does not fit");
     // per packed beam: offsets re-expressed with the common phase stride
     b.d_rel.assign(beams.size(), nullptr);
     for (size_t i = 0; i < beams.size(); ++i) {

@@ -496,7 +496,7 @@ mdsm_status mdsm_server_submit(mdsm_server *sv, int beam, const void *h_block,
     // blocks are copied by several threads, a band of channels each
     const size_t row = (size_t)cols * b.elem;
     const int nthr = (int)std::min<long long>(
-        std::max(1u, std::min(8u, std::thread::hardware_concurrency())),
+        std::max(1u, std::min(16u, std::thread::hardware_concurrency())),
         std::max<long long>(1, (long long)row * p.nchans / (4ll << 20)));
     auto copy_rows = [&](int c0, int c1) {
         for (int c = c0; c < c1; ++c)

@@ -304,3 +304,41 @@ def test_exit_with_a_block_in_flight(lib, cuda, tmp_path):
                        timeout=300)
     assert r.returncode == 0, r.stderr[-2000:]
     assert "submitted" in r.stdout
+
+
+def test_integer_blocks_with_downsampled_passes_stay_float(lib, cuda, tmp_path):
+    """A subband plan with a downsampled pass keeps integer-valued float blocks on the float
+    kernels (its binning averages samples into fractions); the output equals the float plan
+    run directly."""
+    import mdsm_gb300 as m
+    from mdsm_gb300 import compat
+    torch = cuda
+    obs = tmp_path / "obs.xml"
+    obs.write_text(OBS_SUB.format(dir=str(tmp_path)))
+    survey = compat.processSurveyParameters(obs)
+    nsamp, tsamp, nblocks = 4096, 0.000064, 2
+    x = np.random.default_rng(8).integers(0, 256, (256, nblocks * nsamp + 8192)).astype(
+        np.float32)
+    seen = {}
+    outs = _run_blocks(compat, survey, x, nblocks, 0.0, tsamp,
+                       before_teardown=lambda: seen.setdefault("n", compat.blocks_8bit()))
+    assert seen["n"] == 0 and len(outs) == nblocks
+    plan = m.SubbandPlan(256, 1500.0, -1.171875, tsamp, nsamp, 16,
+                         [dict(lowdm=0.0, highdm=32.0, dmstep=0.5, sub_dmstep=4.0, ncalls=8,
+                               calldms=8),
+                          dict(lowdm=32.0, highdm=96.0, dmstep=2.0, sub_dmstep=16.0, ncalls=4,
+                               calldms=8, binsize=2)], in_dtype="f32", out_dtype="f32")
+    nch, stride = plan.input_shape()
+    for k, y in enumerate(outs):
+        d_in = plan.alloc_input()
+        blk = np.zeros((nch, stride), np.float32)
+        w = min(nsamp + plan.info.maxshift, x.shape[1] - k * nsamp)
+        blk[:, :w] = x[:, k * nsamp: k * nsamp + w]
+        d_in[: blk.size].copy_(torch.from_numpy(blk.ravel()))
+        d_out = plan.alloc_output()
+        plan.dedisperse_device(d_in, d_out)
+        torch.cuda.synchronize()
+        want = d_out.cpu().numpy().reshape(y.shape)
+        # pass 1: 64 rows of nsamp samples; pass 2 (downsample 2): 32 rows of nsamp / 2
+        assert np.array_equal(y[:64], want[:64]), k
+        assert np.array_equal(y[64:96, : nsamp // 2], want[64:96, : nsamp // 2]), k

@@ -120,18 +120,35 @@ struct Server {
     }
 };
 
-// Pin `count` staging buffers of at least `bytes` ahead of time (as far as the budget allows),
-// so that the first blocks of a beam do not wait for page pinning.
+// Pin `count` more staging buffers of `bytes` ahead of time, as far as the host staging budget
+// allows without dropping any, so that blocks queued while the GPU is busy do not wait for
+// page pinning (several hundred MB a block) inside the serving loop.
 void Server::prestage(size_t bytes, int count)
 {
-    std::vector<int> got;
     for (int i = 0; i < count; ++i) {
-        int idx = -1;
-        if (stage_get(bytes, &idx, false) != MDSM_OK) break;
-        got.push_back(idx);
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            if (pool_bytes + (long long)bytes > desc.host_stage_bytes) return;
+            pool_bytes += (long long)bytes;
+        }
+        void *h = nullptr;
+        const bool ok = cudaHostAlloc(&h, bytes, 0) == cudaSuccess;
+        std::lock_guard<std::mutex> lk(mu);
+        if (!ok) {
+            pool_bytes -= (long long)bytes;
+            return;
+        }
+        size_t slot = pool.size();
+        for (size_t k = 0; k < pool.size(); ++k)
+            if (!pool[k].h) {
+                slot = k;
+                break;
+            }
+        if (slot == pool.size()) pool.emplace_back();
+        pool[slot].h = h;
+        pool[slot].bytes = bytes;
+        pool[slot].used = false;
     }
-    std::lock_guard<std::mutex> lk(mu);
-    for (int idx : got) pool[(size_t)idx].used = false;
 }
 
 // A free pinned buffer of at least `bytes` (the smallest that fits), else a new one while the

@@ -259,6 +259,26 @@ mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, in
                                       mdsm_candidate *h_cands, long long cap, long long *ncand,
                                       void *stream);
 
+/* Single-pulse search in the form of the reference's prototype (src/prototypes/singlepulse.cpp:
+ * 20-23,41-146,148-300), on the device.  Widths: 1, then the prototype's downfactor ladder
+ * {2,3,4,6,9,14,20,30,45,70,100,150} up to max_downfact (>= 2; the prototype uses 30).  The
+ * response of width w at sample t is the template sum over [t - w/2, t - w/2 + w) (the
+ * prototype's centred templates; zero outside the series) in FP32, left to right, then
+ * (sum - w*mean) / (sigma*sqrt(w)): with normalise = 0 mean 0 and sigma 1 (the prototype's
+ * input is already normalised, e.g. by mdsm_detrend_normalise_device), with normalise = 1 the
+ * row's own statistics as the boxcar search forms them.  Per DM, in chunks of chunk_len
+ * samples (the prototype: 8000): each width's samples with response >= threshold, pruned by
+ * the prototype's pruneRelated (:90-120) for widths > 1; then the DM's survivors in (chunk,
+ * width, sample) order pruned by its pruneRelatedDownfactors (:122-146); the rest are the
+ * candidates, written in that order (width = the template width, snr = the response).  The two
+ * prune functions behave as the prototype writes them; its main loop's defects are not
+ * reproduced.  MDSM_ERANGE if more than max(4*cap, 2^18) crossings survive the first prune. */
+mdsm_status mdsm_singlepulse_detect_device(const void *d_series, int series_dtype, int ndms,
+                                           int nsamp, int max_downfact, int chunk_len,
+                                           int normalise, double threshold,
+                                           mdsm_candidate *h_cands, long long cap,
+                                           long long *ncand, void *stream);
+
 /* Time downsampling of a channel-major block: out[c][t] = f(sum_{k<b} in[c][t*b+k]) for
  * t < len/b, f = sum (mode 0; integer samples widen: uint8 -> uint16 or int32, 16-bit -> int32),
  * mean (mode 1) or sum/sqrt(b) (mode 2) in float32.  The reference's binning kernels

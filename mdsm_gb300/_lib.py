@@ -150,6 +150,9 @@ SIGNATURES = {
                                              _vp]),
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
+    "mdsm_singlepulse_detect_device": (_st, [_vp, _i, _i, _i, _i, _i, _i, _d,
+                                             ctypes.POINTER(Candidate), _ll, ctypes.POINTER(_ll),
+                                             _vp]),
     "mdsm_downsample_device": (_st, [_vp, _i, _i, _ll, _ll, _i, _i, _vp, _i, _ll, _vp]),
     "mdsm_detrend_normalise_device": (_st, [_vp, _i, _ll, _i, _vp]),
     "mdsm_sigproc_read_header": (_st, [ctypes.c_char_p, ctypes.POINTER(SigprocHeader)]),

@@ -260,6 +260,22 @@ def boxcar_detect_device(series, nwidths=9, threshold=6.0, cap=1 << 20, stream=N
     return _cands_to_array(buf, min(n.value, cap)), n.value
 
 
+def singlepulse_detect_device(series, max_downfact=30, chunk_len=8000, threshold=6.0,
+                              normalise=False, cap=1 << 20, stream=None):
+    """The single-pulse prototype's search (template form) on a device series [ndms][nsamp]
+    (float32 or int32): candidates in the prototype's list order (dm, chunk, width, sample)."""
+    import torch
+    ndms, nsamp = series.shape
+    dt = 1 if series.dtype == torch.int32 else 0
+    buf = (Candidate * max(cap, 1))()
+    n = ctypes.c_longlong()
+    check(load().mdsm_singlepulse_detect_device(ctypes.c_void_p(series.data_ptr()), dt, ndms,
+                                                nsamp, int(max_downfact), int(chunk_len),
+                                                int(bool(normalise)), float(threshold), buf, cap,
+                                                ctypes.byref(n), _stream_ptr(stream)))
+    return _cands_to_array(buf, min(n.value, cap)), n.value
+
+
 def detrend_normalise_device(series, length=1024, stream=None):
     """In-place detrend and normalise of a float32 device series [ndms][nsamp]."""
     ndms, nsamp = series.shape

@@ -40,7 +40,7 @@ std::mutex g_slots_mu;
 std::map<int, std::unique_ptr<ScratchSlot>> g_slots;
 }  // namespace
 
-static mdsm_status scratch_get(size_t bytes, void **out, std::unique_lock<std::mutex> *lease)
+mdsm_status scratch_get(size_t bytes, void **out, std::unique_lock<std::mutex> *lease)
 {
     int dev = 0;
     MDSM_CUDA_TRY(cudaGetDevice(&dev));
@@ -63,10 +63,6 @@ static mdsm_status scratch_get(size_t bytes, void **out, std::unique_lock<std::m
     return MDSM_OK;
 }
 
-struct DevCand {
-    int32_t dm_idx, sample, width;
-    float snr;
-};
 
 __device__ __forceinline__ float median5(float n1, float n2, float n3, float n4, float n5)
 {
@@ -591,6 +587,29 @@ __global__ void __launch_bounds__(256)
         const double var = __dadd_rn(e2, -__dmul_rn(m, m));
         musig[d] = make_double2(m, var > 0.0 ? __dsqrt_rn(var) : 0.0);
     }
+}
+
+// Per-DM (mean, sigma) of float32 or int32 series into musig (the statistics both searches
+// use); part: series_stats_part_bytes() of work space for the float form.
+size_t series_stats_part_bytes(int ndms, long long n)
+{
+    return (size_t)ndms * (size_t)((n + 1023) / 1024) * sizeof(double2);
+}
+
+mdsm_status series_stats_launch(const void *y, int dtype, int ndms, long long n, double2 *part,
+                                double2 *musig, cudaStream_t st)
+{
+    if (dtype == MDSM_OUT_F32) {
+        const int nch = (int)((n + 1023) / 1024);
+        dim3 g1((unsigned)((nch + 127) / 128), (unsigned)ndms);
+        k_series_chunk_sums<float><<<g1, 128, 0, st>>>(static_cast<const float *>(y), n, nch,
+                                                       part);
+        k_series_finish<<<(ndms + 127) / 128, 128, 0, st>>>(part, ndms, nch, n, musig);
+    } else {
+        k_series_stats_int<<<ndms, 256, 0, st>>>(static_cast<const int32_t *>(y), n, musig);
+    }
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return MDSM_OK;
 }
 
 constexpr int kBoxTile = 2048;   // output samples per CTA

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -169,7 +170,23 @@ int32_t shift_of(float dms, double delay64, float lowdm, float dmstep, int idx, 
                  int mode);
 
 // ----------------------------------------------------------------------------------------
-// detection / rfi launchers (detect.cu, rfi.cu)
+// detection / rfi launchers (detect.cu, rfi.cu, singlepulse.cu)
+// ----------------------------------------------------------------------------------------
+// candidate record as the device kernels write it
+struct DevCand {
+    int32_t dm_idx, sample, width;
+    float snr;
+};
+// The detectors' grow-only per-device work buffer; the lease holds it until the call returns.
+mdsm_status scratch_get(size_t bytes, void **out, std::unique_lock<std::mutex> *lease);
+// Per-DM (mean, sigma) in double of float32 / int32 series (the boxcar searches' statistics).
+size_t series_stats_part_bytes(int ndms, long long n);
+mdsm_status series_stats_launch(const void *y, int dtype, int ndms, long long n, double2 *part,
+                                double2 *musig, cudaStream_t st);
+mdsm_status singlepulse_detect(const void *d_series, int dtype, int ndms, int nsamp,
+                               int max_downfact, int chunk_len, int normalise, double threshold,
+                               mdsm_candidate *h_cands, long long cap, long long *ncand,
+                               cudaStream_t st);
 // ----------------------------------------------------------------------------------------
 mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, float dmstep,
                        float threshold, mdsm_candidate *h_cands, long long cap,

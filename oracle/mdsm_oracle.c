@@ -637,3 +637,295 @@ void orc_detrend_normalise(float *y, long n, int len)
         for (int i = 0; i < len; i++) y[b0 + i] = (float)(y[b0 + i] / sd);
     }
 }
+
+/* ------------------------------------------------------------------------------------ */
+/* single-pulse search in the prototype's template form                                */
+/* ------------------------------------------------------------------------------------ */
+
+/* src/prototypes/singlepulse.cpp:20 -- the downfactor ladder; :161-164 keeps the factors up to
+ * maxDownfact.  widths[0] = 1 (the unsmoothed series, :240-245), then the kept factors. */
+static const int kSpDownfactors[12] = {2, 3, 4, 6, 9, 14, 20, 30, 45, 70, 100, 150};
+
+int orc_sp_widths(int max_downfact, int *widths)
+{
+    int nw = 0;
+    widths[nw++] = 1;
+    for (int i = 0; i < 12 && kSpDownfactors[i] <= max_downfact; i++) widths[nw++] = kSpDownfactors[i];
+    return nw;
+}
+
+/* src/prototypes/singlepulse.cpp:90-120 and the store test at :279, as written.  For each
+ * candidate x not yet masked, every later candidate y within factor/2 bins that is not masked
+ * either gets mask 1 if x.value > y.value, else mask = (char)(x's list index): the prototype
+ * writes `mask[j] = i` where `mask[i] = 1` was presumably meant, so y is still masked unless
+ * x's index is a multiple of 256 (then y survives).  keep[i] = mask[i] == 0 and the value is
+ * not 0 (masked entries are zeroed and the caller stores only non-zero values). */
+void orc_sp_prune_related(const int32_t *bins, const float *values, long num, int factor,
+                          unsigned char *keep)
+{
+    char *mask = (char *)calloc((size_t)(num > 0 ? num : 1), 1);
+    for (long i = 0; i + 1 < num; i++) {
+        if (mask[i]) continue;
+        for (long j = i + 1; j < num; j++) {
+            if ((unsigned)(bins[j] - bins[i]) > (unsigned)factor / 2u) break;
+            if (mask[j]) continue;
+            if (values[i] > values[j]) mask[j] = 1;
+            else mask[j] = (char)(i & 0xff);
+        }
+    }
+    for (long i = 0; i < num; i++) keep[i] = (unsigned char)(!mask[i] && values[i] != 0.0f);
+    free(mask);
+}
+
+/* src/prototypes/singlepulse.cpp:122-146, as written, with the mask starting at zero: for each
+ * unmasked x and each later y (list order) until |y.bin - x.bin| > maxdf/2, an unmasked y
+ * within max(x.df/2, y.df/2, 1) bins masks the weaker of the two (x when the values tie). */
+void orc_sp_prune_downfactors(const int64_t *bins, const float *values, const int32_t *df,
+                              long n, int maxdf, unsigned char *mask)
+{
+    memset(mask, 0, (size_t)n);
+    for (long i = 0; i < n; i++) {
+        if (mask[i]) continue;
+        for (long j = i + 1; j < n; j++) {
+            const long long d = llabs((long long)(bins[j] - bins[i]));
+            if (d > (long long)((unsigned)maxdf / 2u)) break;
+            if (mask[j]) continue;
+            unsigned prox = (unsigned)df[i] / 2u > (unsigned)df[j] / 2u ? (unsigned)df[i] / 2u
+                                                                        : (unsigned)df[j] / 2u;
+            prox = prox > 1u ? prox : 1u;
+            if (d <= (long long)prox) {
+                if (values[i] > values[j]) mask[j] = 1;
+                else mask[i] = 1;
+            }
+        }
+    }
+}
+
+/* Template response of width w at sample t: the series in float (0 outside [0, n)), summed
+ * left to right over [t - w/2, t - w/2 + w) in FP32, then (sum - w*mu) * inv.  The prototype
+ * convolves with the same centred template (:41-67; the odd widths centred on t, the even ones
+ * one sample longer on the left) by FFT; this direct sum is its exact value. */
+static float sp_value(const float *x, long n, long t, int w, float mu_f, float inv)
+{
+    const long s = t - w / 2;
+    float acc = (s >= 0 && s < n) ? x[s] : 0.0f;
+    for (int k = 1; k < w; k++) {
+        const long u = s + k;
+        acc = acc + ((u >= 0 && u < n) ? x[u] : 0.0f);
+    }
+    return (acc - (float)w * mu_f) * inv;
+}
+
+void orc_sp_values(const double *y, long n, int w, int normalise, int is_int, float *out)
+{
+    float *x = (float *)malloc(sizeof(float) * (size_t)n);
+    for (long t = 0; t < n; t++) x[t] = (float)y[t];
+    double mu = 0.0, sig = 1.0;
+    if (normalise) {
+        if (is_int) orc_series_stats_int(y, n, &mu, &sig);
+        else orc_series_stats(y, n, &mu, &sig);
+    }
+    const float mu_f = (float)mu, inv = (float)(1.0 / (sig * sqrt((double)w)));
+    for (long t = 0; t < n; t++) out[t] = sp_value(x, n, t, w, mu_f, inv);
+    free(x);
+}
+
+/* The prototype's search (singlepulse.cpp:148-300) per DM row, in chunks of chunk_len samples:
+ * for each chunk and each width (1 first, then the ladder) the samples whose response is >=
+ * threshold form a list in sample order; lists of widths > 1 are pruned with pruneRelated; the
+ * survivors of all chunks and widths, in that order, are pruned with pruneRelatedDownfactors
+ * and the unmasked ones are the candidates (dm, sample, width, response).
+ * Deviations, each a defect of the prototype's main loop: the first chunk reads its own DM row
+ * (:229 reads row 0), every sample of a chunk is searched (:240,261 stop `overlap` samples
+ * short), a trailing partial chunk is searched too (:186 drops it), a candidate carries its own
+ * sample and value (:243 adds the overlap to the sample, :281 takes the value of entry j and
+ * the list index as the sample), the list loop does not reuse the DM loop's counter (:295),
+ * the downfactor mask starts at zero and the unmasked candidates are kept (:291-297 keeps the
+ * masked ones of an uninitialised mask), and the response is the exact template sum (the
+ * prototype's spectra hold n/2 bins where the real transform has n/2 + 1).
+ * normalise = 0 takes the series as already normalised (mean 0, sigma 1), as the prototype
+ * does; 1 uses the row's mean and sigma (orc_series_stats_int for integer series). */
+long orc_singlepulse_detect(const double *y, int ndms, long n, int max_downfact, long chunk_len,
+                            int normalise, int is_int, double threshold, int32_t *dm_idx,
+                            int32_t *samp, int32_t *width, float *snr, long cap)
+{
+    int widths[13];
+    const int nw = orc_sp_widths(max_downfact, widths);
+    const int maxdf = widths[nw - 1];
+    const float thr = (float)threshold;
+    long total = 0;
+    float *x = (float *)malloc(sizeof(float) * (size_t)(n > 0 ? n : 1));
+    int32_t *lb = (int32_t *)malloc(sizeof(int32_t) * (size_t)(chunk_len + 1));
+    float *lv = (float *)malloc(sizeof(float) * (size_t)(chunk_len + 1));
+    unsigned char *keep = (unsigned char *)malloc((size_t)(chunk_len + 1));
+    for (int d = 0; d < ndms; d++) {
+        const double *yr = y + (long)d * n;
+        for (long t = 0; t < n; t++) x[t] = (float)yr[t];
+        double mu = 0.0, sig = 1.0;
+        if (normalise) {
+            if (is_int) orc_series_stats_int(yr, n, &mu, &sig);
+            else orc_series_stats(yr, n, &mu, &sig);
+            if (!(sig > 0.0)) continue;
+        }
+        const float mu_f = (float)mu;
+        float inv[13];
+        for (int k = 0; k < nw; k++) inv[k] = (float)(1.0 / (sig * sqrt((double)widths[k])));
+        long cnt = 0, capc = 1024;
+        int64_t *cb = (int64_t *)malloc(sizeof(int64_t) * (size_t)capc);
+        float *cv = (float *)malloc(sizeof(float) * (size_t)capc);
+        int32_t *cw = (int32_t *)malloc(sizeof(int32_t) * (size_t)capc);
+        for (long c0 = 0; c0 < n; c0 += chunk_len) {
+            const long c1 = c0 + chunk_len < n ? c0 + chunk_len : n;
+            for (int k = 0; k < nw; k++) {
+                long num = 0;
+                for (long t = c0; t < c1; t++) {
+                    const float v = sp_value(x, n, t, widths[k], mu_f, inv[k]);
+                    if (v >= thr) {
+                        lb[num] = (int32_t)(t - c0);
+                        lv[num] = v;
+                        num++;
+                    }
+                }
+                if (num == 0) continue;
+                if (k > 0) orc_sp_prune_related(lb, lv, num, widths[k], keep);
+                else for (long i = 0; i < num; i++) keep[i] = 1;
+                for (long i = 0; i < num; i++) {
+                    if (!keep[i]) continue;
+                    if (cnt == capc) {
+                        capc *= 2;
+                        cb = (int64_t *)realloc(cb, sizeof(int64_t) * (size_t)capc);
+                        cv = (float *)realloc(cv, sizeof(float) * (size_t)capc);
+                        cw = (int32_t *)realloc(cw, sizeof(int32_t) * (size_t)capc);
+                    }
+                    cb[cnt] = c0 + lb[i];
+                    cv[cnt] = lv[i];
+                    cw[cnt] = widths[k];
+                    cnt++;
+                }
+            }
+        }
+        unsigned char *mask = (unsigned char *)malloc((size_t)(cnt > 0 ? cnt : 1));
+        orc_sp_prune_downfactors(cb, cv, cw, cnt, maxdf, mask);
+        for (long i = 0; i < cnt; i++) {
+            if (mask[i]) continue;
+            if (total < cap) {
+                dm_idx[total] = d;
+                samp[total] = (int32_t)cb[i];
+                width[total] = cw[i];
+                snr[total] = cv[i];
+            }
+            total++;
+        }
+        free(mask);
+        free(cb);
+        free(cv);
+        free(cw);
+    }
+    free(x);
+    free(lb);
+    free(lv);
+    free(keep);
+    return total;
+}
+
+/* ------------------------------------------------------------------------------------ */
+/* the prototype kernels' own float arithmetic (to pin the oracle to their GPU output)  */
+/* ------------------------------------------------------------------------------------ */
+
+/* src/prototypes/detrend.cu:12-100 in its own float arithmetic and order, for a block of 256
+ * threads: per-thread strided sums, a shared-memory tree (:41-51), the line fit in thread 0
+ * (:55-56), the residuals (:67-75), a second tree (:83-85) and the division by the rms
+ * (:90,97-99).  The second tree has no barrier between its steps in the prototype; this
+ * restatement takes the synchronised order.  contract bit 1: the products summed into sxy, sxx
+ * and the rms are fused multiply-adds; bit 2: the fitted line a + b*x is one. */
+void orc_detrend_ref_f32(float *y, int ndms, int nsamp, int len, int contract)
+{
+    enum { NT = 256 };
+    const int nblk = nsamp / len;
+#pragma omp parallel for schedule(static)
+    for (long blk = 0; blk < (long)ndms * nblk; blk++) {
+        float *in = y + blk * len;
+        float sx[NT], sy[NT], sz[NT];
+        for (int tid = 0; tid < NT; tid++) {
+            float a = 0, b = 0, c = 0;
+            for (int i = tid; i < len; i += NT) {
+                const float x = (float)(-len / 2.0 + 0.5 + i);
+                const float v = in[i];
+                a = a + v;
+                if (contract & 1) {
+                    b = fmaf(x, v, b);
+                    c = fmaf(x, x, c);
+                } else {
+                    b = b + x * v;
+                    c = c + x * x;
+                }
+            }
+            sx[tid] = a;
+            sy[tid] = b;
+            sz[tid] = c;
+        }
+        for (int h = NT / 2; h >= 1; h /= 2)
+            for (int tid = 0; tid < h; tid++) {
+                sx[tid] = sx[tid] + sx[tid + h];
+                sy[tid] = sy[tid] + sy[tid + h];
+                sz[tid] = sz[tid] + sz[tid + h];
+            }
+        const float bb = sy[0] / sz[0];
+        const float aa = sx[0] / (float)len;
+        for (int tid = 0; tid < NT; tid++) {
+            float s = 0;
+            for (int i = tid; i < len; i += NT) {
+                const float x = (float)(-len / 2.0 + 0.5 + i);
+                const float line = (contract & 2) ? fmaf(bb, x, aa) : aa + bb * x;
+                const float val = in[i] - line;
+                in[i] = val;
+                s = (contract & 1) ? fmaf(val, val, s) : s + val * val;
+            }
+            sz[tid] = s;
+        }
+        for (int h = NT / 2; h >= 1; h /= 2)
+            for (int tid = 0; tid < h; tid++) sz[tid] = sz[tid] + sz[tid + h];
+        const float sd = sqrtf(sz[0] / (float)len);
+        for (int i = 0; i < len; i++) in[i] = in[i] / sd;
+    }
+}
+
+/* src/prototypes/rfi_clipper.cu:8-67 in its own float arithmetic and order, rows [nrows][nsamp],
+ * blockdim threads per row: per-thread strided sums (:17-25), thread 0's sequential sum of the
+ * partials (:34-37) starting from zero (the prototype leaves val1/val2 uninitialised), mean and
+ * standard deviation (:40-41), and the clip |x - mean| >= 4 sigma or <= sigma/4 to the mean
+ * (:60-62).  contract bit 1: the squares summed are fused multiply-adds; bit 2: val2 -
+ * (nsamp*mean)*mean is one.  means[r] receives the row mean. */
+void orc_rfi_clip_ref_f32(float *x, int nrows, int nsamp, int blockdim, int contract,
+                          float *means)
+{
+#pragma omp parallel for schedule(static)
+    for (int r = 0; r < nrows; r++) {
+        float *row = x + (long)r * nsamp;
+        float *p1 = (float *)calloc((size_t)blockdim, sizeof(float));
+        float *p2 = (float *)calloc((size_t)blockdim, sizeof(float));
+        for (int tid = 0; tid < blockdim; tid++)
+            for (int s = tid; s < nsamp; s += blockdim) {
+                const float v = row[s];
+                p1[tid] = p1[tid] + v;
+                p2[tid] = (contract & 1) ? fmaf(v, v, p2[tid]) : p2[tid] + v * v;
+            }
+        float v1 = 0.0f, v2 = 0.0f;
+        for (int i = 0; i < blockdim; i++) {
+            v1 = v1 + p1[i];
+            v2 = v2 + p2[i];
+        }
+        const float mean = v1 / (float)nsamp;
+        const float nm = (float)nsamp * mean;
+        const float num = (contract & 2) ? fmaf(-nm, mean, v2) : v2 - nm * mean;
+        const float sd = sqrtf(num / (float)nsamp);
+        means[r] = mean;
+        for (int s = 0; s < nsamp; s++) {
+            const float v = row[s];
+            const float tv = fabsf(v - mean);
+            if (tv >= sd * 4.0f || tv <= sd / 4.0f) row[s] = mean;
+        }
+        free(p1);
+        free(p2);
+    }
+}

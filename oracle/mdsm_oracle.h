@@ -137,6 +137,27 @@ long orc_unpack(const uint8_t *raw, long nbytes, int nbits, float *out);
 /* ---- detrend + normalise (detrend.cu:12-100), double, per block of len samples ---- */
 void orc_detrend_normalise(float *y, long n, int len);
 
+/* Single-pulse search in the prototype's template form (src/prototypes/singlepulse.cpp).
+ * orc_sp_widths: 1 then the downfactors <= max_downfact (:20,161-164); returns the count.
+ * orc_sp_prune_related / orc_sp_prune_downfactors: :90-120 / :122-146 as written.
+ * orc_sp_values: the width-w response at every sample.
+ * orc_singlepulse_detect: the per-DM search of :148-300 (chunked thresholds, both prunes);
+ * candidates in list order (dm, chunk, width, sample). */
+int orc_sp_widths(int max_downfact, int *widths);
+void orc_sp_prune_related(const int32_t *bins, const float *values, long num, int factor,
+                          unsigned char *keep);
+void orc_sp_prune_downfactors(const int64_t *bins, const float *values, const int32_t *df,
+                              long n, int maxdf, unsigned char *mask);
+void orc_sp_values(const double *y, long n, int w, int normalise, int is_int, float *out);
+long orc_singlepulse_detect(const double *y, int ndms, long n, int max_downfact, long chunk_len,
+                            int normalise, int is_int, double threshold, int32_t *dm_idx,
+                            int32_t *samp, int32_t *width, float *snr, long cap);
+/* The prototype kernels' own float arithmetic: src/prototypes/detrend.cu:12-100 (256 threads
+ * per block) and src/prototypes/rfi_clipper.cu:8-67 (blockdim threads per row), each with the
+ * device compiler's possible contractions as switches (see mdsm_oracle.c). */
+void orc_detrend_ref_f32(float *y, int ndms, int nsamp, int len, int contract);
+void orc_rfi_clip_ref_f32(float *x, int nrows, int nsamp, int blockdim, int contract,
+                          float *means);
 #ifdef __cplusplus
 }
 #endif

@@ -15,7 +15,12 @@ ORACLE_SO = os.path.join(HERE, "_build", platform.machine(), "libmdsm_oracle.so"
 HARNESS_SO = os.path.join(HERE, "_build", platform.machine(), "libref_gpu_harness.so")
 REF_HOST_SO = os.path.join(HERE, "_ref", "libref_host.so")
 REF_CUBIN = os.path.join(HERE, "_ref", "ref_kernels.cubin")
-REF_TREE = "/root/reference/src"
+REF_DETREND_CUBIN = os.path.join(HERE, "_ref", "ref_detrend.cubin")
+REF_RFI_CUBIN = os.path.join(HERE, "_ref", "ref_rfi.cubin")
+REF_SP_SO = os.path.join(HERE, "_ref", "libref_singlepulse.so")
+# the reference tree (MDSM's src/ directory): where it is present, build() compiles the
+# reference's own code into oracle/_ref/
+REF_TREE = os.environ.get("MDSM_REFERENCE_SRC", "")
 
 SHIFT = {"l1": 0, "l1_muladd": 1, "opt": 2, "opt_muladd": 3, "fp64_trunc": 4, "fp64_round": 5}
 
@@ -23,7 +28,7 @@ SHIFT = {"l1": 0, "l1_muladd": 1, "opt": 2, "opt_muladd": 3, "fp64_trunc": 4, "f
 def build(reference=True):
     """Build the oracle (always) and, when the reference tree is present here, its builds."""
     subprocess.run(["make", "-s", "-C", HERE, "oracle"], check=True)
-    if reference and os.path.isdir(REF_TREE):
+    if reference and REF_TREE and os.path.isdir(REF_TREE):
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_TREE], check=True)
     cuda_lib = any(os.path.exists(os.path.join(d, "libcuda.so")) for d in
                    ("/usr/local/cuda/lib64/stubs", "/usr/lib/x86_64-linux-gnu",
@@ -60,6 +65,8 @@ def lib():
         _O.orc_ref_detect_subband.restype = ctypes.c_long
         _O.orc_boxcar_detect.restype = ctypes.c_long
         _O.orc_unpack.restype = ctypes.c_long
+        _O.orc_singlepulse_detect.restype = ctypes.c_long
+        _O.orc_sp_widths.restype = ctypes.c_int
     return _O
 
 
@@ -235,6 +242,77 @@ def unpack(raw, nbits):
     return out[:n].copy()
 
 
+def sp_widths(max_downfact=30):
+    w = np.zeros(13, np.int32)
+    n = lib().orc_sp_widths(int(max_downfact), _p(w))
+    return w[:n].copy()
+
+
+def sp_prune_related(bins, values, factor):
+    """keep flags of singlepulse.cpp's pruneRelated (as written) over one sorted list."""
+    bins = np.ascontiguousarray(bins, np.int32)
+    values = np.ascontiguousarray(values, np.float32)
+    keep = np.zeros(bins.size, np.uint8)
+    lib().orc_sp_prune_related(_p(bins), _p(values), ctypes.c_long(bins.size), int(factor),
+                               _p(keep))
+    return keep.astype(bool)
+
+
+def sp_prune_downfactors(bins, values, downfacts, maxdf):
+    """mask of singlepulse.cpp's pruneRelatedDownfactors (as written, mask starting at 0)."""
+    bins = np.ascontiguousarray(bins, np.int64)
+    values = np.ascontiguousarray(values, np.float32)
+    df = np.ascontiguousarray(downfacts, np.int32)
+    mask = np.zeros(bins.size, np.uint8)
+    lib().orc_sp_prune_downfactors(_p(bins), _p(values), _p(df), ctypes.c_long(bins.size),
+                                   int(maxdf), _p(mask))
+    return mask.astype(bool)
+
+
+def sp_values(y, w, normalise=False, is_int=False):
+    """Width-w template response of a 1-D series at every sample."""
+    yd = np.ascontiguousarray(y, np.float64)
+    out = np.empty(yd.size, np.float32)
+    lib().orc_sp_values(_p(yd), ctypes.c_long(yd.size), int(w), int(bool(normalise)),
+                        int(bool(is_int)), _p(out))
+    return out
+
+
+def singlepulse_detect(y, max_downfact=30, chunk_len=8000, threshold=6.0, normalise=False,
+                       is_int=None, cap=1 << 22):
+    """The prototype's search (template form): (dm, sample, width, snr) in list order."""
+    if is_int is None:
+        is_int = np.issubdtype(np.asarray(y).dtype, np.integer)
+    yd = np.ascontiguousarray(y, np.float64)
+    ndms, n = yd.shape
+    dm = np.empty(cap, np.int32)
+    sa = np.empty(cap, np.int32)
+    wd = np.empty(cap, np.int32)
+    sn = np.empty(cap, np.float32)
+    cnt = lib().orc_singlepulse_detect(_p(yd), ndms, ctypes.c_long(n), int(max_downfact),
+                                       ctypes.c_long(chunk_len), int(bool(normalise)),
+                                       int(bool(is_int)), ctypes.c_double(threshold), _p(dm),
+                                       _p(sa), _p(wd), _p(sn), ctypes.c_long(cap))
+    k = min(cnt, cap)
+    return dm[:k].copy(), sa[:k].copy(), wd[:k].copy(), sn[:k].copy()
+
+
+def detrend_ref_f32(y, length, contract):
+    """detrend.cu's kernel arithmetic on y [ndms][nsamp] (a copy is returned)."""
+    y = np.array(y, np.float32, copy=True, order="C")
+    lib().orc_detrend_ref_f32(_p(y), y.shape[0], y.shape[1], int(length), int(contract))
+    return y
+
+
+def rfi_clip_ref_f32(x, blockdim, contract):
+    """rfi_clipper.cu's kernel arithmetic on x [nrows][nsamp]: (clipped copy, row means)."""
+    x = np.array(x, np.float32, copy=True, order="C")
+    means = np.empty(x.shape[0], np.float32)
+    lib().orc_rfi_clip_ref_f32(_p(x), x.shape[0], x.shape[1], int(blockdim), int(contract),
+                               _p(means))
+    return x, means
+
+
 def detrend_normalise(y, length=1024):
     y = np.array(y, np.float32, copy=True)
     lib().orc_detrend_normalise(_p(y), ctypes.c_long(y.size), length)
@@ -249,6 +327,16 @@ def ref_host_available():
     return os.path.exists(REF_HOST_SO)
 
 
+def ref_singlepulse_available():
+    return os.path.exists(REF_SP_SO)
+
+
+def ref_singlepulse():
+    """src/prototypes/singlepulse.cpp's own functions (built here against the FFTW stand-in)."""
+    h = ctypes.CDLL(REF_SP_SO)
+    return h
+
+
 def ref_host():
     h = ctypes.CDLL(REF_HOST_SO)
     h.ref_median_of_five.restype = ctypes.c_float
@@ -258,14 +346,39 @@ def ref_host():
 
 
 class RefGPU:
-    """The reference kernels from oracle/_ref/ref_kernels.cubin, launched on device 0."""
+    """The reference kernels from oracle/_ref/ref_kernels.cubin (and, where built, the
+    prototype kernels of detrend.cu and rfi_clipper.cu), launched on device 0."""
 
-    def __init__(self, cubin=REF_CUBIN):
+    def __init__(self, cubin=REF_CUBIN, proto=False):
         self.h = ctypes.CDLL(HARNESS_SO)
         self.h.rg_error.restype = ctypes.c_char_p
         rc = self.h.rg_init(cubin.encode())
         if rc:
             raise RuntimeError("rg_init: %d %s" % (rc, self.h.rg_error().decode()))
+        if proto:
+            rc = self.h.rg_init_proto(REF_DETREND_CUBIN.encode(), REF_RFI_CUBIN.encode())
+            if rc:
+                raise RuntimeError("rg_init_proto: %d %s" % (rc, self.h.rg_error().decode()))
+
+    def detrend(self, y, length):
+        """detrend_normalise on y [ndms][nsamp] (copy returned) and the kernel time in ms."""
+        y = np.array(y, np.float32, copy=True, order="C")
+        ms = ctypes.c_float()
+        rc = self.h.rg_detrend(_p(y), y.shape[0], y.shape[1], int(length), ctypes.byref(ms))
+        if rc:
+            raise RuntimeError("rg_detrend: %d %s" % (rc, self.h.rg_error().decode()))
+        return y, ms.value
+
+    def rfi_clip(self, x, blockdim):
+        """rfi_clipping on x [nrows][nsamp]: (clipped copy, row means, kernel ms)."""
+        x = np.array(x, np.float32, copy=True, order="C")
+        means = np.zeros(x.shape[0], np.float32)
+        ms = ctypes.c_float()
+        rc = self.h.rg_rfi_clip(_p(x), x.shape[0], x.shape[1], int(blockdim), _p(means),
+                                ctypes.byref(ms))
+        if rc:
+            raise RuntimeError("rg_rfi_clip: %d %s" % (rc, self.h.rg_error().decode()))
+        return x, means, ms.value
 
     def brute(self, kind, x, nsamp, maxshift, lowdm, dmstep, tsamp, tdms, dms):
         x = np.ascontiguousarray(x, np.float32)

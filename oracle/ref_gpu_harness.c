@@ -272,3 +272,87 @@ int rg_subband(const float *in, int nsamp, int nchans, int maxshift, int nsubs, 
     CK(cuMemFree(dout));
     return RG_OK;
 }
+
+/* ---- prototype kernels (src/prototypes/detrend.cu, src/prototypes/rfi_clipper.cu) ---- */
+
+static CUmodule g_mod_dt, g_mod_rfi;
+static CUfunction g_detrend, g_rfi;
+static int g_proto_loaded;
+
+/* Loads oracle/_ref/ref_detrend.cubin and oracle/_ref/ref_rfi.cubin (after rg_init). */
+int rg_init_proto(const char *detrend_cubin, const char *rfi_cubin)
+{
+    if (!g_loaded) return RG_ENOTLOADED;
+    CK(cuModuleLoad(&g_mod_dt, detrend_cubin));
+    CK(cuModuleGetFunction(&g_detrend, g_mod_dt, "_Z17detrend_normalisePfi"));
+    CK(cuModuleLoad(&g_mod_rfi, rfi_cubin));
+    CK(cuModuleGetFunction(&g_rfi, g_mod_rfi, "_Z12rfi_clippingPfS_ii"));
+    g_proto_loaded = 1;
+    return RG_OK;
+}
+
+/* detrend_normalise launched as detrend.cu:139: grid (nsamp/len, ndms), 256 threads, on
+ * y [ndms][nsamp] in place.  Every index the kernel forms, blockIdx.y*gridDim.x*len +
+ * blockIdx.x*len + i with i < len, stays below ndms*nsamp when nsamp is a multiple of len;
+ * its int index needs ndms*nsamp < 2^31. */
+int rg_detrend(float *y, int ndms, int nsamp, int len, float *kernel_ms)
+{
+    if (!g_proto_loaded) return RG_ENOTLOADED;
+    if (len <= 0 || nsamp <= 0 || ndms <= 0 || nsamp % len != 0 ||
+        (long)ndms * nsamp >= 2147483647L || nsamp / len > 2147483647 || ndms > 65535) {
+        snprintf(g_err, sizeof g_err, "detrend: shape %d x %d, len %d not launchable", ndms,
+                 nsamp, len);
+        return RG_EBOUNDS;
+    }
+    size_t bytes = (size_t)ndms * (size_t)nsamp * sizeof(float);
+    CUdeviceptr d;
+    CK(cuMemAlloc(&d, bytes));
+    CK(cuMemcpyHtoD(d, y, bytes));
+    int a_len = len;
+    void *args[] = {&d, &a_len};
+    CUevent e0, e1;
+    int rc;
+    if ((rc = timed_begin(&e0, &e1))) return rc;
+    if ((rc = launch(g_detrend, (unsigned)(nsamp / len), (unsigned)ndms, 256, 1, 0, args)))
+        return rc;
+    if ((rc = timed_end(e0, e1, kernel_ms))) return rc;
+    CK(cuMemcpyDtoH(y, d, bytes));
+    CK(cuMemFree(d));
+    return RG_OK;
+}
+
+/* rfi_clipping launched as rfi_clipper.cu:135: grid (1, nrows), blockdim threads, blockdim*4
+ * bytes of dynamic shared memory, on x [nrows][nsamp] in place; means[nrows] receives the row
+ * means.  The kernel's clip loop calls __syncthreads() once per iteration, so every thread
+ * must run the same number of iterations: nsamp must be a multiple of blockdim (refused
+ * otherwise).  Its static shared array holds 1024 entries, one per thread. */
+int rg_rfi_clip(float *x, int nrows, int nsamp, int blockdim, float *means, float *kernel_ms)
+{
+    if (!g_proto_loaded) return RG_ENOTLOADED;
+    if (blockdim <= 0 || blockdim > 1024 || (blockdim & 31) || nsamp <= 0 || nrows <= 0 ||
+        nsamp % blockdim != 0 || nrows > 65535 || (long)nrows * nsamp >= 2147483647L) {
+        snprintf(g_err, sizeof g_err, "rfi: %d rows x %d, %d threads not launchable", nrows,
+                 nsamp, blockdim);
+        return RG_EBOUNDS;
+    }
+    size_t bytes = (size_t)nrows * (size_t)nsamp * sizeof(float);
+    CUdeviceptr d, dm;
+    CK(cuMemAlloc(&d, bytes));
+    CK(cuMemAlloc(&dm, (size_t)nrows * sizeof(float)));
+    CK(cuMemcpyHtoD(d, x, bytes));
+    CK(cuMemsetD8(dm, 0, (size_t)nrows * sizeof(float)));
+    int a_n = nsamp, a_r = nrows;
+    void *args[] = {&d, &dm, &a_n, &a_r};
+    CUevent e0, e1;
+    int rc;
+    if ((rc = timed_begin(&e0, &e1))) return rc;
+    if ((rc = launch(g_rfi, 1, (unsigned)nrows, (unsigned)blockdim, 1, (unsigned)blockdim * 4,
+                     args)))
+        return rc;
+    if ((rc = timed_end(e0, e1, kernel_ms))) return rc;
+    CK(cuMemcpyDtoH(x, d, bytes));
+    CK(cuMemcpyDtoH(means, dm, (size_t)nrows * sizeof(float)));
+    CK(cuMemFree(d));
+    CK(cuMemFree(dm));
+    return RG_OK;
+}

@@ -95,3 +95,35 @@ def random_pulses(rng, n, nsamp, dm_max, sigma, nchans, widths=(1, 64), snr=(8, 
         t0 = int(rng.integers(0, max(1, nsamp - w)))
         out.append((t0, dm, w, amp))
     return out
+
+
+def cfg3(dtype, nchans, ncols, seed=0, fch1=1500.0, bw=300.0, tsamp=64e-6, pulses=(),
+         impulse_frac=0.01, impulse_sigma=50.0, nb_channels=20, nb_sigma=10.0):
+    """Config 3's block: Gaussian samples (uint8: mean 128, sigma 16; int16: mean 0, sigma
+    1000), broadband impulses of impulse_sigma on impulse_frac of the time samples (all
+    channels), sinusoids of amplitude nb_sigma in nb_channels random channels, and dispersed
+    boxcar pulses (t0, dm, width, amplitude per channel).  Integer samples saturate.  Returns
+    (x, meta) with the impulse columns and narrowband channels in meta."""
+    rng = np.random.default_rng(seed)
+    if dtype == "u8":
+        x = gaussian_u8(nchans, ncols, seed)
+        mean, sigma, lo, hi = 128.0, 16.0, 0, 255
+    elif dtype == "i16":
+        x = gaussian_i16(nchans, ncols, seed)
+        mean, sigma, lo, hi = 0.0, 1000.0, -32768, 32767
+    else:
+        raise ValueError(dtype)
+    foff = -float(bw) / nchans
+    inject(x, fch1, foff, tsamp, pulses)
+    cols = np.sort(rng.choice(ncols, max(1, int(round(impulse_frac * ncols))), replace=False))
+    imp = int(round(impulse_sigma * sigma))
+    x[:, cols] = np.clip(x[:, cols].astype(np.int64) + imp, lo, hi).astype(x.dtype)
+    chans = np.sort(rng.choice(nchans, nb_channels, replace=False))
+    t = np.arange(ncols, dtype=np.float64)
+    for c in chans:
+        period = float(rng.uniform(8.0, 200.0))
+        ph = float(rng.uniform(0, 2 * np.pi))
+        s = np.rint(nb_sigma * sigma * np.sin(2 * np.pi * t / period + ph)).astype(np.int64)
+        x[c] = np.clip(x[c].astype(np.int64) + s, lo, hi).astype(x.dtype)
+    return x, dict(fch1=fch1, foff=foff, tsamp=tsamp, impulse_cols=cols, nb_channels=chans,
+                   mean=mean, sigma=sigma)

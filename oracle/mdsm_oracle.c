@@ -518,59 +518,92 @@ void orc_series_stats_int(const double *y, long n, double *mean, double *sigma)
     *sigma = var > 0.0 ? sqrt(var) : 0.0;
 }
 
+/* One DM row of orc_boxcar_detect; returns the candidates found, appended to *out (grown). */
+typedef struct { int32_t samp, width; float snr; } BoxCand;
+
+static long boxcar_row(const double *yr, long n, int nw, float thr, int is_int, float *B,
+                       float *best, int *bw, BoxCand **out, long *capo)
+{
+    double mu, sig;
+    if (is_int)
+        orc_series_stats_int(yr, n, &mu, &sig);
+    else
+        orc_series_stats(yr, n, &mu, &sig);
+    if (!(sig > 0.0)) return 0;
+    const float mu_f = (float)mu;
+    for (long t = 0; t < n; t++) B[t] = (float)yr[t];
+    for (long t = 0; t < n; t++) { best[t] = -INFINITY; bw[t] = 0; }
+    for (int l = 0; l < nw; l++) {
+        long w = 1L << l;
+        if (l > 0) {
+            long h = w / 2;
+            for (long t = 0; t + w <= n; t++) B[t] = B[t] + B[t + h];
+        }
+        const float wm = (float)w * mu_f;
+        const float inv = (float)(1.0 / (sig * sqrt((double)w)));
+        for (long t = 0; t + w <= n; t++) {
+            const float s = (B[t] - wm) * inv;
+            if (s > best[t]) { best[t] = s; bw[t] = (int)w; }
+        }
+    }
+    long cnt = 0;
+    for (long t = 0; t < n; t++) {
+        if (!(best[t] >= thr)) continue;
+        long h = bw[t] / 2 > 1 ? bw[t] / 2 : 1;
+        int keep = 1;
+        long lo = t - h < 0 ? 0 : t - h, hi = t + h > n - 1 ? n - 1 : t + h;
+        for (long u = lo; u < t && keep; u++) if (!(best[u] < best[t])) keep = 0;
+        for (long u = t + 1; u <= hi && keep; u++) if (!(best[u] <= best[t])) keep = 0;
+        if (!keep) continue;
+        if (cnt == *capo) {
+            *capo = *capo ? 2 * *capo : 64;
+            *out = (BoxCand *)realloc(*out, sizeof(BoxCand) * (size_t)*capo);
+        }
+        (*out)[cnt].samp = (int32_t)t;
+        (*out)[cnt].width = bw[t];
+        (*out)[cnt].snr = best[t];
+        cnt++;
+    }
+    return cnt;
+}
+
 long orc_boxcar_detect(const double *y, int ndms, long n, int nw, double threshold,
                        int32_t *dm_idx, int32_t *samp, int32_t *width, float *snr, long cap,
                        int is_int)
 {
-    long total = 0;
-    float *B = (float *)malloc(sizeof(float) * (size_t)n);
-    float *best = (float *)malloc(sizeof(float) * (size_t)n);
-    int *bw = (int *)malloc(sizeof(int) * (size_t)n);
     const float thr = (float)threshold;
-    for (int d = 0; d < ndms; d++) {
-        const double *yr = y + (long)d * n;
-        double mu, sig;
-        if (is_int)
-            orc_series_stats_int(yr, n, &mu, &sig);
-        else
-            orc_series_stats(yr, n, &mu, &sig);
-        if (!(sig > 0.0)) continue;
-        const float mu_f = (float)mu;
-        for (long t = 0; t < n; t++) B[t] = (float)yr[t];
-        for (long t = 0; t < n; t++) { best[t] = -INFINITY; bw[t] = 0; }
-        for (int l = 0; l < nw; l++) {
-            long w = 1L << l;
-            if (l > 0) {
-                long h = w / 2;
-                for (long t = 0; t + w <= n; t++) B[t] = B[t] + B[t + h];
-            }
-            const float wm = (float)w * mu_f;
-            const float inv = (float)(1.0 / (sig * sqrt((double)w)));
-            for (long t = 0; t + w <= n; t++) {
-                const float s = (B[t] - wm) * inv;
-                if (s > best[t]) { best[t] = s; bw[t] = (int)w; }
-            }
+    BoxCand **rows = (BoxCand **)calloc((size_t)(ndms > 0 ? ndms : 1), sizeof(BoxCand *));
+    long *cnt = (long *)calloc((size_t)(ndms > 0 ? ndms : 1), sizeof(long));
+    /* rows are independent: one per thread at a time, each with its own work arrays */
+#pragma omp parallel
+    {
+        float *B = (float *)malloc(sizeof(float) * (size_t)n);
+        float *best = (float *)malloc(sizeof(float) * (size_t)n);
+        int *bw = (int *)malloc(sizeof(int) * (size_t)n);
+#pragma omp for schedule(dynamic, 1)
+        for (int d = 0; d < ndms; d++) {
+            long capo = 0;
+            cnt[d] = boxcar_row(y + (long)d * n, n, nw, thr, is_int, B, best, bw, &rows[d], &capo);
         }
-        for (long t = 0; t < n; t++) {
-            if (!(best[t] >= thr)) continue;
-            long h = bw[t] / 2 > 1 ? bw[t] / 2 : 1;
-            int keep = 1;
-            long lo = t - h < 0 ? 0 : t - h, hi = t + h > n - 1 ? n - 1 : t + h;
-            for (long u = lo; u < t && keep; u++) if (!(best[u] < best[t])) keep = 0;
-            for (long u = t + 1; u <= hi && keep; u++) if (!(best[u] <= best[t])) keep = 0;
-            if (!keep) continue;
+        free(B);
+        free(best);
+        free(bw);
+    }
+    long total = 0;
+    for (int d = 0; d < ndms; d++) {
+        for (long i = 0; i < cnt[d]; i++) {
             if (total < cap) {
                 dm_idx[total] = d;
-                samp[total] = (int32_t)t;
-                width[total] = bw[t];
-                snr[total] = best[t];
+                samp[total] = rows[d][i].samp;
+                width[total] = rows[d][i].width;
+                snr[total] = rows[d][i].snr;
             }
             total++;
         }
+        free(rows[d]);
     }
-    free(B);
-    free(best);
-    free(bw);
+    free(rows);
+    free(cnt);
     return total;
 }
 

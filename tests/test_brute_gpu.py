@@ -108,7 +108,14 @@ def test_pipelined_host_path(lib, orc, cuda, dtype, nsamp):
 
 
 def test_cfg1_full_size_bitexact_and_fp64_error(lib, orc, cuda):
-    """Config 1 at full size: 256 ch x 32768 float samples, 500 DMs 0-99.8."""
+    """Config 1 at full size: 256 ch x 32768 float samples, 500 DMs 0-99.8.  Bit-identical to
+    the reference kernels' float arithmetic (the oracle), and against FP64:
+    * normwise error max |y32 - y64| / sum_c |x| (the error relative to the summation's own
+      scale, which bounds sequential FP32 summation), required below 1e-6;
+    * elementwise relative error max |y32 - y64| / |y64| over outputs with |y64| > 1e-3 sum_c
+      |x|, printed: the reference's sequential FP32 order makes it ~1e-4 on sums of N(0,1)
+      samples that cancel to 1e-3 of their scale, so no 1e-6 bound holds elementwise for this
+      input type (integer samples take the exact INT32 or compensated FP32 sums instead)."""
     import mdsm_gb300 as m
     from mdsm_gb300 import synth
     torch = cuda
@@ -122,10 +129,13 @@ def test_cfg1_full_size_bitexact_and_fp64_error(lib, orc, cuda):
     want = orc.dedisperse(x, S, nsamp)
     assert np.array_equal(got, want)
     y64 = orc.dedisperse(x, S, nsamp, out="f64")
-    # FP32 error against FP64, relative to the summation scale sum_c |x|
     scale = orc.dedisperse(np.abs(x), S, nsamp, out="f64")
-    rel = np.abs(got.astype(np.float64) - y64) / scale
-    assert rel.max() < 2e-6
+    err = np.abs(got.astype(np.float64) - y64)
+    rel = err / scale
+    big = np.abs(y64) > 1e-3 * scale
+    elem = (err[big] / np.abs(y64[big])).max()
+    print("cfg1 FP32: normwise %.3g, elementwise %.3g" % (rel.max(), elem))
+    assert rel.max() < 1e-6
 
 
 @pytest.mark.parametrize("nchans,nsamp,ndms", [(4096, 2000, 40), (257, 511, 33), (9, 4, 1),

@@ -180,6 +180,13 @@ mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_
                                  void *h_out, void *stream);
 /* Number of kernels the last dedisperse call on this plan launched. */
 int mdsm_plan_last_launches(const mdsm_plan *plan);
+/* Profiling (no counterpart in the reference): with stage timing on, every
+ * mdsm_dedisperse_device call records CUDA events on its stream before the first stage and
+ * after each stage (mdsm_plan_stage_info numbers them; a pass's downsampling counts with its
+ * first stage).  mdsm_plan_stage_times waits for the last call's final event and writes up to
+ * cap stage durations in milliseconds, *n = the number of stages timed. */
+mdsm_status mdsm_plan_set_stage_timing(mdsm_plan *plan, int on);
+mdsm_status mdsm_plan_stage_times(mdsm_plan *plan, float *ms, int cap, int *n);
 
 /* ---------------------------------------------------------------------------------------- */
 /* RFI clipping (src/prototypes/rfi_clipper.cu:8-67): per-channel then per-spectrum.          */

@@ -150,6 +150,9 @@ SIGNATURES = {
                                              _vp]),
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
+    "mdsm_plan_set_stage_timing": (_st, [_vp, _i]),
+    "mdsm_plan_stage_times": (_st, [_vp, ctypes.POINTER(ctypes.c_float), _i,
+                                    ctypes.POINTER(_i)]),
     "mdsm_singlepulse_detect_device": (_st, [_vp, _i, _i, _i, _i, _i, _i, _d,
                                              ctypes.POINTER(Candidate), _ll, ctypes.POINTER(_ll),
                                              _vp]),

@@ -71,6 +71,18 @@ class _PlanBase:
     def last_launches(self):
         return load().mdsm_plan_last_launches(self._h)
 
+    def set_stage_timing(self, on=True):
+        """Record CUDA events around every stage of each dedisperse_device call."""
+        check(load().mdsm_plan_set_stage_timing(self._h, int(bool(on))))
+
+    def stage_times(self):
+        """Milliseconds of each stage of the last timed dedisperse_device call."""
+        cap = 64
+        ms = (ctypes.c_float * cap)()
+        n = ctypes.c_int()
+        check(load().mdsm_plan_stage_times(self._h, ms, cap, ctypes.byref(n)))
+        return [float(ms[i]) for i in range(n.value)]
+
     def input_shape(self):
         """(nchans, row pitch) of the device input the plan reads."""
         i = self.info

@@ -47,6 +47,9 @@ void plan_release(Plan &p)
     if (p.d_err) cudaFree(p.d_err);
     for (cudaEvent_t e : p.seg_ev) cudaEventDestroy(e);
     p.seg_ev.clear();
+    for (cudaEvent_t e : p.stage_ev) cudaEventDestroy(e);
+    p.stage_ev.clear();
+    p.stage_ev_used = 0;
     if (p.s_in) cudaStreamDestroy(p.s_in);
     if (p.s_out) cudaStreamDestroy(p.s_out);
     p.s_in = p.s_out = nullptr;
@@ -341,6 +344,37 @@ mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_
 }
 
 int mdsm_plan_last_launches(const mdsm_plan *plan) { return plan ? plan->p.last_launches : 0; }
+
+mdsm_status mdsm_plan_set_stage_timing(mdsm_plan *plan, int on)
+{
+    if (!plan) return fail(MDSM_EINVAL, "null argument");
+    Plan &p = plan->p;
+    if (on && p.stage_ev.size() < p.stages.size() + 1) {
+        while (p.stage_ev.size() < p.stages.size() + 1) {
+            cudaEvent_t e = nullptr;
+            MDSM_CUDA_TRY(cudaEventCreate(&e));
+            p.stage_ev.push_back(e);
+        }
+    }
+    p.stage_timing = on != 0;
+    p.stage_ev_used = 0;
+    return MDSM_OK;
+}
+
+mdsm_status mdsm_plan_stage_times(mdsm_plan *plan, float *ms, int cap, int *n)
+{
+    if (!plan || !n) return fail(MDSM_EINVAL, "null argument");
+    Plan &p = plan->p;
+    *n = 0;
+    if (p.stage_ev_used < 2) return fail(MDSM_ESTATE, "no timed device-path call on this plan");
+    MDSM_CUDA_TRY(cudaEventSynchronize(p.stage_ev[(size_t)p.stage_ev_used - 1]));
+    const int k = p.stage_ev_used - 1;
+    for (int i = 0; i < k && i < cap; ++i)
+        MDSM_CUDA_TRY(cudaEventElapsedTime(&ms[i], p.stage_ev[(size_t)i],
+                                           p.stage_ev[(size_t)i + 1]));
+    *n = k;
+    return MDSM_OK;
+}
 
 mdsm_status mdsm_rfi_clip_device(void *d_x, int dtype, int nchans, long long stride,
                                  long long len, double k_chan, double k_spec, void *stream)

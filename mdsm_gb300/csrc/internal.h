@@ -150,6 +150,11 @@ struct Plan {
     unsigned *d_err = nullptr;
     int last_launches = 0;
     long long in_stride = 0;         // device pitch for the host path
+    // optional per-stage timing of device-path calls: events before the first stage and after
+    // each stage (a subband pass's downsampling belongs to its first stage)
+    bool stage_timing = false;
+    std::vector<cudaEvent_t> stage_ev;
+    int stage_ev_used = 0;
 };
 
 mdsm_status plan_in_requirements(const Plan &p, long long in_stride, long long *in_bytes);

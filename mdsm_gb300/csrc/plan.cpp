@@ -436,9 +436,17 @@ mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size
                                      " bytes; the plan reads up to " + std::to_string(need));
     if (out_stride < p.nsamp) return fail(MDSM_ERANGE, "output row pitch smaller than nsamp");
     p.last_launches = 0;
+    p.stage_ev_used = 0;
+    const bool timed = p.stage_timing && p.stage_ev.size() >= p.stages.size() + 1;
+    auto mark = [&]() -> mdsm_status {
+        if (timed) MDSM_CUDA_TRY(cudaEventRecord(p.stage_ev[(size_t)p.stage_ev_used++], st));
+        return MDSM_OK;
+    };
+    MDSM_TRY(mark());
     if (p.kind == 1) {
-        return launch_stage(p.stages[0], d_in, in_stride, 0, d_out, out_stride, 0, p.d_err, st,
-                            &p.last_launches);
+        MDSM_TRY(launch_stage(p.stages[0], d_in, in_stride, 0, d_out, out_stride, 0, p.d_err, st,
+                              &p.last_launches));
+        return mark();
     }
     const size_t osz = 4;
     for (size_t i = 0; i < p.stages.size(); i += 2) {
@@ -457,9 +465,11 @@ mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size
         }
         MDSM_TRY(launch_stage(g1, src, pitch, g1.in_group_stride * pitch, p.d_work,
                               g1.out_stride, g1.out_group_stride, p.d_err, st, &p.last_launches));
+        MDSM_TRY(mark());
         void *o = static_cast<char *>(d_out) + (size_t)p.pass_row0[i / 2] * out_stride * osz;
         MDSM_TRY(launch_stage(g2, p.d_work, g2.in_stride, g2.in_group_stride, o, out_stride,
                               (long long)g2.ndms * out_stride, p.d_err, st, &p.last_launches));
+        MDSM_TRY(mark());
     }
     return MDSM_OK;
 }

@@ -166,7 +166,9 @@ mdsm_status mdsm_subband_shift_tables(const mdsm_subband_desc *desc, int pass, i
 /* Dedisperse one block on the device.  d_in: channel-major with row pitch in_stride elements
  * (>= nsamp + maxshift, a multiple of 16 bytes) and in_bytes readable bytes (>= info.in_bytes).
  * d_out: [ndms] rows of out_stride elements.  Replaces call_dedisperse's kernel dispatch
- * (src/mdsm/dedispersion_wrapper.cu:7-9 -> dedispersion_thread.cu:332-341). */
+ * (src/mdsm/dedispersion_wrapper.cu:7-9 -> dedispersion_thread.cu:332-341).  Asynchronous on
+ * stream: a device-side wait that ran out (the kernels' waits are bounded; the block's results
+ * are then invalid) is reported by the next mdsm_plan_check. */
 mdsm_status mdsm_dedisperse_device(mdsm_plan *plan, const void *d_in, long long in_stride,
                                    size_t in_bytes, void *d_out, long long out_stride,
                                    void *stream);
@@ -178,6 +180,18 @@ mdsm_status mdsm_dedisperse_device(mdsm_plan *plan, const void *d_in, long long 
  * let the copies run at full speed.  Results do not depend on the segmentation. */
 mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_in_stride,
                                  void *h_out, void *stream);
+/* Synchronises stream and reports device-side failures of the plan's calls since the last
+ * check: MDSM_ETIMEOUT when a bounded device-side wait ran out (the kernel returned early and
+ * the results of those calls are invalid), else MDSM_OK.  Clears the record; the plan stays
+ * usable.  (The host-buffer entry point checks by itself.) */
+mdsm_status mdsm_plan_check(mdsm_plan *plan, void *stream);
+/* Test hook for the failure path (no counterpart in the reference): on stream, a one-block
+ * kernel whose single bounded wait -- the mbarrier wait the dedispersion kernels use, with
+ * spin_limit (1..65536) try_waits instead of their 2^22 -- waits on a barrier that nothing
+ * arrives at.  The wait runs out, the kernel records the timeout in the plan's device error
+ * word and returns, so the next mdsm_plan_check returns MDSM_ETIMEOUT; no fault, trap or hang
+ * is involved and the plan works as before afterwards. */
+mdsm_status mdsm_plan_wait_selftest(mdsm_plan *plan, unsigned spin_limit, void *stream);
 /* Number of kernels the last dedisperse call on this plan launched. */
 int mdsm_plan_last_launches(const mdsm_plan *plan);
 /* Profiling (no counterpart in the reference): with stage timing on, every

@@ -71,6 +71,14 @@ class _PlanBase:
     def last_launches(self):
         return load().mdsm_plan_last_launches(self._h)
 
+    def check(self, stream=None):
+        """Synchronise and raise if a device-side wait of an earlier call ran out."""
+        check(load().mdsm_plan_check(self._h, _stream_ptr(stream)))
+
+    def wait_selftest(self, spin_limit=4096, stream=None):
+        """Run the bounded-wait self-test kernel (its wait runs out on purpose)."""
+        check(load().mdsm_plan_wait_selftest(self._h, int(spin_limit), _stream_ptr(stream)))
+
     def set_stage_timing(self, on=True):
         """Record CUDA events around every stage of each dedisperse_device call."""
         check(load().mdsm_plan_set_stage_timing(self._h, int(bool(on))))

@@ -345,6 +345,20 @@ mdsm_status mdsm_dedisperse_host(mdsm_plan *plan, const void *h_in, long long h_
 
 int mdsm_plan_last_launches(const mdsm_plan *plan) { return plan ? plan->p.last_launches : 0; }
 
+mdsm_status mdsm_plan_check(mdsm_plan *plan, void *stream)
+{
+    if (!plan) return fail(MDSM_EINVAL, "null argument");
+    return check_err_word(plan->p.d_err, static_cast<cudaStream_t>(stream));
+}
+
+mdsm_status mdsm_plan_wait_selftest(mdsm_plan *plan, unsigned spin_limit, void *stream)
+{
+    if (!plan) return fail(MDSM_EINVAL, "null argument");
+    if (spin_limit == 0 || spin_limit > (1u << 16))
+        return fail(MDSM_EINVAL, "wait self-test: spin limit must be 1..65536");
+    return wait_selftest(plan->p.d_err, spin_limit, static_cast<cudaStream_t>(stream));
+}
+
 mdsm_status mdsm_plan_set_stage_timing(mdsm_plan *plan, int on)
 {
     if (!plan) return fail(MDSM_EINVAL, "null argument");

@@ -1198,4 +1198,26 @@ void batch_release(BatchState &b)
     b.nitems = 0;
 }
 
+// Self-test of the bounded-wait path: thread 0 waits, with the wait the kernels above use, on
+// an mbarrier nothing arrives at; after `limit` try_waits the wait gives up, records
+// ERR_WAIT_TIMEOUT in *err as a starved wait in a dedispersion kernel would, and the kernel
+// returns.  No copy is in flight, so nothing writes the barrier's shared memory afterwards.
+__global__ void k_wait_selftest(unsigned *err, uint32_t limit)
+{
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) mbar_wait_bounded(&bar, 0u, err, ERR_WAIT_TIMEOUT, limit);
+}
+
+mdsm_status wait_selftest(unsigned *d_err, unsigned limit, cudaStream_t st)
+{
+    k_wait_selftest<<<1, 32, 0, st>>>(d_err, limit);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return MDSM_OK;
+}
+
 }  // namespace mdsm

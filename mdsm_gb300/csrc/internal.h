@@ -161,6 +161,8 @@ mdsm_status plan_in_requirements(const Plan &p, long long in_stride, long long *
 mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size_t in_bytes,
                             void *d_out, long long out_stride, cudaStream_t st);
 mdsm_status check_err_word(unsigned *d_err, cudaStream_t st);
+// one-block kernel whose bounded wait runs out after `limit` try_waits (dedisp.cu)
+mdsm_status wait_selftest(unsigned *d_err, unsigned limit, cudaStream_t st);
 
 // Float rows [nrows][in_stride] -> uint8 rows [nrows][out_stride] over columns [0, ncols):
 // every value that is bit for bit an integer 0..255 is stored as that integer; any other

@@ -57,11 +57,12 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
     return ok != 0;
 }
 
-// Bounded wait: returns false (and sets `code` in *err) if the phase did not complete.
+// Bounded wait: returns false (and sets `code` in *err) if the phase did not complete within
+// `limit` try_waits.
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity, unsigned *err,
-                                                  unsigned code)
+                                                  unsigned code, uint32_t limit = kMaxWaitIters)
 {
-    for (uint32_t i = 0; i < kMaxWaitIters; ++i)
+    for (uint32_t i = 0; i < limit; ++i)
         if (mbar_try_wait(bar, parity)) return true;
     if (err) atomicOr(err, code);
     return false;

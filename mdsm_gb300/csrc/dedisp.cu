@@ -185,7 +185,7 @@ __global__ void __launch_bounds__(NW * 32) k_shift_sum(KArgs a)
         return;
     }
 
-    const int osz = a.out_i32 ? 4 : 4;
+    const int osz = 4;  // int32 and float32 outputs alike
 #pragma unroll
     for (int j = 0; j < DPW; ++j) {
         const int d = blk * DB + warp * DPW + j;

@@ -47,3 +47,57 @@ def gather_candidates(local, group=None):
     out = [None] * dist.get_world_size(group)
     dist.all_gather_object(out, local, group=group)
     return out
+
+
+class ShardedServer:
+    """The serving form over several GPUs, one process per GPU: every rank builds the same
+    ShardedServer over the full beam list; assign_beams places each beam on one rank by its
+    cost, and each rank adds, feeds and polls only its own beams on a local server (the native
+    mdsm_gb300.serving.Server on the rank's GPU, or anything with its add_beam /
+    add_beam_subband / submit / poll methods).  No sample or series crosses ranks; candidate
+    lists are gathered on the host at the end.
+
+    beam_costs: per global beam, its work (nchans * ndms * nsamp)."""
+
+    def __init__(self, beam_costs, rank, world, make_server):
+        self.rank, self.world = rank, world
+        self.placement = assign_beams(list(beam_costs), world)
+        self.owner = {b: r for r, bs in enumerate(self.placement) for b in bs}
+        self.local = make_server()
+        self._to_local, self._to_global = {}, {}
+
+    def owns(self, beam):
+        return self.owner[beam] == self.rank
+
+    def add_beam(self, beam, *args, subband=False, **kw):
+        """Add global beam `beam` if this rank owns it; returns whether it did."""
+        if not self.owns(beam):
+            return False
+        add = self.local.add_beam_subband if subband else self.local.add_beam
+        lid = add(*args, **kw)
+        self._to_local[beam] = lid
+        self._to_global[lid] = beam
+        return True
+
+    def submit(self, beam, block):
+        """Submit a block of an own beam (others are no-ops returning None with owned False):
+        (owned, ticket or None when admission refused it for now)."""
+        if not self.owns(beam):
+            return False, None
+        return True, self.local.submit(self._to_local[beam], block)
+
+    def poll(self, wait_ms=0):
+        """A finished block of an own beam, with its global beam index, or None."""
+        r = self.local.poll(wait_ms=wait_ms)
+        if r is None:
+            return None
+        r = dict(r)
+        r["beam"] = self._to_global[r["beam"]]
+        return r
+
+    def gather(self, results, group=None):
+        """All ranks' results (lists of poll() dicts) merged on every rank, ordered by
+        (beam, block)."""
+        parts = gather_candidates(list(results), group=group)
+        merged = [r for part in parts for r in part]
+        return sorted(merged, key=lambda r: (r["beam"], r["block"]))

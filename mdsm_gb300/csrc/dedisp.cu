@@ -31,17 +31,6 @@
 
 namespace mdsm {
 
-struct KArgs {
-    const unsigned char *in;
-    long long in_stride, in_group_stride;    // elements
-    unsigned char *out;
-    long long out_stride, out_group_stride;  // elements
-    const int32_t *rel;                      // [g][blk][c][DB]
-    const int32_t *sminspan;                 // [g][blk][c][2]
-    int nchans, ndms, nsamp, nblk, rowcap, nst, out_i32;
-    int ps;  // packed kernels: bytes per phase copy of a staged row
-    unsigned *err;
-};
 
 __device__ __forceinline__ unsigned warp_sum_u32(unsigned v)
 {
@@ -308,6 +297,7 @@ struct OnePlanItems {
         return make_int4(0, blk, rest % ntiles, rest / ntiles);
     }
     __device__ const KArgs &args(int) const { return *a; }
+    __device__ void stored(int) const {}
 };
 
 // Items of several plans from a list, taken from a global counter.
@@ -323,6 +313,7 @@ struct ListItems {
     }
     __device__ int4 item(int it) const { return items[it]; }
     __device__ const KArgs &args(int beam) const { return beams[beam]; }
+    __device__ void stored(int) const {}
 };
 
 // The odd samples of a word as 32-bit lanes: uint8, (s1, s3) as uint16 lanes; uint16, s1.
@@ -607,6 +598,8 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             if (d >= a.ndms) continue;
             unsigned char *orow =
                 a.out + (size_t)(w.w * a.out_group_stride + (long long)d * a.out_stride) * osz;
+            long long m1 = 0;                    // this lane's share of the row's moments
+            unsigned long long m2lo = 0, m2hi = 0;
 #pragma unroll
             for (int r = 0; r < PRW; ++r) {
                 const long long t = t0 + SPW * (lane + 32 * r);
@@ -638,6 +631,17 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
 #pragma unroll
                     for (int e = 0; e < SPW; ++e) v[e] = f[j][r][e];
                 }
+                if (a.mom) {
+#pragma unroll
+                    for (int e = 0; e < SPW; ++e)
+                        if (t + e < a.nsamp) {
+                            const unsigned long long q =
+                                (unsigned long long)((long long)v[e] * (long long)v[e]);
+                            m1 += v[e];
+                            m2lo += q;
+                            m2hi += (m2lo < q);
+                        }
+                }
                 if (whole && a.out_i32) {
                     if constexpr (SPW == 4)
                         *reinterpret_cast<int4 *>(orow + t * 4) = make_int4(v[0], v[1], v[2], v[3]);
@@ -656,7 +660,27 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                         if (t + e < a.nsamp) store_out<int>(orow, (int)(t + e), v[e], a.out_i32);
                 }
             }
+            if (!U16OUT && a.mom) {
+                // the row's share of this item: warp sum (128-bit with carries), then one
+                // atomic per word; integer sums do not depend on their order
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    m1 += __shfl_xor_sync(0xffffffffu, m1, o);
+                    const unsigned long long lo = __shfl_xor_sync(0xffffffffu, m2lo, o);
+                    const unsigned long long hi = __shfl_xor_sync(0xffffffffu, m2hi, o);
+                    const unsigned long long nl = m2lo + lo;
+                    m2hi += hi + (nl < m2lo);
+                    m2lo = nl;
+                }
+                if (lane == 0) {
+                    unsigned long long *mp = a.mom + 3 * (size_t)(w.w * a.mom_group_rows + d);
+                    atomicAdd(mp, (unsigned long long)m1);
+                    const unsigned long long old = atomicAdd(mp + 1, m2lo);
+                    atomicAdd(mp + 2, m2hi + (old + m2lo < old ? 1ull : 0ull));
+                }
+            }
         }
+        src.stored(w.x);  // this warp's rows of the item are written
     }
     if (aborted) {
         // let the copies already issued land before the CTA exits (bounded as well)
@@ -960,7 +984,8 @@ long long stage_in_bytes(const StageGeom &g, long long in_stride, long long in_g
 mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride,
                          long long in_group_stride, void *out, long long out_stride,
                          long long out_group_stride, unsigned *d_err, cudaStream_t st,
-                         int *launches, long long nsamp_run)
+                         int *launches, long long nsamp_run, unsigned long long *mom,
+                         long long mom_group_rows)
 {
     const int SZ = (int)dtype_size(g.in_dtype);
     const long long nsamp = nsamp_run >= 0 ? std::min<long long>(nsamp_run, g.nsamp) : g.nsamp;
@@ -1015,6 +1040,8 @@ mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride
     a.out_i32 = g.out_i32;
     a.ps = g.ps;
     a.err = d_err;
+    a.mom = (mom && stage_folds_moments(g)) ? mom : nullptr;
+    a.mom_group_rows = mom_group_rows;
     const long long ntiles = (nsamp + g.T - 1) / g.T;
     if (persistent) {
         // at most one CTA per SM walks the (DM block, tile, group) items

@@ -934,6 +934,23 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
     return fetch_cands(d_c, d_count, cap, h_cands, ncand, st);
 }
 
+// (mean, sigma) of int32 series from their exact moments folded into the dedispersion store
+// (sum, sum of squares as two 64-bit words): the same conversion as k_series_stats_int's.
+__global__ void k_mom_finish(const unsigned long long *__restrict__ mom, int ndms, long long n,
+                             double2 *__restrict__ musig)
+{
+    const int d = blockIdx.x * blockDim.x + threadIdx.x;
+    if (d >= ndms) return;
+    const long long s1 = (long long)mom[3 * (size_t)d];
+    const unsigned long long lo = mom[3 * (size_t)d + 1], hi = mom[3 * (size_t)d + 2];
+    const double e2 = __ddiv_rn(__dadd_rn(__dmul_rn((double)hi, 18446744073709551616.0),
+                                          (double)lo),
+                                (double)n);
+    const double m = __ddiv_rn((double)s1, (double)n);
+    const double var = __dadd_rn(e2, -__dmul_rn(m, m));
+    musig[d] = make_double2(m, var > 0.0 ? __dsqrt_rn(var) : 0.0);
+}
+
 // Bytes of device work area boxcar_launch needs.
 size_t boxcar_work_bytes(int ndms, int nsamp, long long cap)
 {
@@ -948,7 +965,8 @@ size_t boxcar_work_bytes(int ndms, int nsamp, long long cap)
 // the device record layout until devcand_to_candidate() puts it in mdsm_candidate order).
 mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
                           double threshold, void *d_work, size_t work_bytes, long long cap,
-                          mdsm_candidate *h_cands, long long *h_count, cudaStream_t st)
+                          mdsm_candidate *h_cands, long long *h_count, cudaStream_t st,
+                          const unsigned long long *mom)
 {
     if (dtype != MDSM_OUT_F32 && dtype != MDSM_OUT_I32)
         return fail(MDSM_EINVAL, "boxcar detector: series must be float32 or int32");
@@ -974,7 +992,10 @@ mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, 
                                     st));
     } else {
         const int32_t *y = static_cast<const int32_t *>(d_series);
-        k_series_stats_int<<<ndms, 256, 0, st>>>(y, nsamp, d_ms);
+        if (mom)  // moments already folded into the series' store: no pass over the series
+            k_mom_finish<<<(ndms + 127) / 128, 128, 0, st>>>(mom, ndms, nsamp, d_ms);
+        else
+            k_series_stats_int<<<ndms, 256, 0, st>>>(y, nsamp, d_ms);
         MDSM_CUDA_TRY(launch_boxcar(y, ndms, nsamp, nwidths, threshold, d_ms, d_c, d_count, cap,
                                     st));
     }

@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <mutex>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -38,6 +39,30 @@ enum : unsigned {
 };
 
 size_t dtype_size(int dtype);
+
+// candidate record as the device kernels write it
+struct DevCand {
+    int32_t dm_idx, sample, width;
+    float snr;
+};
+
+// arguments of one beam / stage of the shift-and-sum kernels (dedisp.cu)
+struct KArgs {
+    const unsigned char *in;
+    long long in_stride, in_group_stride;    // elements
+    unsigned char *out;
+    long long out_stride, out_group_stride;  // elements
+    const int32_t *rel;                      // [g][blk][c][DB]
+    const int32_t *sminspan;                 // [g][blk][c][2]
+    int nchans, ndms, nsamp, nblk, rowcap, nst, out_i32;
+    int ps;  // packed kernels: bytes per phase copy of a staged row
+    unsigned *err;
+    // optional (packed kernels, int32 output): exact moments of every output row, accumulated
+    // as the row is stored -- (sum, sum of squares low 64 bits, high 64 bits) per row at
+    // mom + 3 * (group * mom_group_rows + row)
+    unsigned long long *mom;
+    long long mom_group_rows;
+};
 
 // ----------------------------------------------------------------------------------------
 // one launch of the generic shift-and-sum kernel: out[g][d][t] = sum_c in[g][c][t + S[g][d][c]]
@@ -82,10 +107,17 @@ long long stage_in_bytes(const StageGeom &g, long long in_stride, long long in_g
 // Launch the stage kernel.  Returns number of kernels launched via *launches.
 // nsamp_run >= 0 computes only output samples [0, nsamp_run) (a time segment of the block,
 // with in/out already offset to its first sample); -1 computes all g.nsamp.
+// mom (optional): exact row moments of int32 output accumulated by the packed kernels as they
+// store (see KArgs); ignored by the generic kernel (stage_folds_moments tells which).
 mdsm_status launch_stage(const StageGeom &g, const void *in, long long in_stride,
                          long long in_group_stride, void *out, long long out_stride,
                          long long out_group_stride, unsigned *d_err, cudaStream_t st,
-                         int *launches, long long nsamp_run = -1);
+                         int *launches, long long nsamp_run = -1,
+                         unsigned long long *mom = nullptr, long long mom_group_rows = 0);
+inline bool stage_folds_moments(const StageGeom &g)
+{
+    return (g.kernel == 2 || g.kernel == 3) && g.out_i32 && !g.out_u16;
+}
 
 // ----------------------------------------------------------------------------------------
 // batched persistent launch (dedisp.cu)
@@ -158,8 +190,12 @@ struct Plan {
 };
 
 mdsm_status plan_in_requirements(const Plan &p, long long in_stride, long long *in_bytes);
+// mom (optional): [ndms][3] exact moments of every int32 output row (sum, sum of squares as
+// two 64-bit words), zeroed and accumulated on st when every final stage folds them
+// (*folded = true); otherwise left alone (*folded = false).
 mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size_t in_bytes,
-                            void *d_out, long long out_stride, cudaStream_t st);
+                            void *d_out, long long out_stride, cudaStream_t st,
+                            unsigned long long *mom = nullptr, bool *folded = nullptr);
 mdsm_status check_err_word(unsigned *d_err, cudaStream_t st);
 // one-block kernel whose bounded wait runs out after `limit` try_waits (dedisp.cu)
 mdsm_status wait_selftest(unsigned *d_err, unsigned limit, cudaStream_t st);
@@ -179,11 +215,6 @@ int32_t shift_of(float dms, double delay64, float lowdm, float dmstep, int idx, 
 // ----------------------------------------------------------------------------------------
 // detection / rfi launchers (detect.cu, rfi.cu, singlepulse.cu)
 // ----------------------------------------------------------------------------------------
-// candidate record as the device kernels write it
-struct DevCand {
-    int32_t dm_idx, sample, width;
-    float snr;
-};
 // The detectors' grow-only per-device work buffer; the lease holds it until the call returns.
 mdsm_status scratch_get(size_t bytes, void **out, std::unique_lock<std::mutex> *lease);
 // Per-DM (mean, sigma) in double of float32 / int32 series (the boxcar searches' statistics).
@@ -216,9 +247,12 @@ mdsm_status boxcar_detect(const void *d_series, int dtype, int ndms, int nsamp, 
                           double threshold, mdsm_candidate *h_cands, long long cap,
                           long long *ncand, cudaStream_t st);
 size_t boxcar_work_bytes(int ndms, int nsamp, long long cap);
+// mom (optional, int32 series): the rows' exact moments as plan_run_device folds them; the
+// statistics then come from them instead of a pass over the series.
 mdsm_status boxcar_launch(const void *d_series, int dtype, int ndms, int nsamp, int nwidths,
                           double threshold, void *d_work, size_t work_bytes, long long cap,
-                          mdsm_candidate *h_cands, long long *h_count, cudaStream_t st);
+                          mdsm_candidate *h_cands, long long *h_count, cudaStream_t st,
+                          const unsigned long long *mom = nullptr);
 void devcand_to_candidate(mdsm_candidate *c, long long n);
 mdsm_status downsample(const void *in, int in_dtype, int nchans, long long in_stride,
                        long long len, int b, int mode, void *out, int out_dtype,

@@ -427,7 +427,8 @@ mdsm_status plan_in_requirements(const Plan &p, long long in_stride, long long *
 }
 
 mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size_t in_bytes,
-                            void *d_out, long long out_stride, cudaStream_t st)
+                            void *d_out, long long out_stride, cudaStream_t st,
+                            unsigned long long *mom, bool *folded)
 {
     long long need = 0;
     MDSM_TRY(plan_in_requirements(p, in_stride, &need));
@@ -442,10 +443,16 @@ mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size
         if (timed) MDSM_CUDA_TRY(cudaEventRecord(p.stage_ev[(size_t)p.stage_ev_used++], st));
         return MDSM_OK;
     };
+    // row moments folded into the final stages' stores, where all of them can
+    bool fold = mom != nullptr;
+    for (size_t i = p.kind == 1 ? 0 : 1; fold && i < p.stages.size(); i += p.kind == 1 ? 1 : 2)
+        fold = stage_folds_moments(p.stages[i]);
+    if (folded) *folded = fold;
+    if (fold) MDSM_CUDA_TRY(cudaMemsetAsync(mom, 0, (size_t)p.ndms * 3 * sizeof(*mom), st));
     MDSM_TRY(mark());
     if (p.kind == 1) {
         MDSM_TRY(launch_stage(p.stages[0], d_in, in_stride, 0, d_out, out_stride, 0, p.d_err, st,
-                              &p.last_launches));
+                              &p.last_launches, -1, fold ? mom : nullptr, p.ndms));
         return mark();
     }
     const size_t osz = 4;
@@ -468,7 +475,8 @@ mdsm_status plan_run_device(Plan &p, const void *d_in, long long in_stride, size
         MDSM_TRY(mark());
         void *o = static_cast<char *>(d_out) + (size_t)p.pass_row0[i / 2] * out_stride * osz;
         MDSM_TRY(launch_stage(g2, p.d_work, g2.in_stride, g2.in_group_stride, o, out_stride,
-                              (long long)g2.ndms * out_stride, p.d_err, st, &p.last_launches));
+                              (long long)g2.ndms * out_stride, p.d_err, st, &p.last_launches, -1,
+                              fold ? mom + 3 * (size_t)p.pass_row0[i / 2] : nullptr, g2.ndms));
         MDSM_TRY(mark());
     }
     return MDSM_OK;

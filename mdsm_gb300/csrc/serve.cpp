@@ -79,6 +79,8 @@ struct Slot {
     size_t out_bytes = 0;
     void *d_det = nullptr;  // detector work arrays + device candidates
     size_t det_bytes = 0;
+    unsigned long long *d_mom = nullptr;  // the block's row moments, folded into its store
+    size_t mom_bytes = 0;
     mdsm_candidate *h_cands = nullptr;  // pinned
     long long *h_count = nullptr;       // pinned
     bool busy = false;
@@ -265,12 +267,18 @@ bool Server::launch(Slot &s, Pending &job)
         fault = cuda_fail(e, "serving: input copy");
         return false;
     }
-    mdsm_status rc = plan_run_device(p, b.d_buf[cur], b.stride, b.buf_bytes, s.d_out, ns, st);
+    // with the boxcar search, the dedispersion store also folds the rows' exact moments, so
+    // the search's statistics need no pass of their own over the series
+    bool folded = false;
+    unsigned long long *mom = desc.detector == 1 && p.out_dtype == MDSM_OUT_I32 ? s.d_mom : nullptr;
+    mdsm_status rc = plan_run_device(p, b.d_buf[cur], b.stride, b.buf_bytes, s.d_out, ns, st,
+                                     mom, &folded);
     if (rc == MDSM_OK && cudaEventRecord(b.buf_free[cur], st) != cudaSuccess)
         rc = fail(MDSM_ECUDA, "serving: event record");
     if (rc == MDSM_OK && desc.detector == 1)
         rc = boxcar_launch(s.d_out, p.out_dtype, p.ndms, (int)ns, desc.nwidths, desc.threshold,
-                           s.d_det, s.det_bytes, desc.cand_cap, s.h_cands, s.h_count, st);
+                           s.d_det, s.det_bytes, desc.cand_cap, s.h_cands, s.h_count, st,
+                           folded ? mom : nullptr);
     if (rc == MDSM_OK && desc.detector != 1) {
         *s.h_count = 0;
     }
@@ -381,8 +389,15 @@ mdsm_status add_beam(mdsm_server *sv, mdsm_plan *plan, int *beam)
         const size_t det = boxcar_work_bytes(p.ndms, p.nsamp, S.desc.cand_cap);
         if (sl.det_bytes < det) {
             if (sl.d_det) cudaFree(sl.d_det);
+        if (sl.d_mom) cudaFree(sl.d_mom);
             MDSM_CUDA_TRY(cudaMalloc(&sl.d_det, det));
             sl.det_bytes = det;
+        }
+        const size_t mb = (size_t)p.ndms * 3 * sizeof(unsigned long long);
+        if (sl.mom_bytes < mb) {
+            if (sl.d_mom) cudaFree(sl.d_mom);
+            MDSM_CUDA_TRY(cudaMalloc(reinterpret_cast<void **>(&sl.d_mom), mb));
+            sl.mom_bytes = mb;
         }
     }
     {
@@ -606,6 +621,7 @@ void mdsm_server_destroy(mdsm_server *sv)
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.d_out) cudaFree(sl.d_out);
         if (sl.d_det) cudaFree(sl.d_det);
+        if (sl.d_mom) cudaFree(sl.d_mom);
         if (sl.h_cands) cudaFreeHost(sl.h_cands);
         if (sl.h_count) cudaFreeHost(sl.h_count);
     }

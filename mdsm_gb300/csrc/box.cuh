@@ -1,0 +1,269 @@
+// box.cuh -- the boxcar single-pulse search's tile loop as a device function, shared by the
+// standalone search kernel (detect.cu) and the fused batched launch (dedisp.cu).
+//
+// Widths 1, 2, 4, ..., 2^(NW-1); per DM row the mean and sigma come from the caller.  A run of
+// consecutive 2048-sample tiles of one row is searched by THREADS threads of the calling CTA
+// (every thread of the CTA calls box_run: it holds the CTA barriers; threads at or past THREADS
+// only take part in them).  The samples of the next tile are copied into shared memory
+// (cp.async) while the current one is searched.  Arithmetic per sample and width is FP32,
+// explicitly rounded, in the oracle's order; each thread owns the position pairs
+// (2 tid + 2 THREADS q, +1), keeps their boxcar sums and best SNR in registers across the
+// widths and reads only the partner sums B[i + w/2] from shared memory (one 8-byte load per
+// pair), so one width costs per pair one shared load, one shared store, three paired FP32
+// operations, two maxima and one barrier (the sums alternate between two buffers).  Which
+// width gave the best SNR is needed only where the best passes the threshold (few
+// positions): there box_best_at forms it again, with the same sums.  Candidates are local
+// maxima of the best SNR over max(w/2, 1) samples on each side.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "internal.h"
+#include "ptx.cuh"
+
+namespace mdsm {
+
+constexpr int kBoxTile = 2048;   // output samples per tile
+
+// Two FP32 lanes at once (Blackwell add/mul.f32x2, each lane rounded to nearest as the scalar
+// operation would be).
+__device__ __forceinline__ unsigned long long f2_bits(float2 v)
+{
+    return (unsigned long long)__float_as_uint(v.x) |
+           ((unsigned long long)__float_as_uint(v.y) << 32);
+}
+__device__ __forceinline__ float2 bits_f2(unsigned long long v)
+{
+    return make_float2(__uint_as_float((unsigned)v), __uint_as_float((unsigned)(v >> 32)));
+}
+__device__ __forceinline__ float2 add_f2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(d);
+}
+__device__ __forceinline__ float2 mul_f2(float2 a, float2 b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
+    return bits_f2(d);
+}
+
+// Staged samples for NW widths: the region [t0 - HL, t0 + TILE + HL + wmax - 1), rounded up to
+// whole pairs of positions per thread; each sum buffer has wmax floats more so that partner
+// reads past the region stay inside it (those positions feed no kept boxcar).
+template <int NW, int THREADS>
+struct BoxGeom {
+    static constexpr int WMAX = 1 << (NW - 1);
+    static constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
+    static constexpr int SPAN = kBoxTile + 2 * HL + WMAX;  // samples a kept boxcar can touch
+    static constexpr int NBEST = kBoxTile + 2 * HL;        // positions with a best value
+    static constexpr int PAIRS = (SPAN + 2 * THREADS - 1) / (2 * THREADS);  // per thread
+    // floats; even, so the second buffer and the pairs in it stay 8-byte aligned
+    static constexpr int BUF = PAIRS * 2 * THREADS + (WMAX < 2 ? 2 : WMAX);
+    // shared memory of box_run: two sum buffers, the best SNR of NBEST positions, the next
+    // tile's samples
+    static constexpr size_t SMEM =
+        (size_t)BUF * 8 + (size_t)NBEST * 4 + (size_t)PAIRS * 2 * THREADS * 4;
+    static_assert(BUF % 2 == 0 && NBEST % 2 == 0, "pairs of positions");
+    static_assert((THREADS & (THREADS - 1)) == 0, "power-of-two thread count");
+};
+
+// Best SNR over the widths 1, 2, ..., 2^(NW-1) at series position t (0 <= t < n) and the first
+// width reaching it, for a position that passed the threshold.  The sums are formed in the
+// order of the tile loop (B_w[t] = B_{w/2}[t] + B_{w/2}[t + w/2]): a pairwise sum over the
+// samples in order, merging equal-sized partial sums as a binary counter carries, completes
+// the width-w sum exactly when w samples have been added.
+template <typename T, int NW>
+__device__ __noinline__ void box_best_at(const T *__restrict__ r, long long t, long long n,
+                                         float mu_f, const float *inv_w, float *bv, int *bw)
+{
+    float st[NW];
+    int sp = 0;
+    float best = -INFINITY;
+    int width = 0;
+    for (int j = 0; j < (1 << (NW - 1)) && t + j < n; ++j) {
+        st[sp++] = (float)__ldg(r + t + j);
+        for (int k = j + 1; (k & 1) == 0; k >>= 1) {
+            st[sp - 2] = __fadd_rn(st[sp - 2], st[sp - 1]);
+            --sp;
+        }
+        if (((j + 1) & j) == 0) {  // j + 1 = w, a power of two: st[0] is the width-w sum
+            const int w = j + 1;
+            const int l = 31 - __clz(w);
+            const float sv = __fmul_rn(__fadd_rn(st[0], -__fmul_rn((float)w, mu_f)), inv_w[l]);
+            if (sv > best) {
+                best = sv;
+                width = w;
+            }
+        }
+    }
+    *bv = best;
+    *bw = width;
+}
+
+// Asynchronous copy of one tile's samples into NB: this thread's pairs
+// (r0 + 2 tid + 2 THREADS q, +1), zero outside the series.  Only the issuing thread reads
+// them back, so its own wait is the only synchronisation.
+template <typename T, int PAIRS, int THREADS>
+__device__ __forceinline__ void box_prefetch(uint32_t *NB, const T *__restrict__ r, long long r0,
+                                             long long n, int tid)
+{
+    static_assert(sizeof(T) == 4, "4-byte samples");
+#pragma unroll
+    for (int q = 0; q < PAIRS; ++q)
+#pragma unroll
+        for (int e = 0; e < 2; ++e) {
+            const int i = 2 * tid + 2 * THREADS * q + e;
+            const long long t = r0 + i;
+            const bool in = t >= 0 && t < n;
+            cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
+        }
+    cp_async_commit();
+}
+
+template <typename T>
+__device__ __forceinline__ float box_value(uint32_t raw)
+{
+    if constexpr (std::is_same<T, float>::value)
+        return __uint_as_float(raw);
+    else
+        return (float)(int32_t)raw;
+}
+
+// Tiles [tile_lo, tile_hi) of row r (n samples, DM index d) with the row's mean and sigma
+// (sigma > 0); sm holds BoxGeom<NW, THREADS>::SMEM bytes.  Candidates (d, sample, width, snr)
+// go to cands[atomicAdd(count)] below cap.  ALL: the CTA has exactly THREADS threads.  When
+// it returns, no copy is in flight (the last tile prefetches nothing).
+template <typename T, int NW, int THREADS, bool ALL>
+__device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, long long tile_lo,
+                                        long long tile_hi, double mu, double sig, double threshold,
+                                        int d, DevCand *__restrict__ cands,
+                                        unsigned long long *__restrict__ count, long long cap,
+                                        unsigned char *sm)
+{
+    using G = BoxGeom<NW, THREADS>;
+    constexpr int HL = G::HL, NBEST = G::NBEST, PAIRS = G::PAIRS;
+    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
+    float *best_s = B1 + G::BUF;
+    uint32_t *NB = reinterpret_cast<uint32_t *>(best_s + NBEST);  // next tile's samples
+    const bool active = ALL || threadIdx.x < THREADS;
+    // (the mask tells the compiler tid < THREADS, so range tests fold at compile time for all
+    // but the last pair)
+    const int tid = threadIdx.x & (THREADS - 1);
+    const float mu_f = __double2float_rn(mu);
+    const float thr = __double2float_rn(threshold);
+    // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
+    __shared__ float inv_w[NW];
+    if (threadIdx.x < NW)
+        inv_w[threadIdx.x] = __double2float_rn(
+            __ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << threadIdx.x)))));
+    // every staged sample and every boxcar of the tile inside the series: no per-element tests
+    auto inside = [&](long long tile) {
+        const long long r0 = tile * kBoxTile - HL;
+        return r0 >= 0 && r0 + PAIRS * 2 * THREADS <= n;
+    };
+    if (active) box_prefetch<T, PAIRS, THREADS>(NB, r, tile_lo * kBoxTile - HL, n, tid);
+    for (long long tile = tile_lo; tile < tile_hi; ++tile) {
+        const long long t0 = tile * kBoxTile;
+        const long long r0 = t0 - HL;  // series index of B[0] and best[0]
+        const bool interior = inside(tile);
+        float2 b[PAIRS], best[PAIRS];
+        if (active) {
+            cp_async_wait_all();
+#pragma unroll
+            for (int q = 0; q < PAIRS; ++q) {
+                const int i = 2 * tid + 2 * THREADS * q;
+                b[q] = make_float2(box_value<T>(NB[i]), box_value<T>(NB[i + 1]));
+                *reinterpret_cast<float2 *>(B0 + i) = b[q];
+                best[q] = make_float2(-INFINITY, -INFINITY);
+            }
+        }
+        if (active && tile + 1 < tile_hi)  // in flight while this tile is searched
+            box_prefetch<T, PAIRS, THREADS>(NB, r, r0 + kBoxTile, n, tid);
+        __syncthreads();  // B0 written (each thread reads back only its own NB words)
+#pragma unroll
+        for (int l = 0; l < NW; ++l) {
+            const int w = 1 << l;
+            if (l > 0) {
+                // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
+                const int h = w >> 1;
+                const float *cur = (l & 1) ? B0 : B1;
+                float *nxt = (l & 1) ? B1 : B0;
+                if (active) {
+#pragma unroll
+                    for (int q = 0; q < PAIRS; ++q) {
+                        const int i = 2 * tid + 2 * THREADS * q;
+                        // partner sums of positions i and i + 1
+                        const float2 pv = h == 1 ? make_float2(b[q].y, cur[i + 2])
+                                                 : *reinterpret_cast<const float2 *>(cur + i + h);
+                        b[q] = add_f2(b[q], pv);
+                        *reinterpret_cast<float2 *>(nxt + i) = b[q];
+                    }
+                }
+                __syncthreads();
+            }
+            if (active) {
+                const float wm = __fmul_rn((float)w, mu_f);
+                const float inv = inv_w[l];
+#pragma unroll
+                for (int q = 0; q < PAIRS; ++q) {
+                    const int i = 2 * tid + 2 * THREADS * q;
+                    if (i >= NBEST) continue;  // i even and NBEST even: i + 1 < NBEST too
+                    const long long t = r0 + i;
+                    const float2 sv =
+                        mul_f2(add_f2(b[q], make_float2(-wm, -wm)), make_float2(inv, inv));
+                    if (interior) {
+                        best[q].x = fmaxf(best[q].x, sv.x);
+                        best[q].y = fmaxf(best[q].y, sv.y);
+                    } else {
+                        if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
+                        if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
+                    }
+                }
+            }
+        }
+        bool any = false;
+        if (active) {
+#pragma unroll
+            for (int q = 0; q < PAIRS; ++q)
+                if (2 * tid + 2 * THREADS * q < NBEST) any |= best[q].x >= thr || best[q].y >= thr;
+        }
+        // most tiles hold no sample over the threshold: skip the neighbourhood test there
+        if (!__syncthreads_or(any)) continue;
+        if (active) {
+#pragma unroll
+            for (int q = 0; q < PAIRS; ++q) {
+                const int i = 2 * tid + 2 * THREADS * q;
+                if (i < NBEST) *reinterpret_cast<float2 *>(best_s + i) = best[q];
+            }
+        }
+        __syncthreads();
+        if (active) {
+            for (int q = tid; q < kBoxTile; q += THREADS) {
+                const long long t = t0 + q;
+                if (t >= n) break;
+                const int i = q + HL;
+                const float bv = best_s[i];
+                if (!(bv >= thr)) continue;
+                float snr;
+                int width;
+                box_best_at<T, NW>(r, t, n, mu_f, inv_w, &snr, &width);
+                const int h = max(width / 2, 1);
+                bool keep = true;
+                for (int u = 1; u <= h && keep; ++u)
+                    if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
+                for (int u = 1; u <= h && keep; ++u)
+                    if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
+                if (!keep) continue;
+                const unsigned long long at = atomicAdd(count, 1ull);
+                if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, width, snr};
+            }
+        }
+        // (the next tile writes best_s only after its own barriers)
+    }
+}
+
+}  // namespace mdsm

@@ -20,6 +20,7 @@
 #include <type_traits>
 #include <vector>
 
+#include "box.cuh"
 #include "internal.h"
 #include "ptx.cuh"
 
@@ -612,241 +613,24 @@ mdsm_status series_stats_launch(const void *y, int dtype, int ndms, long long n,
     return MDSM_OK;
 }
 
-constexpr int kBoxTile = 2048;   // output samples per CTA
 constexpr int kBoxThreads = 256;
 
-// Two FP32 lanes at once (Blackwell add/mul.f32x2, each lane rounded to nearest as the scalar
-// operation would be).
-__device__ __forceinline__ unsigned long long f2_bits(float2 v)
-{
-    return (unsigned long long)__float_as_uint(v.x) |
-           ((unsigned long long)__float_as_uint(v.y) << 32);
-}
-__device__ __forceinline__ float2 bits_f2(unsigned long long v)
-{
-    return make_float2(__uint_as_float((unsigned)v), __uint_as_float((unsigned)(v >> 32)));
-}
-__device__ __forceinline__ float2 add_f2(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-    return bits_f2(d);
-}
-__device__ __forceinline__ float2 mul_f2(float2 a, float2 b)
-{
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-    return bits_f2(d);
-}
-
-// Staged samples of k_boxcar for NW widths: the region [t0 - HL, t0 + TILE + HL + wmax - 1),
-// rounded up to whole pairs of positions per thread; each sum buffer has wmax floats more so
-// that partner reads past the region stay inside it (those positions feed no kept boxcar).
-template <int NW>
-struct BoxGeom {
-    static constexpr int WMAX = 1 << (NW - 1);
-    static constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
-    static constexpr int SPAN = kBoxTile + 2 * HL + WMAX;  // samples a kept boxcar can touch
-    static constexpr int NBEST = kBoxTile + 2 * HL;        // positions with a best value
-    static constexpr int PAIRS = (SPAN + 2 * kBoxThreads - 1) / (2 * kBoxThreads);  // per thread
-    // floats; even, so the second buffer and the pairs in it stay 8-byte aligned
-    static constexpr int BUF = PAIRS * 2 * kBoxThreads + (WMAX < 2 ? 2 : WMAX);
-    static_assert(BUF % 2 == 0 && NBEST % 2 == 0, "pairs of positions");
-};
-
-// Best SNR over the widths 1, 2, ..., 2^(NW-1) at series position t (0 <= t < n) and the first
-// width reaching it, for a position that passed the threshold.  The sums are formed in the
-// order of the tile loop (B_w[t] = B_{w/2}[t] + B_{w/2}[t + w/2]): a pairwise sum over the
-// samples in order, merging equal-sized partial sums as a binary counter carries, completes
-// the width-w sum exactly when w samples have been added.
-template <typename T, int NW>
-__device__ __noinline__ void box_best_at(const T *__restrict__ r, long long t, long long n,
-                                         float mu_f, const float *inv_w, float *bv, int *bw)
-{
-    float st[NW];
-    int sp = 0;
-    float best = -INFINITY;
-    int width = 0;
-    for (int j = 0; j < (1 << (NW - 1)) && t + j < n; ++j) {
-        st[sp++] = (float)__ldg(r + t + j);
-        for (int k = j + 1; (k & 1) == 0; k >>= 1) {
-            st[sp - 2] = __fadd_rn(st[sp - 2], st[sp - 1]);
-            --sp;
-        }
-        if (((j + 1) & j) == 0) {  // j + 1 = w, a power of two: st[0] is the width-w sum
-            const int w = j + 1;
-            const int l = 31 - __clz(w);
-            const float sv = __fmul_rn(__fadd_rn(st[0], -__fmul_rn((float)w, mu_f)), inv_w[l]);
-            if (sv > best) {
-                best = sv;
-                width = w;
-            }
-        }
-    }
-    *bv = best;
-    *bw = width;
-}
-
-// Asynchronous copy of one tile's samples into NB: this thread's pairs
-// (r0 + 2 tid + 2 kBoxThreads q, +1), zero outside the series.  Only the issuing thread reads
-// them back, so its own wait is the only synchronisation.
-template <typename T, int PAIRS>
-__device__ __forceinline__ void box_prefetch(uint32_t *NB, const T *__restrict__ r, long long r0,
-                                             long long n, int tid)
-{
-    static_assert(sizeof(T) == 4, "4-byte samples");
-#pragma unroll
-    for (int q = 0; q < PAIRS; ++q)
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int i = 2 * tid + 2 * kBoxThreads * q + e;
-            const long long t = r0 + i;
-            const bool in = t >= 0 && t < n;
-            cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
-        }
-    cp_async_commit();
-}
-
-template <typename T>
-__device__ __forceinline__ float box_value(uint32_t raw)
-{
-    if constexpr (std::is_same<T, float>::value)
-        return __uint_as_float(raw);
-    else
-        return (float)(int32_t)raw;
-}
-
-// One CTA per (DM, run of `tpc` consecutive tiles); the samples of the next tile are copied
-// into shared memory (cp.async) while the current one is searched.  Arithmetic per sample and width is FP32
-// (explicitly rounded, same order as the oracle); only the per-DM statistics are FP64.  Each
-// thread owns the position pairs (2 tid + 2 kBoxThreads q, +1): it keeps their boxcar sums and
-// best SNR in registers across the widths and reads only the partner sums B[i + w/2] from
-// shared memory (one 8-byte load per pair), so one width costs per pair one shared load, one
-// shared store, three paired FP32 operations, two maxima and one barrier (the sums alternate
-// between two buffers).  Which width gave the best SNR is needed only where the best passes
-// the threshold (few positions): there box_best_at forms it again, with the same sums.
+// One CTA per (DM, run of `tpc` consecutive tiles): the tile loop of box.cuh.
 template <typename T, int NW>
 __global__ void __launch_bounds__(kBoxThreads, 5)
     k_boxcar(const T *__restrict__ y, long long n, int tpc, double threshold,
              const double2 *__restrict__ musig, DevCand *__restrict__ cands,
              unsigned long long *__restrict__ count, long long cap)
 {
-    using G = BoxGeom<NW>;
-    constexpr int HL = G::HL, NBEST = G::NBEST, PAIRS = G::PAIRS;
     extern __shared__ __align__(16) unsigned char sm[];
-    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
-    float *best_s = B1 + G::BUF;
-    uint32_t *NB = reinterpret_cast<uint32_t *>(best_s + NBEST);  // next tile's samples
-
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
     if (!(sig > 0.0)) return;
-    const float mu_f = __double2float_rn(mu);
-    const float thr = __double2float_rn(threshold);
-    const T *r = y + (size_t)d * n;
-    static_assert((kBoxThreads & (kBoxThreads - 1)) == 0, "power-of-two block");
-    // (the mask tells the compiler tid < kBoxThreads, so range tests fold at compile time for
-    // all but the last pair)
-    const int tid = threadIdx.x & (kBoxThreads - 1);
-    // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
-    __shared__ float inv_w[NW];
-    if (tid < NW)
-        inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
-
     const long long ntiles = (n + kBoxTile - 1) / kBoxTile;
     const long long tile_lo = (long long)blockIdx.x * tpc;
     const long long tile_hi = tile_lo + tpc < ntiles ? tile_lo + tpc : ntiles;
-    // every staged sample and every boxcar of the tile inside the series: no per-element tests
-    auto inside = [&](long long tile) {
-        const long long r0 = tile * kBoxTile - HL;
-        return r0 >= 0 && r0 + PAIRS * 2 * kBoxThreads <= n;
-    };
-    box_prefetch<T, PAIRS>(NB, r, tile_lo * kBoxTile - HL, n, tid);
-    for (long long tile = tile_lo; tile < tile_hi; ++tile) {
-        const long long t0 = tile * kBoxTile;
-        const long long r0 = t0 - HL;  // series index of B[0] and best[0]
-        const bool interior = inside(tile);
-        float2 b[PAIRS], best[PAIRS];
-        cp_async_wait_all();
-#pragma unroll
-        for (int q = 0; q < PAIRS; ++q) {
-            const int i = 2 * tid + 2 * kBoxThreads * q;
-            b[q] = make_float2(box_value<T>(NB[i]), box_value<T>(NB[i + 1]));
-            *reinterpret_cast<float2 *>(B0 + i) = b[q];
-            best[q] = make_float2(-INFINITY, -INFINITY);
-        }
-        if (tile + 1 < tile_hi)  // in flight while this tile is searched
-            box_prefetch<T, PAIRS>(NB, r, r0 + kBoxTile, n, tid);
-        __syncthreads();
-#pragma unroll
-        for (int l = 0; l < NW; ++l) {
-            const int w = 1 << l;
-            if (l > 0) {
-                // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
-                const int h = w >> 1;
-                const float *cur = (l & 1) ? B0 : B1;
-                float *nxt = (l & 1) ? B1 : B0;
-#pragma unroll
-                for (int q = 0; q < PAIRS; ++q) {
-                    const int i = 2 * tid + 2 * kBoxThreads * q;
-                    // partner sums of positions i and i + 1
-                    const float2 pv = h == 1 ? make_float2(b[q].y, cur[i + 2])
-                                             : *reinterpret_cast<const float2 *>(cur + i + h);
-                    b[q] = add_f2(b[q], pv);
-                    *reinterpret_cast<float2 *>(nxt + i) = b[q];
-                }
-                __syncthreads();
-            }
-            const float wm = __fmul_rn((float)w, mu_f);
-            const float inv = inv_w[l];
-#pragma unroll
-            for (int q = 0; q < PAIRS; ++q) {
-                const int i = 2 * tid + 2 * kBoxThreads * q;
-                if (i >= NBEST) continue;  // i even and NBEST even: i + 1 < NBEST too
-                const long long t = r0 + i;
-                const float2 sv = mul_f2(add_f2(b[q], make_float2(-wm, -wm)), make_float2(inv, inv));
-                if (interior) {
-                    best[q].x = fmaxf(best[q].x, sv.x);
-                    best[q].y = fmaxf(best[q].y, sv.y);
-                } else {
-                    if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
-                    if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
-                }
-            }
-        }
-        bool any = false;
-#pragma unroll
-        for (int q = 0; q < PAIRS; ++q)
-            if (2 * tid + 2 * kBoxThreads * q < NBEST) any |= best[q].x >= thr || best[q].y >= thr;
-        // most tiles hold no sample over the threshold: skip the neighbourhood test there
-        if (!__syncthreads_or(any)) continue;
-#pragma unroll
-        for (int q = 0; q < PAIRS; ++q) {
-            const int i = 2 * tid + 2 * kBoxThreads * q;
-            if (i < NBEST) *reinterpret_cast<float2 *>(best_s + i) = best[q];
-        }
-        __syncthreads();
-        for (int q = tid; q < kBoxTile; q += kBoxThreads) {
-            const long long t = t0 + q;
-            if (t >= n) break;
-            const int i = q + HL;
-            const float bv = best_s[i];
-            if (!(bv >= thr)) continue;
-            float snr;
-            int width;
-            box_best_at<T, NW>(r, t, n, mu_f, inv_w, &snr, &width);
-            const int h = max(width / 2, 1);
-            bool keep = true;
-            for (int u = 1; u <= h && keep; ++u)
-                if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
-            for (int u = 1; u <= h && keep; ++u)
-                if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
-            if (!keep) continue;
-            const unsigned long long at = atomicAdd(count, 1ull);
-            if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, width, snr};
-        }
-        // (the next tile writes best_s only after its own barriers)
-    }
+    box_run<T, NW, kBoxThreads, true>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold,
+                                      d, cands, count, cap, sm);
 }
 
 // The boxcar search of every DM row, for 1..9 widths (a template per width count).
@@ -860,8 +644,7 @@ static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, doub
 template <int NW>
 static size_t boxcar_smem()
 {
-    using G = BoxGeom<NW>;
-    return (size_t)G::BUF * 8 + (size_t)G::NBEST * 4 + (size_t)G::PAIRS * 2 * kBoxThreads * 4;
+    return BoxGeom<NW, kBoxThreads>::SMEM;
 }
 
 template <typename T, int NW>

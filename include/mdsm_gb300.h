@@ -339,13 +339,21 @@ mdsm_status mdsm_unpack_device(const void *d_raw, long long nspectra, int nchans
 
 /* ---------------------------------------------------------------------------------------- */
 /* Batched form: several brute-force plans (beams of uneven block length, channel count and  */
-/* DM plan) dedispersed by one persistent launch over all their (DM block, time tile) items,  */
-/* optionally with RFI clipping before and a boxcar search after; the pass can be captured  */
-/* once in a CUDA graph and replayed.  mdsm_batch_autotune times the launch shapes (one     */
-/* persistent launch walking tiles or DM blocks first, or one launch per beam) on the        */
-/* registered buffers and keeps the fastest; with MDSM_AUTOTUNE_CACHE set to a file path the */
-/* choice is cached per beam geometry.  Replaces the one-beam, one-launch-per-segment loop   */
-/* of src/mdsm/dedispersion_thread.cu:64-94,220-243.  The plans must outlive the batch.      */
+/* DM plan) in one pass, optionally with RFI clipping before dedispersion and a boxcar search */
+/* after; the pass can be captured once in a CUDA graph and replayed.  Replaces the one-beam, */
+/* one-launch-per-segment loop of src/mdsm/dedispersion_thread.cu:64-94,220-243.  The plans  */
+/* must outlive the batch.                                                                    */
+/*  * Fused form (every plan uint8 samples with int32 output; the search, if on, over widths */
+/*    1..256): clip, dedispersion and search in ONE persistent launch over four work lists   */
+/*    (channel clips, spectrum clips, DM-block x time-tile tiles, search runs) tied by per-   */
+/*    beam completion counts with bounded device waits; the rows' statistics are folded into */
+/*    the dedispersion store.  mdsm_batch_autotune times its tile shapes (DM trials per      */
+/*    block x samples per tile x compute warps) and item orders on the registered buffers     */
+/*    and keeps the fastest.                                                                  */
+/*  * Otherwise clip launches, one persistent dedispersion launch over the packed beams'     */
+/*    tiles (a launch per beam for the rest) and per-beam search launches; the autotuner     */
+/*    picks the dedispersion launch shape.                                                    */
+/* With MDSM_AUTOTUNE_CACHE set to a file path the choice is cached per beam geometry.        */
 typedef struct mdsm_batch_s mdsm_batch;
 mdsm_status mdsm_batch_create(mdsm_plan *const *plans, int nbeams, mdsm_batch **out);
 mdsm_status mdsm_batch_set_buffers(mdsm_batch *b, const void *const *d_in,
@@ -359,6 +367,12 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice);
 /* use_graph: the first call runs the pass and captures it; later calls replay the graph. */
 mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream);
 int mdsm_batch_last_launches(const mdsm_batch *b);
+/* What an autotuner choice means: fused = 1 for the fused launch with its DM trials per block,
+ * samples per tile, compute warps and item order (0: a beam's DM blocks of one tile adjacent,
+ * 1: a DM block's tiles adjacent); fused = 0 for the unfused shapes, order = 0 persistent
+ * tile-major, 1 persistent DM-block-major, 2 one launch per beam. */
+mdsm_status mdsm_batch_choice_info(int choice, int *fused, int *dm_block, int *time_tile,
+                                   int *warps, int *order);
 mdsm_status mdsm_batch_candidates(mdsm_batch *b, int beam, mdsm_candidate *out, long long cap,
                                   long long *ncand, void *stream);
 void mdsm_batch_destroy(mdsm_batch *b);

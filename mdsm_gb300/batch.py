@@ -64,3 +64,10 @@ class Batch:
         check(load().mdsm_batch_candidates(self._h, beam, buf, self.cap, ctypes.byref(n),
                                            _stream_ptr(stream)))
         return np.frombuffer(buf, dtype=CAND_DTYPE, count=min(n.value, self.cap)).copy()
+
+
+def choice_info(choice):
+    """What an autotuner choice means: a dict with fused, dm_block, time_tile, warps, order."""
+    v = [ctypes.c_int() for _ in range(5)]
+    check(load().mdsm_batch_choice_info(int(choice), *[ctypes.byref(x) for x in v]))
+    return dict(zip(("fused", "dm_block", "time_tile", "warps", "order"), [x.value for x in v]))

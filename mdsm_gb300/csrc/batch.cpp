@@ -1,8 +1,15 @@
 // batch.cpp -- the batched form: many beams of uneven block length, channel count and DM plan
-// dedispersed by one persistent launch over the work list of all their tiles, optionally with
-// RFI clipping before and a boxcar search after, the whole pass captured once in a CUDA graph
-// and replayed.  An autotuner times the launch shapes on the caller's buffers and keeps the
-// fastest; choices can be cached per beam geometry in a text file.
+// in one persistent launch, the whole pass captured once in a CUDA graph and replayed.
+//
+// Fused form (every beam a uint8 brute-force plan with int32 output, boxcar widths 1..256 if
+// detection is on): RFI clip, dedispersion and boxcar search in ONE persistent launch
+// (k_batch_fused) over four work lists tied by per-beam completion counts, with the rows'
+// statistics folded into the dedispersion store.  The autotuner times its tile shapes (DM
+// trials per block x samples per tile x compute warps) and item orders on the caller's
+// buffers and keeps the fastest.
+// Otherwise: clip launches, one persistent dedispersion launch over the packed beams' tiles
+// (one launch per beam for the rest) and per-beam search launches, in one graph; the autotuner
+// picks the dedispersion launch shape.  Choices can be cached per beam geometry in a file.
 //
 // The reference dedisperses one beam per process, one launch per DM segment, each launch
 // followed by a synchronous copy (src/mdsm/dedispersion_thread.cu:69-94,220-243,332-355).
@@ -18,6 +25,24 @@
 #include "internal.h"
 
 using namespace mdsm;
+
+// The fused launch's tables, work lists and buffers for one tile shape and item order.
+struct FusedRun {
+    int shape = -1, order = 0;
+    bool clip = false, detect = false;
+    std::vector<StageGeom> geoms;      // per beam, this shape's tables (device copies owned)
+    std::vector<void *> d_rel;         // per beam, offsets with the common phase stride
+    int rawcap = 0, ps = 0, n_dd = 0;
+    FusedArgs f{};
+    void *d_kargs = nullptr, *d_fb = nullptr, *d_dd = nullptr, *d_cc = nullptr, *d_cs = nullptr,
+         *d_bx = nullptr;
+    unsigned *d_sync = nullptr;        // 4 work counters, then 3 completion counts per beam
+    size_t sync_bytes = 0;
+    unsigned long long *d_mom = nullptr;  // all beams' row moments
+    size_t mom_bytes = 0;
+    DevCand *d_cands = nullptr;        // [beam][cap]
+    unsigned long long *d_counts = nullptr;
+};
 
 struct mdsm_batch_s {
     std::vector<mdsm_plan *> plans;
@@ -45,9 +70,197 @@ struct mdsm_batch_s {
     std::vector<long long> in_stride;
     std::vector<void *> out;
     std::vector<long long> out_stride;
+    // fused form
+    bool fusable = false;      // every beam a uint8 brute-force plan with int32 output
+    FusedRun fz;
+    bool fz_dirty = true;
 };
 
 namespace {
+
+void fused_free(FusedRun &z)
+{
+    for (StageGeom &g : z.geoms) free_stage(g);
+    for (void *p : z.d_rel)
+        if (p) cudaFree(p);
+    for (void *p : {z.d_kargs, z.d_fb, z.d_dd, z.d_cc, z.d_cs, z.d_bx})
+        if (p) cudaFree(p);
+    if (z.d_sync) cudaFree(z.d_sync);
+    if (z.d_mom) cudaFree(z.d_mom);
+    if (z.d_cands) cudaFree(z.d_cands);
+    if (z.d_counts) cudaFree(z.d_counts);
+    z = FusedRun();
+}
+
+template <typename T>
+mdsm_status upload(const std::vector<T> &v, void **d)
+{
+    if (*d) cudaFree(*d);
+    *d = nullptr;
+    MDSM_CUDA_TRY(cudaMalloc(d, std::max<size_t>(1, v.size()) * sizeof(T)));
+    if (!v.empty())
+        MDSM_CUDA_TRY(cudaMemcpy(*d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return MDSM_OK;
+}
+
+// Tables and work lists of the fused launch for tile shape `shape` and item order `order`
+// (0: a beam's DM blocks of one time tile adjacent, 1: a DM block's time tiles adjacent), with
+// the batch's buffers, clip and detection settings.
+mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool detect)
+{
+    fused_free(b->fz);
+    FusedRun &z = b->fz;
+    z.shape = shape;
+    z.order = order;
+    z.clip = clip;
+    z.detect = detect;
+    const size_t nb = b->plans.size();
+    const FusedShapeInfo si = fused_shape_info(shape);
+    z.geoms.resize(nb);
+    for (size_t i = 0; i < nb; ++i) {
+        const Plan &p = b->plans[i]->p;
+        StageGeom g = p.stages[0];  // geometry; the tables are rebuilt for this shape
+        g.rel.clear();
+        g.sminspan.clear();
+        g.d_rel = nullptr;
+        g.d_sminspan = nullptr;
+        z.geoms[i] = g;
+        MDSM_TRY(fused_tables(shape, z.geoms[i], p.S));
+        // the caller's buffer holds what the plan's own tile shape reads (mdsm_plan_info
+        // in_bytes); a shape whose last tile reads further is not used for this batch
+        if (stage_in_bytes(z.geoms[i], b->in_stride[i], 0) >
+            stage_in_bytes(p.stages[0], b->in_stride[i], 0))
+            return fail(MDSM_EINVAL, "fused batch: this tile shape reads past beam " +
+                                         std::to_string(i) + "'s input");
+        z.rawcap = std::max(z.rawcap, z.geoms[i].rowcap);
+        z.ps = std::max(z.ps, z.geoms[i].ps);
+    }
+    z.d_rel.assign(nb, nullptr);
+    for (size_t i = 0; i < nb; ++i) {  // offsets re-expressed with the common phase stride
+        const StageGeom &g = z.geoms[i];
+        std::vector<int32_t> rel(g.rel.size());
+        for (size_t j = 0; j < rel.size(); ++j)
+            rel[j] = g.rel[j] / g.ps * z.ps + g.rel[j] % g.ps;
+        MDSM_TRY(upload(rel, &z.d_rel[i]));
+    }
+    // moments and candidates
+    std::vector<size_t> mom_off(nb);
+    for (size_t i = 0; i < nb; ++i) {
+        mom_off[i] = z.mom_bytes / sizeof(unsigned long long);
+        z.mom_bytes += (size_t)b->plans[i]->p.ndms * 3 * sizeof(unsigned long long);
+    }
+    MDSM_CUDA_TRY(cudaMalloc(&z.d_mom, std::max<size_t>(z.mom_bytes, 8)));
+    MDSM_CUDA_TRY(cudaMalloc(&z.d_cands, nb * (size_t)b->cap * sizeof(DevCand)));
+    MDSM_CUDA_TRY(cudaMalloc(&z.d_counts, nb * sizeof(unsigned long long)));
+    z.sync_bytes = (4 + 3 * nb) * sizeof(unsigned);
+    MDSM_CUDA_TRY(cudaMalloc(&z.d_sync, z.sync_bytes));
+    // work lists; beams with more channels first
+    std::vector<int> beams(nb);
+    for (size_t i = 0; i < nb; ++i) beams[i] = (int)i;
+    std::stable_sort(beams.begin(), beams.end(), [&](int x, int y) {
+        return b->plans[x]->p.nchans > b->plans[y]->p.nchans;
+    });
+    std::vector<KArgs> ka(nb);
+    std::vector<FusedBeam> fb(nb);
+    std::vector<int4> dd, bx;
+    std::vector<int2> cc, cs;
+    const int kFusedBoxTile = 2048, tpc = 4;
+    for (int i : beams) {
+        const Plan &p = b->plans[i]->p;
+        const StageGeom &g = z.geoms[i];
+        unsigned char *in = static_cast<unsigned char *>(const_cast<void *>(b->in[i]));
+        int32_t *out = static_cast<int32_t *>(b->out[i]);
+        unsigned long long *mom = z.d_mom + mom_off[i];
+        ka[i] = fused_kargs(g, z.d_rel[i], in, b->in_stride[i], out, b->out_stride[i], z.rawcap,
+                            z.ps, mom, b->d_err);
+        const long long ncols = (long long)p.nsamp + p.maxshift;
+        const int ntiles = (p.nsamp + g.T - 1) / g.T;
+        const size_t dd0 = dd.size();
+        if (order == 0) {
+            for (int t = 0; t < ntiles; ++t)
+                for (int k = 0; k < g.nblk; ++k) dd.push_back(make_int4(i, k, t, 0));
+        } else {
+            for (int k = 0; k < g.nblk; ++k)
+                for (int t = 0; t < ntiles; ++t) dd.push_back(make_int4(i, k, t, 0));
+        }
+        FusedBeam &B = fb[i];
+        B.in = in;
+        B.in_stride = b->in_stride[i];
+        B.ncols = ncols;
+        B.nchans = p.nchans;
+        B.ndms = p.ndms;
+        B.nsamp = p.nsamp;
+        B.nspec_items =
+            clip ? (unsigned)((ncols + kFusedSpecColsHost - 1) / kFusedSpecColsHost) : 0u;
+        B.ndd_done = (unsigned)((dd.size() - dd0) * (size_t)si.compute_warps);
+        B.out = out;
+        B.out_stride = b->out_stride[i];
+        B.mom = mom;
+        B.cands = z.d_cands + (size_t)i * (size_t)b->cap;
+        B.count = z.d_counts + i;
+        if (clip && b->k_chan > 0)
+            for (int c = 0; c < p.nchans; ++c) cc.push_back(make_int2(i, c));
+        if (clip)
+            for (long long c0 = 0; c0 < ncols; c0 += kFusedSpecColsHost)
+                cs.push_back(make_int2(i, (int)c0));
+        if (detect) {
+            const int nbt = (p.nsamp + kFusedBoxTile - 1) / kFusedBoxTile;
+            for (int d = 0; d < p.ndms; ++d)
+                for (int t0 = 0; t0 < nbt; t0 += tpc)
+                    bx.push_back(make_int4(i, d, t0, std::min(nbt, t0 + tpc)));
+        }
+    }
+    if (dd.size() > 0x7fffffffULL || bx.size() > 0x7fffffffULL || cc.size() > 0x7fffffffULL)
+        return fail(MDSM_EINVAL, "fused batch: work lists too long");
+    z.n_dd = (int)dd.size();
+    MDSM_TRY(upload(ka, &z.d_kargs));
+    MDSM_TRY(upload(fb, &z.d_fb));
+    MDSM_TRY(upload(dd, &z.d_dd));
+    MDSM_TRY(upload(cc, &z.d_cc));
+    MDSM_TRY(upload(cs, &z.d_cs));
+    MDSM_TRY(upload(bx, &z.d_bx));
+    FusedArgs &f = z.f;
+    f.fb = static_cast<const FusedBeam *>(z.d_fb);
+    f.cc_items = static_cast<const int2 *>(z.d_cc);
+    f.cs_items = static_cast<const int2 *>(z.d_cs);
+    f.bx_items = static_cast<const int4 *>(z.d_bx);
+    f.n_cc = (int)cc.size();
+    f.n_cs = (int)cs.size();
+    f.n_bx = (int)bx.size();
+    f.counters = z.d_sync;
+    f.done = z.d_sync + 4;
+    f.k_chan = clip ? b->k_chan : 0.0;
+    f.k_spec = clip ? b->k_spec : 0.0;
+    f.threshold = b->threshold;
+    f.cap = b->cap;
+    f.err = b->d_err;
+    return MDSM_OK;
+}
+
+// One fused pass: counters and moments zeroed, the launch, the candidates' copies.
+mdsm_status fused_pass(mdsm_batch *b, cudaStream_t st)
+{
+    FusedRun &z = b->fz;
+    MDSM_CUDA_TRY(cudaMemsetAsync(z.d_sync, 0, z.sync_bytes, st));
+    MDSM_CUDA_TRY(cudaMemsetAsync(z.d_mom, 0, z.mom_bytes, st));
+    MDSM_CUDA_TRY(
+        cudaMemsetAsync(z.d_counts, 0, b->plans.size() * sizeof(unsigned long long), st));
+    MDSM_TRY(fused_launch(z.shape, z.f, static_cast<const KArgs *>(z.d_kargs),
+                          static_cast<const int4 *>(z.d_dd), z.n_dd, z.rawcap, z.ps, st));
+    b->launches = 1;
+    if (z.detect)
+        for (size_t i = 0; i < b->plans.size(); ++i) {
+            static_assert(sizeof(DevCand) == sizeof(mdsm_candidate), "record sizes differ");
+            MDSM_CUDA_TRY(cudaMemcpyAsync(b->h_count[i], z.d_counts + i, sizeof(long long),
+                                          cudaMemcpyDeviceToHost, st));
+            MDSM_CUDA_TRY(cudaMemcpyAsync(b->h_cands[i], z.d_cands + i * (size_t)b->cap,
+                                          (size_t)b->cap * sizeof(DevCand),
+                                          cudaMemcpyDeviceToHost, st));
+        }
+    return MDSM_OK;
+}
+
+bool fused_wanted(const mdsm_batch *b) { return b->fusable && (!b->detect || b->nwidths == 9); }
 
 void drop_graph(mdsm_batch *b)
 {
@@ -97,11 +310,25 @@ void cache_store(const std::string &key, int choice)
     f << key << " " << choice << "\n";
 }
 
+// Autotuner choices: 0-2 the unfused dedispersion launch shapes (persistent tile-major,
+// persistent DM-block-major, one launch per beam); 10 + 2 shape + order the fused launch.
+constexpr int kFusedChoice0 = 10;
+
 // One pass (no graph): optional clip, dedispersion with `choice`, optional detection.
 mdsm_status pass(mdsm_batch *b, int choice, cudaStream_t st)
 {
     const size_t nb = b->plans.size();
     b->launches = 0;
+    if (choice >= kFusedChoice0) {
+        const int shape = (choice - kFusedChoice0) / 2, order = (choice - kFusedChoice0) % 2;
+        FusedRun &z = b->fz;
+        if (b->fz_dirty || z.shape != shape || z.order != order || z.clip != b->clip ||
+            z.detect != b->detect) {
+            MDSM_TRY(fused_build(b, shape, order, b->clip, b->detect));
+            b->fz_dirty = false;
+        }
+        return fused_pass(b, st);
+    }
     if (b->clip)
         for (size_t i = 0; i < nb; ++i) {
             const Plan &p = b->plans[i]->p;
@@ -142,6 +369,13 @@ mdsm_status mdsm_batch_create(mdsm_plan *const *plans, int nbeams, mdsm_batch **
     }
     mdsm_batch *b = new mdsm_batch();
     b->plans.assign(plans, plans + nbeams);
+    b->fusable = true;
+    for (int i = 0; i < nbeams; ++i) {
+        const Plan &p = plans[i]->p;
+        if (p.in_dtype != MDSM_U8 || p.out_dtype != MDSM_OUT_I32 || p.S.empty())
+            b->fusable = false;
+    }
+    b->choice = b->fusable ? kFusedChoice0 : 0;
     mdsm_status st = batch_prepare(b->st, beams);
     if (st == MDSM_OK && cudaMalloc(&b->d_err, sizeof(unsigned)) != cudaSuccess)
         st = fail(MDSM_ENOMEM, "batch: error word");
@@ -171,6 +405,7 @@ mdsm_status mdsm_batch_set_buffers(mdsm_batch *b, const void *const *d_in,
     }
     drop_graph(b);
     b->buffers = true;
+    b->fz_dirty = true;
     return batch_set_buffers(b->st, b->in, b->in_stride, b->out, b->out_stride, b->d_err,
                              b->choice == 1 ? 0 : 1);
 }
@@ -181,6 +416,7 @@ mdsm_status mdsm_batch_enable_clip(mdsm_batch *b, double k_chan, double k_spec)
     b->clip = k_chan > 0 || k_spec > 0;
     b->k_chan = k_chan;
     b->k_spec = k_spec;
+    b->fz_dirty = true;
     drop_graph(b);
     return MDSM_OK;
 }
@@ -211,28 +447,42 @@ mdsm_status mdsm_batch_enable_detect(mdsm_batch *b, int nwidths, double threshol
     b->nwidths = nwidths;
     b->threshold = threshold;
     b->cap = cap;
+    b->fz_dirty = true;
+    if (b->choice >= kFusedChoice0 && !fused_wanted(b)) b->choice = 0;
     drop_graph(b);
     return MDSM_OK;
 }
 
-// Times each launch shape twice on the registered buffers (after one warm pass) and keeps
-// the fastest.  A cached choice for the same beam geometry is reused when
-// MDSM_AUTOTUNE_CACHE names a file.
+// Times each candidate twice on the registered buffers (after one warm pass) and keeps the
+// fastest: the fused launch's tile shapes and item orders where the beams allow it, else the
+// unfused dedispersion launch shapes.  The clip is left out of the timed passes (it changes
+// the input in place); the search stays in.  A cached choice for the same beam geometry is
+// reused when MDSM_AUTOTUNE_CACHE names a file.
 mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
 {
     if (!b || !b->buffers) return fail(MDSM_ESTATE, "batch: set buffers first");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const std::string key = geometry_key(b);
+    const bool fused = fused_wanted(b);
+    const std::string key =
+        geometry_key(b) + (fused ? "fused" : "") + (b->detect ? "det" : "");
     int best = cache_lookup(key);
     if (best < 0) {
-        const bool clip = b->clip, det = b->detect;
-        b->clip = b->detect = false;  // time the dedispersion launch shapes alone
+        const bool clip = b->clip;
+        const bool det = b->detect;
+        b->clip = false;
+        if (!fused) b->detect = false;  // the unfused shapes: the dedispersion launch alone
         float best_ms = 1e30f;
         cudaEvent_t e0, e1;
         MDSM_CUDA_TRY(cudaEventCreate(&e0));
         MDSM_CUDA_TRY(cudaEventCreate(&e1));
-        for (int c = 0; c < 3; ++c) {
-            MDSM_TRY(pass(b, c, st));
+        std::vector<int> cands;
+        if (fused)
+            for (int c = 0; c < 2 * fused_num_shapes(); ++c) cands.push_back(kFusedChoice0 + c);
+        else
+            cands = {0, 1, 2};
+        for (int c : cands) {
+            if (c >= kFusedChoice0 && pass(b, c, st) != MDSM_OK) continue;  // does not fit
+            if (c < kFusedChoice0) MDSM_TRY(pass(b, c, st));
             MDSM_CUDA_TRY(cudaEventRecord(e0, st));
             for (int r = 0; r < 2; ++r) MDSM_TRY(pass(b, c, st));
             MDSM_CUDA_TRY(cudaEventRecord(e1, st));
@@ -248,10 +498,12 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
         cudaEventDestroy(e1);
         b->clip = clip;
         b->detect = det;
+        if (best < 0) return fail(MDSM_EINVAL, "batch: no launch shape fits these beams");
         cache_store(key, best);
     }
     b->choice = best;
     b->tuned = true;
+    b->fz_dirty = true;
     drop_graph(b);
     if (choice) *choice = best;
     return MDSM_OK;
@@ -293,6 +545,27 @@ mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream)
 
 int mdsm_batch_last_launches(const mdsm_batch *b) { return b ? b->launches : 0; }
 
+mdsm_status mdsm_batch_choice_info(int choice, int *fused, int *dm_block, int *time_tile,
+                                   int *warps, int *order)
+{
+    if (!fused || !dm_block || !time_tile || !warps || !order)
+        return fail(MDSM_EINVAL, "null argument");
+    if (choice >= kFusedChoice0 && choice < kFusedChoice0 + 2 * fused_num_shapes()) {
+        const FusedShapeInfo si = fused_shape_info((choice - kFusedChoice0) / 2);
+        *fused = 1;
+        *dm_block = si.dm_block;
+        *time_tile = si.time_tile;
+        *warps = si.compute_warps;
+        *order = (choice - kFusedChoice0) % 2;
+        return MDSM_OK;
+    }
+    if (choice < 0 || choice > 2) return fail(MDSM_EINVAL, "no such choice");
+    *fused = 0;
+    *dm_block = *time_tile = *warps = 0;
+    *order = choice;
+    return MDSM_OK;
+}
+
 // Candidates of beam `beam` from the last pass (synchronises the stream first).
 mdsm_status mdsm_batch_candidates(mdsm_batch *b, int beam, mdsm_candidate *out, long long cap,
                                   long long *ncand, void *stream)
@@ -316,6 +589,7 @@ void mdsm_batch_destroy(mdsm_batch *b)
 {
     if (!b) return;
     drop_graph(b);
+    fused_free(b->fz);
     batch_release(b->st);
     for (void *p : b->d_det) cudaFree(p);
     for (auto *p : b->h_cands) cudaFreeHost(p);

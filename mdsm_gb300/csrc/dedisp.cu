@@ -27,6 +27,7 @@
 #include <type_traits>
 
 #include "internal.h"
+#include "box.cuh"
 #include "ptx.cuh"
 
 namespace mdsm {
@@ -725,6 +726,245 @@ __global__ void __launch_bounds__(CfgU8::THREADS, 1)
 }
 
 // ------------------------------------------------------------------------------------------
+// fused batched launch: RFI clip, dedispersion and boxcar search of several uint8 beams in one
+// persistent launch
+// ------------------------------------------------------------------------------------------
+// Four phases over four work lists, each item taken from its own global counter by a whole
+// CTA: (1) clip one channel of one beam; (2) clip one run of columns (spectra) of one beam;
+// (3) dedisperse one (beam, DM block, time tile) through the packed stream, storing int32
+// series and folding each row's exact moments; (4) boxcar-search one run of tiles of one row.
+// Each item first waits (bounded) for its beam's items of the phase before: a count in
+// `done` that the items raise after a fence once their results are written.  A CTA leaves a
+// phase only when that phase's list is exhausted, so every item an item waits for has already
+// been taken by a running CTA, which depends only on earlier phases: the waits always end.
+constexpr int kFusedSpecCols = kFusedSpecColsHost;  // columns of one phase-2 item (a thread each)
+constexpr int kFusedBoxThreads = 512;
+constexpr int kFusedBoxWidths = 9;   // widths 1..256
+
+// Bounded wait until *ctr >= target (raised by other CTAs after a fence): polling with
+// backoff, about 4 s at most; on timeout sets ERR_WAIT_TIMEOUT and returns false.
+__device__ __forceinline__ bool wait_count(const unsigned *ctr, unsigned target, unsigned *err)
+{
+    for (unsigned i = 0; i < (1u << 22); ++i) {
+        if (*reinterpret_cast<const volatile unsigned *>(ctr) >= target) {
+            __threadfence();
+            return true;
+        }
+        __nanosleep(i < 64 ? 32 : 1000);
+    }
+    atomicOr(err, ERR_WAIT_TIMEOUT);
+    return false;
+}
+
+// The whole CTA's next item of a list: thread 0 takes it from the counter.
+__device__ __forceinline__ int cta_grab(unsigned *counter, int n, int *slot)
+{
+    __syncthreads();  // everyone is done with the previous item and with *slot
+    if (threadIdx.x == 0) *slot = (int)atomicAdd(counter, 1u);
+    __syncthreads();
+    const int it = *slot;
+    return it < n ? it : -1;
+}
+
+// Marks an item of `phase` of beam b done, after this CTA's writes.
+__device__ __forceinline__ void cta_done(unsigned *done, int b, int phase)
+{
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) atomicAdd(&done[3 * b + phase], 1u);
+}
+
+// The clip test of the standalone clip (rfi.cu), fabs(v - mean) >= lim in double, is monotone
+// in v on each side of the mean (the rounded difference is monotone), so for integer samples
+// it holds exactly for v >= hi when v >= ceil(mean) and for v <= lo below: the bounds are found
+// from the real-valued estimates and corrected with that same test.
+__device__ __forceinline__ void clip_bounds_u8(double mu, double lim, int *cm, int *lo, int *hi)
+{
+    auto clipped = [&](int v) { return fabs(__dadd_rn((double)v, -mu)) >= lim; };
+    const int c = (int)ceil(mu);
+    int h = (int)fmin(fmax(ceil(mu + lim), (double)c), 256.0);
+    while (h > c && clipped(h - 1)) --h;
+    while (h <= 255 && !clipped(h)) ++h;
+    int l = (int)fmax(fmin(floor(mu - lim), (double)(c - 1)), -1.0);
+    while (l < c - 1 && clipped(l + 1)) ++l;
+    while (l >= 0 && !clipped(l)) --l;
+    *cm = c;
+    *lo = l;
+    *hi = h;
+}
+
+__device__ __forceinline__ uint8_t clip_rep_u8(double mu)
+{
+    const int r = __double2int_rn(mu);
+    return (uint8_t)min(max(r, 0), 255);
+}
+
+__device__ __forceinline__ void mean_sigma_ll(long long s1, long long s2, long long n, double *mu,
+                                              double *sig)
+{
+    const double m = __ddiv_rn((double)s1, (double)n);
+    const double var = __dadd_rn(__ddiv_rn((double)s2, (double)n), -__dmul_rn(m, m));
+    *mu = m;
+    *sig = var > 0.0 ? __dsqrt_rn(var) : 0.0;
+}
+
+// Phase 3's item source: the dedispersion list, each item waiting for its beam's clip, each
+// compute warp counting its stores.
+struct FusedItems {
+    const KArgs *beams;
+    const int4 *items;
+    int nitems;
+    unsigned *counter;
+    const FusedBeam *fb;
+    unsigned *done;
+    unsigned *err;
+    __device__ int grab()
+    {
+        const int it = (int)atomicAdd(counter, 1u);
+        if (it >= nitems) return -1;
+        const int b = items[it].x;
+        wait_count(&done[3 * b + 1], fb[b].nspec_items, err);  // (a timeout is recorded)
+        return it;
+    }
+    __device__ int4 item(int it) const { return items[it]; }
+    __device__ const KArgs &args(int beam) const { return beams[beam]; }
+    __device__ void stored(int beam) const
+    {
+        __threadfence();
+        __syncwarp();
+        if ((threadIdx.x & 31) == 0) atomicAdd(&done[3 * beam + 2], 1u);
+    }
+};
+
+template <class Cfg>
+__global__ void __launch_bounds__(Cfg::THREADS, 1)
+    k_batch_fused(const FusedArgs f, const KArgs *__restrict__ beams,
+                  const int4 *__restrict__ dd_items, int n_dd, int rawcap, int ps)
+{
+    static_assert(Cfg::THREADS >= kFusedSpecCols && Cfg::THREADS >= kFusedBoxThreads,
+                  "CTA too narrow for the clip and search phases");
+    extern __shared__ __align__(128) unsigned char smem[];
+    __shared__ int slot;
+    __shared__ long long red[2][Cfg::THREADS / 32];
+    __shared__ double s_mu, s_sig;
+    __shared__ int s_ok;
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    constexpr int NWARP = Cfg::THREADS / 32;
+
+    // ---- phase 1: clip each channel over its row ----
+    if (f.k_chan > 0.0)
+        for (int it; (it = cta_grab(&f.counters[0], f.n_cc, &slot)) >= 0;) {
+            const int2 w = f.cc_items[it];
+            const FusedBeam &B = f.fb[w.x];
+            uint8_t *row = B.in + (size_t)w.y * (size_t)B.in_stride;
+            long long a1 = 0, a2 = 0;
+            for (long long i = tid; i < B.ncols; i += Cfg::THREADS) {
+                const long long v = row[i];
+                a1 += v;
+                a2 += v * v;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                a1 += __shfl_xor_sync(0xffffffffu, a1, o);
+                a2 += __shfl_xor_sync(0xffffffffu, a2, o);
+            }
+            if (lane == 0) {
+                red[0][warp] = a1;
+                red[1][warp] = a2;
+            }
+            __syncthreads();
+            if (tid == 0) {
+                long long s1 = 0, s2 = 0;
+                for (int k = 0; k < NWARP; ++k) {
+                    s1 += red[0][k];
+                    s2 += red[1][k];
+                }
+                mean_sigma_ll(s1, s2, B.ncols, &s_mu, &s_sig);
+            }
+            __syncthreads();
+            int cm, lo, hi;
+            clip_bounds_u8(s_mu, __dmul_rn(f.k_chan, s_sig), &cm, &lo, &hi);
+            const uint8_t rep = clip_rep_u8(s_mu);
+            for (long long i = tid; i < B.ncols; i += Cfg::THREADS) {
+                const int v = row[i];
+                if (v >= cm ? v >= hi : v <= lo) row[i] = rep;
+            }
+            cta_done(f.done, w.x, 0);
+        }
+
+    // ---- phase 2: clip each spectrum over the channels (one column per thread) ----
+    for (int it; (it = cta_grab(&f.counters[1], f.n_cs, &slot)) >= 0;) {
+        const int2 w = f.cs_items[it];
+        const FusedBeam &B = f.fb[w.x];
+        if (tid == 0)
+            s_ok = wait_count(&f.done[3 * w.x + 0], f.k_chan > 0.0 ? (unsigned)B.nchans : 0u, f.err);
+        __syncthreads();
+        const long long t = (long long)w.y + tid;
+        if (f.k_spec > 0.0 && s_ok && tid < kFusedSpecCols && t < B.ncols) {
+            long long s1 = 0, s2 = 0;
+            const uint8_t *col = B.in + t;
+            for (int c = 0; c < B.nchans; ++c) {
+                const long long v = col[(size_t)c * (size_t)B.in_stride];
+                s1 += v;
+                s2 += v * v;
+            }
+            double mu, sig;
+            mean_sigma_ll(s1, s2, B.nchans, &mu, &sig);
+            int cm, lo, hi;
+            clip_bounds_u8(mu, __dmul_rn(f.k_spec, sig), &cm, &lo, &hi);
+            const uint8_t rep = clip_rep_u8(mu);
+            uint8_t *cw = B.in + t;
+            for (int c = 0; c < B.nchans; ++c) {
+                uint8_t *p = cw + (size_t)c * (size_t)B.in_stride;
+                const int v = *p;
+                if (v >= cm ? v >= hi : v <= lo) *p = rep;
+            }
+        }
+        cta_done(f.done, w.x, 1);
+    }
+
+    // ---- phase 3: dedispersion through the packed stream ----
+    __syncthreads();
+    packed_init_barriers(smem);
+    {
+        FusedItems src{beams, dd_items, n_dd, &f.counters[2], f.fb, f.done, f.err};
+        packed_stream<Cfg>(src, smem, rawcap, ps, f.err);
+    }
+    __syncthreads();
+    if (tid == 0) {  // the barriers' memory is used for other data from here on
+        uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
+        for (int k = 0; k < kPNR; ++k)
+            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(&bars[k]))
+                         : "memory");
+    }
+
+    // ---- phase 4: boxcar search, one run of tiles of one row per item ----
+    for (int it; (it = cta_grab(&f.counters[3], f.n_bx, &slot)) >= 0;) {
+        const int4 w = f.bx_items[it];
+        const FusedBeam &B = f.fb[w.x];
+        if (tid == 0) {
+            s_ok = wait_count(&f.done[3 * w.x + 2], B.ndd_done, f.err);
+            // the row's mean and sigma from its folded moments (k_mom_finish's conversion)
+            const unsigned long long *m = B.mom + 3 * (size_t)w.y;
+            const long long s1 = (long long)m[0];
+            const double e2 = __ddiv_rn(__dadd_rn(__dmul_rn((double)m[2], 18446744073709551616.0),
+                                                  (double)m[1]),
+                                        (double)B.nsamp);
+            const double mm = __ddiv_rn((double)s1, (double)B.nsamp);
+            const double var = __dadd_rn(e2, -__dmul_rn(mm, mm));
+            s_mu = mm;
+            s_sig = var > 0.0 ? __dsqrt_rn(var) : 0.0;
+        }
+        __syncthreads();
+        const double mu = s_mu, sig = s_sig;
+        if (!s_ok || !(sig > 0.0)) continue;  // (uniform across the CTA)
+        box_run<int32_t, kFusedBoxWidths, kFusedBoxThreads, Cfg::THREADS == kFusedBoxThreads>(
+            B.out + (size_t)w.y * (size_t)B.out_stride, B.nsamp, w.z, w.w, mu, sig, f.threshold,
+            w.y, B.cands, B.count, f.cap, smem);
+    }
+}
+
+// ------------------------------------------------------------------------------------------
 // host side
 // ------------------------------------------------------------------------------------------
 
@@ -881,6 +1121,108 @@ bool packed_tables(StageGeom &g, const std::vector<int32_t> &S, int kernel_id)
 }
 
 }  // namespace
+
+// ---- fused batched launch: its tile shapes, tables and launch ----
+namespace {
+using FusedCfg0 = CfgU8;                               // 19 warps x 2 trials, 512 samples
+using FusedCfg1 = CfgU8w16;                            // 16 x 2, 512
+using FusedCfg2 = PackedCfg<1, 19, 2, false, 256>;     // 19 x 2, 256
+using FusedCfg3 = PackedCfg<1, 16, 2, false, 768>;     // 16 x 2, 768
+
+template <class Cfg>
+size_t fused_smem_t(int rawcap, int ps)
+{
+    return std::max(packed_smem<Cfg>(rawcap, ps),
+                    BoxGeom<kFusedBoxWidths, kFusedBoxThreads>::SMEM);
+}
+
+template <class Cfg>
+mdsm_status fused_launch_t(const FusedArgs &f, const KArgs *kargs, const int4 *items, int n_dd,
+                           int rawcap, int ps, cudaStream_t st)
+{
+    const size_t smem = fused_smem_t<Cfg>(rawcap, ps);
+    cudaFuncAttributes at;
+    MDSM_CUDA_TRY(cudaFuncGetAttributes(&at, k_batch_fused<Cfg>));
+    if (smem + at.sharedSizeBytes > packed_smem_limit())
+        return fail(MDSM_EINVAL, "fused batch: staging does not fit this tile shape");
+    MDSM_CUDA_TRY(cudaFuncSetAttribute(k_batch_fused<Cfg>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int dev = 0, sms = 0;
+    MDSM_CUDA_TRY(cudaGetDevice(&dev));
+    MDSM_CUDA_TRY(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    k_batch_fused<Cfg><<<sms, Cfg::THREADS, smem, st>>>(f, kargs, items, n_dd, rawcap, ps);
+    MDSM_CUDA_TRY(cudaGetLastError());
+    return MDSM_OK;
+}
+}  // namespace
+
+int fused_num_shapes() { return 4; }
+
+FusedShapeInfo fused_shape_info(int shape)
+{
+    switch (shape) {
+    case 0: return {FusedCfg0::DB, FusedCfg0::PT, FusedCfg0::NW};
+    case 1: return {FusedCfg1::DB, FusedCfg1::PT, FusedCfg1::NW};
+    case 2: return {FusedCfg2::DB, FusedCfg2::PT, FusedCfg2::NW};
+    default: return {FusedCfg3::DB, FusedCfg3::PT, FusedCfg3::NW};
+    }
+}
+
+// g: a copy of a uint8 brute-force plan's stage (its geometry); S: the plan's shift table.
+mdsm_status fused_tables(int shape, StageGeom &g, const std::vector<int32_t> &S)
+{
+    g.out_u16 = 0;
+    g.out_i32 = 1;
+    g.d_rel = nullptr;
+    g.d_sminspan = nullptr;
+    bool ok = false;
+    switch (shape) {
+    case 0: ok = packed_tables<FusedCfg0>(g, S, 2); break;
+    case 1: ok = packed_tables<FusedCfg1>(g, S, 2); break;
+    case 2: ok = packed_tables<FusedCfg2>(g, S, 2); break;
+    default: ok = packed_tables<FusedCfg3>(g, S, 2); break;
+    }
+    if (!ok) return fail(MDSM_EINVAL, "fused batch: a beam's staging does not fit this shape");
+    return upload_stage(g);
+}
+
+mdsm_status fused_launch(int shape, const FusedArgs &f, const KArgs *d_kargs, const int4 *d_items,
+                         int n_dd, int rawcap, int ps, cudaStream_t st)
+{
+    switch (shape) {
+    case 0: return fused_launch_t<FusedCfg0>(f, d_kargs, d_items, n_dd, rawcap, ps, st);
+    case 1: return fused_launch_t<FusedCfg1>(f, d_kargs, d_items, n_dd, rawcap, ps, st);
+    case 2: return fused_launch_t<FusedCfg2>(f, d_kargs, d_items, n_dd, rawcap, ps, st);
+    default: return fused_launch_t<FusedCfg3>(f, d_kargs, d_items, n_dd, rawcap, ps, st);
+    }
+}
+
+// KArgs of one beam of the fused launch (with the launch's common staging geometry)
+KArgs fused_kargs(const StageGeom &g, const void *d_rel_common, const unsigned char *in,
+                  long long in_stride, int32_t *out, long long out_stride, int rawcap, int ps,
+                  unsigned long long *mom, unsigned *err)
+{
+    KArgs a;
+    std::memset(&a, 0, sizeof a);
+    a.in = in;
+    a.in_stride = in_stride;
+    a.out = reinterpret_cast<unsigned char *>(out);
+    a.out_stride = out_stride;
+    a.rel = static_cast<const int32_t *>(d_rel_common);
+    a.sminspan = g.d_sminspan;
+    a.nchans = g.nchans;
+    a.ndms = g.ndms;
+    a.nsamp = g.nsamp;
+    a.nblk = g.nblk;
+    a.rowcap = rawcap;
+    a.nst = g.nst;
+    a.out_i32 = 1;
+    a.ps = ps;
+    a.err = err;
+    a.mom = mom;
+    a.mom_group_rows = g.ndms;
+    return a;
+}
 
 // Tile S[g][d][c] for the kernel.  Fails if any shift is negative.  uint8 and uint16 samples
 // use the packed kernels (Db 38 / 16, T 512) unless g.kernel == 1 asks for the generic one or

@@ -141,6 +141,50 @@ struct BatchState {
     size_t smem = 0;
 };
 
+// ----------------------------------------------------------------------------------------
+// fused batched launch (dedisp.cu): clip, dedisperse and boxcar-search uint8 beams in one
+// persistent launch; see k_batch_fused
+// ----------------------------------------------------------------------------------------
+struct FusedBeam {
+    unsigned char *in;          // uint8 block [nchans][in_stride]
+    long long in_stride;        // elements
+    long long ncols;            // nsamp + maxshift: the columns the clip covers
+    int nchans, ndms, nsamp;
+    unsigned nspec_items;       // phase-2 items of this beam
+    unsigned ndd_done;          // phase-3 completions of this beam (items x compute warps)
+    const int32_t *out;         // int32 series [ndms][out_stride]
+    long long out_stride;
+    unsigned long long *mom;    // [ndms][3] exact row moments
+    DevCand *cands;             // [cap]
+    unsigned long long *count;
+};
+
+struct FusedArgs {
+    const FusedBeam *fb;
+    const int2 *cc_items;       // (beam, channel)
+    const int2 *cs_items;       // (beam, first column)
+    const int4 *bx_items;       // (beam, row, first tile, last tile + 1)
+    int n_cc, n_cs, n_bx;
+    unsigned *counters;         // [4], zero at the start of the launch
+    unsigned *done;             // [nbeams][3], zero at the start of the launch
+    double k_chan, k_spec, threshold;
+    long long cap;
+    unsigned *err;
+};
+
+struct FusedShapeInfo {
+    int dm_block, time_tile, compute_warps;
+};
+int fused_num_shapes();
+FusedShapeInfo fused_shape_info(int shape);
+mdsm_status fused_tables(int shape, StageGeom &g, const std::vector<int32_t> &S);
+KArgs fused_kargs(const StageGeom &g, const void *d_rel_common, const unsigned char *in,
+                  long long in_stride, int32_t *out, long long out_stride, int rawcap, int ps,
+                  unsigned long long *mom, unsigned *err);
+mdsm_status fused_launch(int shape, const FusedArgs &f, const KArgs *d_kargs,
+                         const int4 *d_items, int n_dd, int rawcap, int ps, cudaStream_t st);
+constexpr int kFusedSpecColsHost = 512;  // columns of one spectrum-clip item
+
 mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams);
 mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in,
                               const std::vector<long long> &in_stride,

@@ -115,3 +115,83 @@ def test_batch_autotune_and_fused_clip_detect(lib, orc, cuda):
         assert np.array_equal(c["dm_idx"], dm) and np.array_equal(c["sample"], samp)
         assert np.array_equal(c["width"], wid) and np.array_equal(c["snr"], snr)
     b.close()
+
+
+def _restore(torch, xs, d_in):
+    for x, t in zip(xs, d_in):
+        t[: x.size].copy_(torch.from_numpy(x.ravel()))
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_fused_launch_every_shape_equals_oracle(lib, orc, cuda, graph):
+    """The fused form (every beam uint8 -> int32, widths 1..256): clip, dedispersion and search
+    in one persistent launch.  For every tile shape and item order the autotuner can pick, the
+    clipped inputs, the series and each beam's candidates equal the oracle's clip, dedispersion
+    and boxcar search."""
+    from mdsm_gb300 import synth
+    from mdsm_gb300.batch import Batch, choice_info
+    torch = cuda
+    plans, xs, d_in, d_out = _setup(torch, seed=20)
+    for k, p in enumerate(plans):
+        nch, stride = p.input_shape()
+        x = synth.gaussian_u8(nch, stride, 60 + k)
+        synth.inject(x, FCH1, -BW / nch, TSAMP, [(400 + 150 * k, 15.0, 3 + k, 45.0)],
+                     K=4148.741601)
+        x[:, 100 + 7 * k] = 255   # broadband impulses for the spectrum clip
+        x[3 + k, ::50] = 0        # a channel with dropouts for the channel clip
+        xs[k] = x
+    _restore(torch, xs, d_in)
+    want = []
+    for p, x in zip(plans, xs):
+        info = p.info
+        xc = orc.rfi_clip(x.copy(), info.nsamp + info.maxshift, 4.0, 4.0)
+        y = orc.dedisperse(xc, p.shift_table(), info.nsamp)
+        want.append((xc, y, orc.boxcar_detect(y, 9, 6.0)))
+    b = Batch(plans)
+    b.set_buffers(d_in, d_out)
+    b.enable_clip(4.0, 4.0)
+    b.enable_detect(nwidths=9, threshold=6.0, cap=8192)
+    ran = 0
+    for choice in range(10, 18):
+        try:
+            _set_choice(b, choice)
+        except Exception:
+            continue  # this tile shape's staging does not fit some beam
+        assert choice_info(choice)["fused"] == 1
+        for rep in range(2):  # (graph: the first run captures, the second replays)
+            _restore(torch, xs, d_in)
+            for t in d_out:
+                t.zero_()
+            b.run(graph=graph)
+            torch.cuda.synchronize()
+        assert graph or b.last_launches == 1
+        for k, p in enumerate(plans):
+            info_k = p.info
+            xc, y, (dm, samp, wid, snr) = want[k]
+            nch, stride = p.input_shape()
+            got_in = d_in[k][: nch * stride].view(nch, stride)[:, : info_k.nsamp + info_k.maxshift]
+            assert np.array_equal(got_in.cpu().numpy(), xc), (choice, k)
+            assert np.array_equal(d_out[k].cpu().numpy(), y), (choice, k)
+            c = b.candidates(k)
+            assert len(dm) > 0
+            assert np.array_equal(c["dm_idx"], dm) and np.array_equal(c["sample"], samp), (choice, k)
+            assert np.array_equal(c["width"], wid) and np.array_equal(c["snr"], snr), (choice, k)
+        ran += 1
+    assert ran >= 4
+    b.close()
+
+
+def test_fused_autotune_picks_a_fused_shape(lib, cuda):
+    from mdsm_gb300.batch import Batch, choice_info
+    torch = cuda
+    plans, xs, d_in, d_out = _setup(torch, seed=30)
+    b = Batch(plans)
+    b.set_buffers(d_in, d_out)
+    b.enable_detect(nwidths=9, threshold=6.0, cap=1024)
+    c = b.autotune()
+    info = choice_info(c)
+    assert info["fused"] == 1 and info["dm_block"] in (32, 38)
+    assert info["time_tile"] in (256, 512, 768)
+    b.run(graph=True)
+    torch.cuda.synchronize()
+    b.close()

@@ -324,11 +324,18 @@ mdsm_status pass(mdsm_batch *b, int choice, cudaStream_t st)
         FusedRun &z = b->fz;
         if (b->fz_dirty || z.shape != shape || z.order != order || z.clip != b->clip ||
             z.detect != b->detect) {
-            MDSM_TRY(fused_build(b, shape, order, b->clip, b->detect));
+            if (fused_build(b, shape, order, b->clip, b->detect) != MDSM_OK) {
+                // a beam's staging does not fit the fused launch: the unfused pass from now on
+                fused_free(b->fz);
+                b->fusable = false;
+                b->choice = choice = 0;
+                goto unfused;
+            }
             b->fz_dirty = false;
         }
         return fused_pass(b, st);
     }
+unfused:
     if (b->clip)
         for (size_t i = 0; i < nb; ++i) {
             const Plan &p = b->plans[i]->p;
@@ -462,9 +469,11 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
 {
     if (!b || !b->buffers) return fail(MDSM_ESTATE, "batch: set buffers first");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    const bool fused = fused_wanted(b);
+    bool fused = fused_wanted(b);
+    // (the beams' geometry decides whether they fit the fused launch; the search settings
+    // decide whether it is wanted)
     const std::string key =
-        geometry_key(b) + (fused ? "fused" : "") + (b->detect ? "det" : "");
+        geometry_key(b) + (b->detect ? "det" + std::to_string(b->nwidths) : "");
     int best = cache_lookup(key);
     if (best < 0) {
         const bool clip = b->clip;
@@ -478,11 +487,26 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
         std::vector<int> cands;
         if (fused)
             for (int c = 0; c < 2 * fused_num_shapes(); ++c) cands.push_back(kFusedChoice0 + c);
-        else
-            cands = {0, 1, 2};
+        cands.push_back(0);  // the unfused shapes, timed only where no fused shape fits
+        cands.push_back(1);
+        cands.push_back(2);
+        std::string why;
         for (int c : cands) {
-            if (c >= kFusedChoice0 && pass(b, c, st) != MDSM_OK) continue;  // does not fit
-            if (c < kFusedChoice0) MDSM_TRY(pass(b, c, st));
+            if (c < kFusedChoice0 && best >= kFusedChoice0) break;
+            if (c < kFusedChoice0 && fused) {
+                // no fused shape fits: the unfused shapes, the dedispersion launch alone
+                fused = false;
+                b->detect = false;
+                b->fusable = false;
+            }
+            if (c >= kFusedChoice0 && fused_build(b, (c - kFusedChoice0) / 2,
+                                                  (c - kFusedChoice0) % 2, false,
+                                                  b->detect) != MDSM_OK) {
+                why = mdsm_last_error();  // a beam's staging does not fit this shape
+                continue;
+            }
+            if (c >= kFusedChoice0) b->fz_dirty = false;
+            MDSM_TRY(pass(b, c, st));
             MDSM_CUDA_TRY(cudaEventRecord(e0, st));
             for (int r = 0; r < 2; ++r) MDSM_TRY(pass(b, c, st));
             MDSM_CUDA_TRY(cudaEventRecord(e1, st));
@@ -498,7 +522,9 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
         cudaEventDestroy(e1);
         b->clip = clip;
         b->detect = det;
-        if (best < 0) return fail(MDSM_EINVAL, "batch: no launch shape fits these beams");
+        if (best < 0)
+            return fail(MDSM_EINVAL, "batch: no launch shape fits these beams (" + why + ")");
+        if (best < kFusedChoice0) fused_free(b->fz);
         cache_store(key, best);
     }
     b->choice = best;

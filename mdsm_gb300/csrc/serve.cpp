@@ -389,7 +389,6 @@ mdsm_status add_beam(mdsm_server *sv, mdsm_plan *plan, int *beam)
         const size_t det = boxcar_work_bytes(p.ndms, p.nsamp, S.desc.cand_cap);
         if (sl.det_bytes < det) {
             if (sl.d_det) cudaFree(sl.d_det);
-        if (sl.d_mom) cudaFree(sl.d_mom);
             MDSM_CUDA_TRY(cudaMalloc(&sl.d_det, det));
             sl.det_bytes = det;
         }

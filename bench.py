@@ -14,9 +14,13 @@ serving: the serving form on 64 beams x 2^16-sample blocks x 4096 DM trials (eve
         latency, real-time factor, and the ratio to the plain per-block path on the same blocks
         (same algorithm; detections compared block by block); a run at Poisson arrivals of
         1.0-1.5x real time; the first subband stage's add rate; clocks sampled meanwhile.
+batched: the batched form on 32 uneven beams (RFI clip, dedispersion and boxcar search as one
+        fused persistent launch in a CUDA graph, launch shape autotuned) against the plain
+        per-beam path on the same blocks, detections compared beam by beam; clocks sampled.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
        python bench.py --case serve   (the serving object alone)
+       python bench.py --case batch   (the batched object alone)
 For N > 1 run under torch.distributed.run; each rank processes its own beam (weak scaling).
 """
 import argparse
@@ -461,70 +465,130 @@ def serving_object(args, local=0):
     return out
 
 
-def run_batch(args):
-    """Batched form: 32 beams, blocks of 2^14..2^18 samples, 1024 or 4096 channels, each with
-    its own DM plan (1024-4096 trials to 500-2000), uint8; one persistent dedispersion launch
-    (plus clip before and boxcar search after) replayed as one CUDA graph, launch shape
-    chosen by the autotuner."""
+def batch_workload(nbeams, seed=4):
+    """Config 4's beams: 2^14..2^18 samples, 1024 or 4096 channels, 1024-4096 DM trials (in
+    32s) to 500-2000, Gaussian uint8 (mean 128, sigma 16) with two dispersed pulses each,
+    generated on the device.  Returns [(plan, host copy of the block)]."""
     import torch
 
     import mdsm_gb300 as m
-    from mdsm_gb300.batch import Batch
-    rng = np.random.default_rng(4)
-    gen = torch.Generator(device="cuda")
-    gen.manual_seed(7)
-    plans, d_in, d_out = [], [], []
-    for b in range(args.batch_beams):
+    from mdsm_gb300 import synth
+    rng = np.random.default_rng(seed)
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed + 3)
+    out = []
+    for b in range(nbeams):
         nsamp = 1 << int(rng.integers(14, 19))
         nch = int(rng.choice([1024, 4096]))
         ndms = int(rng.integers(32, 129)) * 32
         maxdm = float(rng.uniform(500, 2000))
         p = m.BrutePlan(nch, FCH1, -BW / nch, TSAMP, nsamp, [(0.0, maxdm / ndms, ndms)],
                         in_dtype="u8", out_dtype="i32")
-        t = p.alloc_input()
-        n = p.info.nchans * p.info.in_stride
-        v = torch.randn(n, generator=gen, device="cuda")
-        t[:n].copy_(torch.clamp(torch.round(v * 16 + 128), 0, 255).to(torch.uint8))
+        i = p.info
+        ncols = nsamp + i.maxshift
+        v = torch.empty((nch, i.in_stride), device="cuda")
+        v.normal_(128.0, 16.0, generator=g)
+        for t0, dm, w, amp in synth.random_pulses(rng, 2, nsamp - 64, 0.9 * maxdm, 16.0, nch,
+                                                  widths=(1, 32), snr=(15, 40)):
+            dl = synth.pulse_delays(nch, FCH1, -BW / nch, TSAMP, dm)
+            idx = torch.from_numpy((t0 + dl)[:, None] + np.arange(w)[None, :]).cuda()
+            v.scatter_add_(1, idx.clamp(max=ncols - 1),
+                           torch.full(idx.shape, float(amp), device="cuda"))
+        x = torch.clamp(torch.round(v), 0, 255).to(torch.uint8).cpu().numpy()
         del v
-        plans.append(p)
-        d_in.append(t)
-        d_out.append(p.alloc_output())
+        out.append((p, x))
+    return out
+
+
+def batch_object(args, local=0):
+    """The batched form on config 4: the beams' clip, dedispersion and boxcar search as one
+    pass (the fused persistent launch where the beams allow it) replayed as a CUDA graph, with
+    the launch shape the autotuner picks; against the plain per-beam path on the same blocks
+    (clip, dedispersion, search and candidates back, one beam after another), detections
+    compared beam by beam."""
+    import torch
+
+    import mdsm_gb300 as m
+    from mdsm_gb300.batch import Batch, choice_info
+    beams = batch_workload(args.batch_beams)
+    plans = [p for p, _ in beams]
+    d_in = [p.alloc_input() for p in plans]
+    d_out = [p.alloc_output() for p in plans]
+
+    def load_inputs():
+        for (p, x), t in zip(beams, d_in):
+            t[: x.size].copy_(torch.from_numpy(x.ravel()))
+
     batch = Batch(plans)
     batch.set_buffers(d_in, d_out)
-    if args.batch_fused:
-        batch.enable_clip(4.0, 4.0)
-        batch.enable_detect(nwidths=9, threshold=6.0, cap=4096)
+    batch.enable_clip(4.0, 4.0)
+    batch.enable_detect(nwidths=9, threshold=6.0, cap=4096)
+    load_inputs()
     choice = batch.autotune()
     stream = torch.cuda.current_stream()
-    for _ in range(args.warmup):
-        batch.run(graph=True)
+    # detections of one pass on fresh inputs
+    load_inputs()
+    batch.run(graph=True)  # (runs and captures)
     torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        batch.run(graph=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / args.steps
+    bc = [batch.candidates(k) for k in range(len(plans))]
     units = sum(p.info.ndms * p.info.nsamp for p in plans)
-    adds = sum(float(p.info.ndms) * p.info.nsamp * p.info.nchans for p in plans)
-    packed = sum(1 for p in plans if p.info.kernel == 2)
     data_s = sum(p.info.nsamp * TSAMP for p in plans)
-    line = {"metric": METRIC, "value": units / (ms / 1e3), "unit": METRIC, "n_gpus": 1,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
-            "data": "synthetic (seeded Gaussian uint8 on the device)",
-            "config": {"workload": "batched: %d beams, 2^14-2^18 samples, 1024/4096 ch, "
-                                   "1024-4096 DM trials to 500-2000, %s, one CUDA graph"
-                                   % (args.batch_beams, "clip+dedisperse+boxcar"
-                                      if args.batch_fused else "dedisperse"),
-                       "autotune_choice": ["persistent tile-major", "persistent DM-block-major",
-                                           "one launch per beam"][choice],
-                       "packed_beams": packed},
-            "real_time_factor": data_s / (ms / 1e3),
-            "add_rate_tadd_s": adds / (ms / 1e3) / 1e12}
-    print(json.dumps(line), flush=True)
+
+    def plain_pass():
+        cands = []
+        for p, t, o in zip(plans, d_in, d_out):
+            i = p.info
+            m.rfi_clip_device(t, i.nchans, i.in_stride, i.nsamp + i.maxshift, 4.0, 4.0,
+                              dtype="u8", stream=stream)
+            p.dedisperse_device(t, o, stream=stream)
+            cands.append(m.boxcar_detect_device(o, nwidths=9, threshold=6.0, cap=4096,
+                                                stream=stream)[0])
+        return cands
+
+    load_inputs()
+    pc = plain_pass()
+    ident = all(same_cands(a, b) for a, b in zip(bc, pc))
+    res = {"workload": "batched: %d beams, 2^14-2^18 samples, 1024/4096 ch, 1024-4096 DM trials "
+                       "to 500-2000, uint8, RFI clip 4 sigma + dedispersion + boxcar widths "
+                       "1..256 at 6 sigma" % len(plans),
+           "data": "seeded Gaussian uint8 (mean 128, sigma 16) with two dispersed pulses per "
+                   "beam, generated on the device",
+           "autotune_choice": choice_info(choice),
+           "detections_identical_to_plain": bool(ident),
+           "candidates": int(sum(len(c) for c in bc))}
+    with ClockSampler(local) as clk:
+        for _ in range(args.warmup):
+            batch.run(graph=True)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            batch.run(graph=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / args.steps
+        plain_pass()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(max(1, args.steps // 2)):
+            plain_pass()
+        torch.cuda.synchronize()
+        plain_ms = (time.perf_counter() - t0) * 1e3 / max(1, args.steps // 2)
+    res.update({"value": units / (ms / 1e3), "unit": METRIC, "ms_per_pass": ms,
+                "real_time_factor": data_s / (ms / 1e3), "launches_per_pass": batch.last_launches,
+                "plain": {"value": units / (plain_ms / 1e3), "ms_per_pass": plain_ms,
+                          # per beam: two clips, the dedispersion, statistics and search
+                          "launches_per_pass": 5 * len(plans)},
+                "vs_plain": plain_ms / ms, "clocks": clk.summary()})
     batch.close()
+    return res
+
+
+def run_batch(args):
+    """The batched form alone (config 4), as its own JSON line."""
+    import torch
+    torch.cuda.set_device(0)
+    print(json.dumps({"batched": batch_object(args)}), flush=True)
 
 
 def run_stage(args):
@@ -677,7 +741,8 @@ def main():
                     help="leave the serving object out of the default line")
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--batch-beams", type=int, default=32)
-    ap.add_argument("--batch-fused", type=int, default=1)
+    ap.add_argument("--no-batched", action="store_true",
+                    help="leave the batched object out of the default line")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.case == "serve":
@@ -837,6 +902,9 @@ def main():
         plan = None
         torch.cuda.empty_cache()
         line["serving"] = serving_object(args, local)
+        torch.cuda.empty_cache()
+    if world == 1 and args.case == "full" and not args.no_batched:
+        line["batched"] = batch_object(args, local)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:

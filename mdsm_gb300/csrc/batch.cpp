@@ -31,7 +31,6 @@ struct FusedRun {
     int shape = -1, order = 0;
     bool clip = false, detect = false;
     std::vector<StageGeom> geoms;      // per beam, this shape's tables (device copies owned)
-    std::vector<void *> d_rel;         // per beam, offsets with the common phase stride
     int rawcap = 0, ps = 0, n_dd = 0;
     FusedArgs f{};
     void *d_kargs = nullptr, *d_fb = nullptr, *d_dd = nullptr, *d_cc = nullptr, *d_cs = nullptr,
@@ -81,8 +80,6 @@ namespace {
 void fused_free(FusedRun &z)
 {
     for (StageGeom &g : z.geoms) free_stage(g);
-    for (void *p : z.d_rel)
-        if (p) cudaFree(p);
     for (void *p : {z.d_kargs, z.d_fb, z.d_dd, z.d_cc, z.d_cs, z.d_bx})
         if (p) cudaFree(p);
     if (z.d_sync) cudaFree(z.d_sync);
@@ -135,14 +132,8 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
         z.rawcap = std::max(z.rawcap, z.geoms[i].rowcap);
         z.ps = std::max(z.ps, z.geoms[i].ps);
     }
-    z.d_rel.assign(nb, nullptr);
-    for (size_t i = 0; i < nb; ++i) {  // offsets re-expressed with the common phase stride
-        const StageGeom &g = z.geoms[i];
-        std::vector<int32_t> rel(g.rel.size());
-        for (size_t j = 0; j < rel.size(); ++j)
-            rel[j] = g.rel[j] / g.ps * z.ps + g.rel[j] % g.ps;
-        MDSM_TRY(upload(rel, &z.d_rel[i]));
-    }
+    // (each beam keeps its own phase stride and offsets: the launch expands a beam's chunks
+    // with its stride; the shared-memory buffers are sized for the widest)
     // moments and candidates
     std::vector<size_t> mom_off(nb);
     for (size_t i = 0; i < nb; ++i) {
@@ -164,15 +155,15 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
     std::vector<FusedBeam> fb(nb);
     std::vector<int4> dd, bx;
     std::vector<int2> cc, cs;
-    const int kFusedBoxTile = 2048, tpc = 4;
+    const int kFusedBoxTile = 2048, tpc = 16;  // search items: runs of up to 16 tiles
     for (int i : beams) {
         const Plan &p = b->plans[i]->p;
         const StageGeom &g = z.geoms[i];
         unsigned char *in = static_cast<unsigned char *>(const_cast<void *>(b->in[i]));
         int32_t *out = static_cast<int32_t *>(b->out[i]);
         unsigned long long *mom = z.d_mom + mom_off[i];
-        ka[i] = fused_kargs(g, z.d_rel[i], in, b->in_stride[i], out, b->out_stride[i], z.rawcap,
-                            z.ps, mom, b->d_err);
+        ka[i] = fused_kargs(g, g.d_rel, in, b->in_stride[i], out, b->out_stride[i], z.rawcap,
+                            g.ps, mom, b->d_err);
         const long long ncols = (long long)p.nsamp + p.maxshift;
         const int ntiles = (p.nsamp + g.T - 1) / g.T;
         const size_t dd0 = dd.size();

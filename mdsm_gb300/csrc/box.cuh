@@ -2,9 +2,10 @@
 // standalone search kernel (detect.cu) and the fused batched launch (dedisp.cu).
 //
 // Widths 1, 2, 4, ..., 2^(NW-1); per DM row the mean and sigma come from the caller.  A run of
-// consecutive 2048-sample tiles of one row is searched by THREADS threads of the calling CTA
-// (every thread of the CTA calls box_run: it holds the CTA barriers; threads at or past THREADS
-// only take part in them).  The samples of the next tile are copied into shared memory
+// consecutive 2048-sample tiles of one row is searched by a group of THREADS threads: the
+// whole CTA (BoxBarCta) or one of several groups of a CTA, each with its own named barrier and
+// shared memory (BoxBarGroup), so that one wide CTA runs several searches whose barriers
+// overlap.  The samples of the next tile are copied into shared memory
 // (cp.async) while the current one is searched.  Arithmetic per sample and width is FP32,
 // explicitly rounded, in the oracle's order; each thread owns the position pairs
 // (2 tid + 2 THREADS q, +1), keeps their boxcar sums and best SNR in registers across the
@@ -64,9 +65,10 @@ struct BoxGeom {
     // floats; even, so the second buffer and the pairs in it stay 8-byte aligned
     static constexpr int BUF = PAIRS * 2 * THREADS + (WMAX < 2 ? 2 : WMAX);
     // shared memory of box_run: two sum buffers, the best SNR of NBEST positions, the next
-    // tile's samples
+    // tile's samples, 1 / (sigma sqrt(w)) per width (16 floats)
     static constexpr size_t SMEM =
-        (size_t)BUF * 8 + (size_t)NBEST * 4 + (size_t)PAIRS * 2 * THREADS * 4;
+        (size_t)BUF * 8 + (size_t)NBEST * 4 + (size_t)PAIRS * 2 * THREADS * 4 + 64;
+    static_assert(NW <= 16, "widths");
     static_assert(BUF % 2 == 0 && NBEST % 2 == 0, "pairs of positions");
     static_assert((THREADS & (THREADS - 1)) == 0, "power-of-two thread count");
 };
@@ -124,6 +126,34 @@ __device__ __forceinline__ void box_prefetch(uint32_t *NB, const T *__restrict__
     cp_async_commit();
 }
 
+// The search group's barriers.  BoxBarCta: the group is the whole CTA (threads at or past
+// the group's size only take part in the barriers).  BoxBarGroup: named barrier `id` (1..15)
+// of `count` threads, a multiple of 32 (whole warps).
+struct BoxBarCta {
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ __forceinline__ bool any(bool p) const { return __syncthreads_or(p) != 0; }
+};
+struct BoxBarGroup {
+    int id, count;
+    __device__ __forceinline__ void sync() const
+    {
+        asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+    }
+    __device__ __forceinline__ bool any(bool p) const
+    {
+        unsigned r;
+        asm volatile(
+            "{\n\t.reg .pred p, q;\n\t"
+            "setp.ne.u32 p, %1, 0;\n\t"
+            "bar.red.or.pred q, %2, %3, p;\n\t"
+            "selp.u32 %0, 1, 0, q;\n\t}"
+            : "=r"(r)
+            : "r"((unsigned)p), "r"(id), "r"(count)
+            : "memory");
+        return r != 0;
+    }
+};
+
 template <typename T>
 __device__ __forceinline__ float box_value(uint32_t raw)
 {
@@ -134,32 +164,32 @@ __device__ __forceinline__ float box_value(uint32_t raw)
 }
 
 // Tiles [tile_lo, tile_hi) of row r (n samples, DM index d) with the row's mean and sigma
-// (sigma > 0); sm holds BoxGeom<NW, THREADS>::SMEM bytes.  Candidates (d, sample, width, snr)
-// go to cands[atomicAdd(count)] below cap.  ALL: the CTA has exactly THREADS threads.  When
-// it returns, no copy is in flight (the last tile prefetches nothing).
-template <typename T, int NW, int THREADS, bool ALL>
+// (sigma > 0), searched by the calling group: `active` threads with group index tid in
+// [0, THREADS) (every thread of the group's barrier calls it); sm holds
+// BoxGeom<NW, THREADS>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr) go
+// to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight (the last tile
+// prefetches nothing); the caller synchronises the group before sm is written again.
+template <typename T, int NW, int THREADS, class Bar>
 __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, long long tile_lo,
                                         long long tile_hi, double mu, double sig, double threshold,
                                         int d, DevCand *__restrict__ cands,
                                         unsigned long long *__restrict__ count, long long cap,
-                                        unsigned char *sm)
+                                        unsigned char *sm, const Bar &bar, int tid_in, bool active)
 {
     using G = BoxGeom<NW, THREADS>;
     constexpr int HL = G::HL, NBEST = G::NBEST, PAIRS = G::PAIRS;
     float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
     float *best_s = B1 + G::BUF;
     uint32_t *NB = reinterpret_cast<uint32_t *>(best_s + NBEST);  // next tile's samples
-    const bool active = ALL || threadIdx.x < THREADS;
+    float *inv_w = reinterpret_cast<float *>(NB + PAIRS * 2 * THREADS);
     // (the mask tells the compiler tid < THREADS, so range tests fold at compile time for all
     // but the last pair)
-    const int tid = threadIdx.x & (THREADS - 1);
+    const int tid = tid_in & (THREADS - 1);
     const float mu_f = __double2float_rn(mu);
     const float thr = __double2float_rn(threshold);
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
-    __shared__ float inv_w[NW];
-    if (threadIdx.x < NW)
-        inv_w[threadIdx.x] = __double2float_rn(
-            __ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << threadIdx.x)))));
+    if (active && tid < NW)
+        inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
     // every staged sample and every boxcar of the tile inside the series: no per-element tests
     auto inside = [&](long long tile) {
         const long long r0 = tile * kBoxTile - HL;
@@ -183,7 +213,7 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
         }
         if (active && tile + 1 < tile_hi)  // in flight while this tile is searched
             box_prefetch<T, PAIRS, THREADS>(NB, r, r0 + kBoxTile, n, tid);
-        __syncthreads();  // B0 written (each thread reads back only its own NB words)
+        bar.sync();  // B0 (and inv_w) written (each thread reads back only its own NB words)
 #pragma unroll
         for (int l = 0; l < NW; ++l) {
             const int w = 1 << l;
@@ -203,7 +233,7 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
                         *reinterpret_cast<float2 *>(nxt + i) = b[q];
                     }
                 }
-                __syncthreads();
+                bar.sync();
             }
             if (active) {
                 const float wm = __fmul_rn((float)w, mu_f);
@@ -232,7 +262,7 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
                 if (2 * tid + 2 * THREADS * q < NBEST) any |= best[q].x >= thr || best[q].y >= thr;
         }
         // most tiles hold no sample over the threshold: skip the neighbourhood test there
-        if (!__syncthreads_or(any)) continue;
+        if (!bar.any(any)) continue;
         if (active) {
 #pragma unroll
             for (int q = 0; q < PAIRS; ++q) {
@@ -240,7 +270,7 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
                 if (i < NBEST) *reinterpret_cast<float2 *>(best_s + i) = best[q];
             }
         }
-        __syncthreads();
+        bar.sync();
         if (active) {
             for (int q = tid; q < kBoxTile; q += THREADS) {
                 const long long t = t0 + q;

@@ -299,6 +299,7 @@ struct OnePlanItems {
     }
     __device__ const KArgs &args(int) const { return *a; }
     __device__ void stored(int) const {}
+    static constexpr bool kBeamStride = false;  // every chunk has the kernel's phase stride
 };
 
 // Items of several plans from a list, taken from a global counter.
@@ -315,6 +316,7 @@ struct ListItems {
     __device__ int4 item(int it) const { return items[it]; }
     __device__ const KArgs &args(int beam) const { return beams[beam]; }
     __device__ void stored(int) const {}
+    static constexpr bool kBeamStride = false;
 };
 
 // The odd samples of a word as 32-bit lanes: uint8, (s1, s3) as uint16 lanes; uint16, s1.
@@ -459,14 +461,25 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             // chunk holds (rows past its channels, or the whole stage at the end of the
             // stream, hold earlier data nobody reads), so the expansion does not wait for the
             // chunk's entry.
-            for (int q = tid; q < kPCC * nq; q += NW * 32) {
-                const int row = (int)(((unsigned)q * nq_inv) >> 20);  // q / nq
-                const int i = q - row * nq;
+            int nwc = nwp, nqc = nq;  // this chunk's phase stride (words) and quads per row
+            unsigned nqc_inv = nq_inv;
+            if constexpr (Src::kBeamStride) {
+                const int4 mm = meta[s];
+                if (mm.x >= 0) {
+                    nwc = src.args(src.item(mm.x).x).ps >> 2;
+                    nqc = nwc >> 2;
+                    nqc_inv = ((1u << 20) + (unsigned)nqc - 1) / (unsigned)nqc;
+                }
+            }
+            for (int q = tid; q < kPCC * nqc; q += NW * 32) {
+                const int row = (int)(((unsigned)q * nqc_inv) >> 20);  // q / nqc
+                const int i = q - row * nqc;
                 const uint32_t *W =
                     reinterpret_cast<const uint32_t *>(raw + (size_t)(s * kPCC + row) * rawcap);
-                // phase-major: copy a of row r at (a * 16 + r) * nwp, so a warp whose quads
-                // cross from one row into the next stores to consecutive addresses
-                uint32_t *Pr = P + ((size_t)pb * SPW * kPCC + row) * nwp;
+                // phase-major: copy a of row r at (a * 16 + r) * nwc from the phase buffer's
+                // start (buffers kPCC * SPW * nwp words apart), so a warp whose quads cross from
+                // one row into the next stores to consecutive addresses
+                uint32_t *Pr = P + (size_t)pb * SPW * kPCC * nwp + (size_t)row * nwc;
                 {
                     uint4 w = reinterpret_cast<const uint4 *>(W)[i];
                     uint32_t w4 = W[4 * i + 4];
@@ -480,7 +493,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                     reinterpret_cast<uint4 *>(Pr)[i] = w;
 #pragma unroll
                     for (int a = 1; a < SPW; ++a)
-                        reinterpret_cast<uint4 *>(Pr + a * kPCC * nwp)[i] =
+                        reinterpret_cast<uint4 *>(Pr + a * kPCC * nwc)[i] =
                             make_uint4(__funnelshift_r(w.x, w.y, 8 * SW * a),
                                        __funnelshift_r(w.y, w.z, 8 * SW * a),
                                        __funnelshift_r(w.z, w.w, 8 * SW * a),
@@ -738,8 +751,10 @@ __global__ void __launch_bounds__(CfgU8::THREADS, 1)
 // phase only when that phase's list is exhausted, so every item an item waits for has already
 // been taken by a running CTA, which depends only on earlier phases: the waits always end.
 constexpr int kFusedSpecCols = kFusedSpecColsHost;  // columns of one phase-2 item (a thread each)
-constexpr int kFusedBoxThreads = 512;
-constexpr int kFusedBoxWidths = 9;   // widths 1..256
+constexpr int kFusedBoxThreads = 128;  // threads of one search group (4 warps)
+constexpr int kFusedBoxWidths = 9;     // widths 1..256
+// shared memory of one search group (16-byte multiple)
+constexpr size_t kFusedBoxSmem = (BoxGeom<kFusedBoxWidths, kFusedBoxThreads>::SMEM + 15) / 16 * 16;
 
 // Bounded wait until *ctr >= target (raised by other CTAs after a fence): polling with
 // backoff, about 4 s at most; on timeout sets ERR_WAIT_TIMEOUT and returns false.
@@ -834,6 +849,9 @@ struct FusedItems {
         __syncwarp();
         if ((threadIdx.x & 31) == 0) atomicAdd(&done[3 * beam + 2], 1u);
     }
+    // each beam's chunks are expanded with the beam's own phase stride (KArgs::ps, at most
+    // the kernel's), so a narrow beam does not expand the widest beam's row length
+    static constexpr bool kBeamStride = true;
 };
 
 template <class Cfg>
@@ -939,28 +957,50 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1)
     }
 
     // ---- phase 4: boxcar search, one run of tiles of one row per item ----
-    for (int it; (it = cta_grab(&f.counters[3], f.n_bx, &slot)) >= 0;) {
+    // The CTA splits into groups of kFusedBoxThreads threads, each taking items on its own
+    // (named barrier 1 + group, its own shared memory), so that one group's barriers overlap
+    // the others' work; warps past the last whole group have nothing to do.
+    constexpr int NG = Cfg::THREADS / kFusedBoxThreads;
+    static_assert(NG >= 1 && NG <= 8, "search groups");
+    __shared__ int g_item[NG], g_ok[NG];
+    __shared__ double g_mu[NG], g_sig[NG];
+    const int grp = tid / kFusedBoxThreads, gt = tid % kFusedBoxThreads;
+    __syncthreads();  // the barriers are invalidated before their memory is reused
+    if (grp >= NG) return;
+    const BoxBarGroup gbar{1 + grp, kFusedBoxThreads};
+    unsigned char *gsm = smem + (size_t)grp * kFusedBoxSmem;
+    for (;;) {
+        gbar.sync();  // the group is done with its previous item and with g_*[grp]
+        if (gt == 0) {
+            const int it = (int)atomicAdd(&f.counters[3], 1u);
+            g_item[grp] = it;
+            if (it < f.n_bx) {
+                const int4 w = f.bx_items[it];
+                const FusedBeam &B = f.fb[w.x];
+                g_ok[grp] = wait_count(&f.done[3 * w.x + 2], B.ndd_done, f.err);
+                // the row's mean and sigma from its folded moments (k_mom_finish's conversion)
+                const unsigned long long *m = B.mom + 3 * (size_t)w.y;
+                const long long s1 = (long long)m[0];
+                const double e2 =
+                    __ddiv_rn(__dadd_rn(__dmul_rn((double)m[2], 18446744073709551616.0),
+                                        (double)m[1]),
+                              (double)B.nsamp);
+                const double mm = __ddiv_rn((double)s1, (double)B.nsamp);
+                const double var = __dadd_rn(e2, -__dmul_rn(mm, mm));
+                g_mu[grp] = mm;
+                g_sig[grp] = var > 0.0 ? __dsqrt_rn(var) : 0.0;
+            }
+        }
+        gbar.sync();
+        const int it = g_item[grp];
+        if (it >= f.n_bx) break;
+        const double mu = g_mu[grp], sig = g_sig[grp];
+        if (!g_ok[grp] || !(sig > 0.0)) continue;  // (uniform across the group)
         const int4 w = f.bx_items[it];
         const FusedBeam &B = f.fb[w.x];
-        if (tid == 0) {
-            s_ok = wait_count(&f.done[3 * w.x + 2], B.ndd_done, f.err);
-            // the row's mean and sigma from its folded moments (k_mom_finish's conversion)
-            const unsigned long long *m = B.mom + 3 * (size_t)w.y;
-            const long long s1 = (long long)m[0];
-            const double e2 = __ddiv_rn(__dadd_rn(__dmul_rn((double)m[2], 18446744073709551616.0),
-                                                  (double)m[1]),
-                                        (double)B.nsamp);
-            const double mm = __ddiv_rn((double)s1, (double)B.nsamp);
-            const double var = __dadd_rn(e2, -__dmul_rn(mm, mm));
-            s_mu = mm;
-            s_sig = var > 0.0 ? __dsqrt_rn(var) : 0.0;
-        }
-        __syncthreads();
-        const double mu = s_mu, sig = s_sig;
-        if (!s_ok || !(sig > 0.0)) continue;  // (uniform across the CTA)
-        box_run<int32_t, kFusedBoxWidths, kFusedBoxThreads, Cfg::THREADS == kFusedBoxThreads>(
+        box_run<int32_t, kFusedBoxWidths, kFusedBoxThreads>(
             B.out + (size_t)w.y * (size_t)B.out_stride, B.nsamp, w.z, w.w, mu, sig, f.threshold,
-            w.y, B.cands, B.count, f.cap, smem);
+            w.y, B.cands, B.count, f.cap, gsm, gbar, gt, true);
     }
 }
 
@@ -1133,7 +1173,7 @@ template <class Cfg>
 size_t fused_smem_t(int rawcap, int ps)
 {
     return std::max(packed_smem<Cfg>(rawcap, ps),
-                    BoxGeom<kFusedBoxWidths, kFusedBoxThreads>::SMEM);
+                    (size_t)(Cfg::THREADS / kFusedBoxThreads) * kFusedBoxSmem);
 }
 
 template <class Cfg>

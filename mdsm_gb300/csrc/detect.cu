@@ -629,8 +629,8 @@ __global__ void __launch_bounds__(kBoxThreads, 5)
     const long long ntiles = (n + kBoxTile - 1) / kBoxTile;
     const long long tile_lo = (long long)blockIdx.x * tpc;
     const long long tile_hi = tile_lo + tpc < ntiles ? tile_lo + tpc : ntiles;
-    box_run<T, NW, kBoxThreads, true>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold,
-                                      d, cands, count, cap, sm);
+    box_run<T, NW, kBoxThreads>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold, d,
+                                cands, count, cap, sm, BoxBarCta{}, (int)threadIdx.x, true);
 }
 
 // The boxcar search of every DM row, for 1..9 widths (a template per width count).

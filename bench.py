@@ -500,6 +500,17 @@ def batch_workload(nbeams, seed=4):
     return out
 
 
+def tune_label(choice):
+    """A readable name for an autotuner choice of the batched form."""
+    from mdsm_gb300.batch import choice_info
+    i = choice_info(choice)
+    if i["fused"]:
+        return "fused %dx%d %s" % (i["dm_block"], i["time_tile"],
+                                   ("tile-major", "block-major")[i["order"]])
+    return ("unfused persistent tile-major", "unfused persistent block-major",
+            "unfused per beam")[i["order"]]
+
+
 def batch_object(args, local=0):
     """The batched form on config 4: the beams' clip, dedispersion and boxcar search as one
     pass (the fused persistent launch where the beams allow it) replayed as a CUDA graph, with
@@ -554,6 +565,8 @@ def batch_object(args, local=0):
            "data": "seeded Gaussian uint8 (mean 128, sigma 16) with two dispersed pulses per "
                    "beam, generated on the device",
            "autotune_choice": choice_info(choice),
+           # every candidate the autotuner timed (search on, clip off): ms per pass
+           "autotune_ms": {tune_label(c): round(t, 2) for c, t in batch.tune_times()},
            "detections_identical_to_plain": bool(ident),
            "candidates": int(sum(len(c) for c in bc))}
     with ClockSampler(local) as clk:

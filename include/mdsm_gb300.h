@@ -347,12 +347,14 @@ mdsm_status mdsm_unpack_device(const void *d_raw, long long nspectra, int nchans
 /*    1..256): clip, dedispersion and search in ONE persistent launch over four work lists   */
 /*    (channel clips, spectrum clips, DM-block x time-tile tiles, search runs) tied by per-   */
 /*    beam completion counts with bounded device waits; the rows' statistics are folded into */
-/*    the dedispersion store.  mdsm_batch_autotune times its tile shapes (DM trials per      */
-/*    block x samples per tile x compute warps) and item orders on the registered buffers     */
-/*    and keeps the fastest.                                                                  */
-/*  * Otherwise clip launches, one persistent dedispersion launch over the packed beams'     */
-/*    tiles (a launch per beam for the rest) and per-beam search launches; the autotuner     */
-/*    picks the dedispersion launch shape.                                                    */
+/*    the dedispersion store.  The fused launch stages every beam with one tile shape, whose */
+/*    shared memory the beam with the widest DM span sizes.                                   */
+/*  * Unfused: clip launches, one persistent dedispersion launch over the packed beams' tiles */
+/*    (a launch per beam for the rest) or one launch per beam with each plan's own tile      */
+/*    shape, then per-beam search launches.                                                   */
+/* mdsm_batch_autotune times, with the search on as configured, the fused tile shapes (DM    */
+/* trials per block x samples per tile x compute warps) and item orders where the beams fit  */
+/* them, and the unfused passes, on the registered buffers, and keeps the fastest.            */
 /* With MDSM_AUTOTUNE_CACHE set to a file path the choice is cached per beam geometry.        */
 typedef struct mdsm_batch_s mdsm_batch;
 mdsm_status mdsm_batch_create(mdsm_plan *const *plans, int nbeams, mdsm_batch **out);
@@ -367,6 +369,10 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice);
 /* use_graph: the first call runs the pass and captures it; later calls replay the graph. */
 mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream);
 int mdsm_batch_last_launches(const mdsm_batch *b);
+/* The candidates the last mdsm_batch_autotune timed (none when it took a cached choice):
+ * *n of them, the first cap written as (choice, milliseconds per pass). */
+mdsm_status mdsm_batch_autotune_times(const mdsm_batch *b, int *choices, float *ms, int cap,
+                                      int *n);
 /* What an autotuner choice means: fused = 1 for the fused launch with its DM trials per block,
  * samples per tile, compute warps and item order (0: a beam's DM blocks of one tile adjacent,
  * 1: a DM block's tiles adjacent); fused = 0 for the unfused shapes, order = 0 persistent

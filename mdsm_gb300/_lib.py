@@ -151,6 +151,8 @@ SIGNATURES = {
     "mdsm_boxcar_detect_device": (_st, [_vp, _i, _i, _i, _i, _d, ctypes.POINTER(Candidate), _ll,
                                         ctypes.POINTER(_ll), _vp]),
     "mdsm_batch_choice_info": (_st, [_i] + [ctypes.POINTER(_i)] * 5),
+    "mdsm_batch_autotune_times": (_st, [_vp, ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_float),
+                                        _i, ctypes.POINTER(_i)]),
     "mdsm_plan_check": (_st, [_vp, _vp]),
     "mdsm_plan_wait_selftest": (_st, [_vp, ctypes.c_uint, _vp]),
     "mdsm_plan_set_stage_timing": (_st, [_vp, _i]),

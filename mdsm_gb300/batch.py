@@ -51,6 +51,15 @@ class Batch:
         check(load().mdsm_batch_autotune(self._h, _stream_ptr(stream), ctypes.byref(c)))
         return c.value
 
+    def tune_times(self):
+        """[(choice, ms per pass)] of the candidates the last autotune timed."""
+        n = ctypes.c_int()
+        check(load().mdsm_batch_autotune_times(self._h, None, None, 0, ctypes.byref(n)))
+        ch = (ctypes.c_int * max(n.value, 1))()
+        ms = (ctypes.c_float * max(n.value, 1))()
+        check(load().mdsm_batch_autotune_times(self._h, ch, ms, n.value, ctypes.byref(n)))
+        return [(ch[i], ms[i]) for i in range(n.value)]
+
     def run(self, graph=True, stream=None):
         check(load().mdsm_batch_run(self._h, int(bool(graph)), _stream_ptr(stream)))
 

@@ -55,6 +55,7 @@ struct mdsm_batch_s {
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     int graph_choice = -1;
+    std::vector<std::pair<int, float>> tune_ms;  // the last tuning: (choice, ms per pass)
     // fused stages
     bool clip = false;
     double k_chan = 0, k_spec = 0;
@@ -452,15 +453,17 @@ mdsm_status mdsm_batch_enable_detect(mdsm_batch *b, int nwidths, double threshol
 }
 
 // Times each candidate twice on the registered buffers (after one warm pass) and keeps the
-// fastest: the fused launch's tile shapes and item orders where the beams allow it, else the
-// unfused dedispersion launch shapes.  The clip is left out of the timed passes (it changes
-// the input in place); the search stays in.  A cached choice for the same beam geometry is
+// fastest: the fused launch's tile shapes and item orders where the beams allow it, and the
+// unfused passes (the persistent dedispersion launch in either item order, or one launch per
+// beam with each plan's own tile shape, each followed by the search launches).  Every
+// candidate does the same work: the clip is left out of the timed passes (it changes the
+// input in place); the search stays in.  A cached choice for the same beam geometry is
 // reused when MDSM_AUTOTUNE_CACHE names a file.
 mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
 {
     if (!b || !b->buffers) return fail(MDSM_ESTATE, "batch: set buffers first");
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    bool fused = fused_wanted(b);
+    const bool fused = fused_wanted(b);
     // (the beams' geometry decides whether they fit the fused launch; the search settings
     // decide whether it is wanted)
     const std::string key =
@@ -470,7 +473,6 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
         const bool clip = b->clip;
         const bool det = b->detect;
         b->clip = false;
-        if (!fused) b->detect = false;  // the unfused shapes: the dedispersion launch alone
         float best_ms = 1e30f;
         cudaEvent_t e0, e1;
         MDSM_CUDA_TRY(cudaEventCreate(&e0));
@@ -478,18 +480,12 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
         std::vector<int> cands;
         if (fused)
             for (int c = 0; c < 2 * fused_num_shapes(); ++c) cands.push_back(kFusedChoice0 + c);
-        cands.push_back(0);  // the unfused shapes, timed only where no fused shape fits
+        cands.push_back(0);
         cands.push_back(1);
         cands.push_back(2);
         std::string why;
+        b->tune_ms.clear();
         for (int c : cands) {
-            if (c < kFusedChoice0 && best >= kFusedChoice0) break;
-            if (c < kFusedChoice0 && fused) {
-                // no fused shape fits: the unfused shapes, the dedispersion launch alone
-                fused = false;
-                b->detect = false;
-                b->fusable = false;
-            }
             if (c >= kFusedChoice0 && fused_build(b, (c - kFusedChoice0) / 2,
                                                   (c - kFusedChoice0) % 2, false,
                                                   b->detect) != MDSM_OK) {
@@ -504,6 +500,7 @@ mdsm_status mdsm_batch_autotune(mdsm_batch *b, void *stream, int *choice)
             MDSM_CUDA_TRY(cudaEventSynchronize(e1));
             float ms = 0;
             MDSM_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+            b->tune_ms.emplace_back(c, ms / 2);
             if (ms < best_ms) {
                 best_ms = ms;
                 best = c;
@@ -561,6 +558,18 @@ mdsm_status mdsm_batch_run(mdsm_batch *b, int use_graph, void *stream)
 }
 
 int mdsm_batch_last_launches(const mdsm_batch *b) { return b ? b->launches : 0; }
+
+mdsm_status mdsm_batch_autotune_times(const mdsm_batch *b, int *choices, float *ms, int cap,
+                                      int *n)
+{
+    if (!b || !n || (cap > 0 && (!choices || !ms))) return fail(MDSM_EINVAL, "null argument");
+    *n = (int)b->tune_ms.size();
+    for (int i = 0; i < std::min(cap, *n); ++i) {
+        choices[i] = b->tune_ms[(size_t)i].first;
+        ms[i] = b->tune_ms[(size_t)i].second;
+    }
+    return MDSM_OK;
+}
 
 mdsm_status mdsm_batch_choice_info(int choice, int *fused, int *dm_block, int *time_tile,
                                    int *warps, int *order)

@@ -9,9 +9,10 @@
 // (cp.async) while the current one is searched.  Arithmetic per sample and width is FP32,
 // explicitly rounded, in the oracle's order; each thread owns the position pairs
 // (2 tid + 2 THREADS q, +1), keeps their boxcar sums and best SNR in registers across the
-// widths and reads only the partner sums B[i + w/2] from shared memory (one 8-byte load per
-// pair), so one width costs per pair one shared load, one shared store, three paired FP32
-// operations, two maxima and one barrier (the sums alternate between two buffers).  Which
+// widths and reads only partner sums from shared memory: two widths per step (B_2u and B_4u
+// from B_u, three 8-byte loads per pair), so two widths cost per pair three shared loads, one
+// shared store, one barrier (the sums alternate between two buffers), and per width three
+// paired FP32 operations and two maxima.  Which
 // width gave the best SNR is needed only where the best passes the threshold (few
 // positions): there box_best_at forms it again, with the same sums.  Candidates are local
 // maxima of the best SNR over max(w/2, 1) samples on each side.
@@ -29,27 +30,40 @@ namespace mdsm {
 constexpr int kBoxTile = 2048;   // output samples per tile
 
 // Two FP32 lanes at once (Blackwell add/mul.f32x2, each lane rounded to nearest as the scalar
-// operation would be).
-__device__ __forceinline__ unsigned long long f2_bits(float2 v)
-{
-    return (unsigned long long)__float_as_uint(v.x) |
-           ((unsigned long long)__float_as_uint(v.y) << 32);
-}
-__device__ __forceinline__ float2 bits_f2(unsigned long long v)
-{
-    return make_float2(__uint_as_float((unsigned)v), __uint_as_float((unsigned)(v >> 32)));
-}
+// operation would be).  The operands are formed as register pairs (mov.b64 of two .f32), so
+// packing costs no integer instructions.
 __device__ __forceinline__ float2 add_f2(float2 a, float2 b)
 {
-    unsigned long long d;
-    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-    return bits_f2(d);
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
 }
 __device__ __forceinline__ float2 mul_f2(float2 a, float2 b)
 {
-    unsigned long long d;
-    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(f2_bits(a)), "l"(f2_bits(b)));
-    return bits_f2(d);
+    float2 d;
+    asm("{\n\t.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+
+// max(a, b, c) in one instruction (three-input max.f32, sm_100 and later); for values that
+// are not NaN the same as two two-input maxima.
+__device__ __forceinline__ float fmax3(float a, float b, float c)
+{
+    float r;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(r) : "f"(a), "f"(b), "f"(c));
+    return r;
 }
 
 // Staged samples for NW widths: the region [t0 - HL, t0 + TILE + HL + wmax - 1), rounded up to
@@ -114,15 +128,26 @@ __device__ __forceinline__ void box_prefetch(uint32_t *NB, const T *__restrict__
                                              long long n, int tid)
 {
     static_assert(sizeof(T) == 4, "4-byte samples");
+    const bool inside = r0 >= 0 && r0 + PAIRS * 2 * THREADS <= n;
+    if (inside && ((uintptr_t)(r + r0) & 7) == 0) {
+        // the whole region inside the series, pairs 8-byte aligned: one 8-byte copy a pair
+        const T *base = r + r0;
 #pragma unroll
-    for (int q = 0; q < PAIRS; ++q)
-#pragma unroll
-        for (int e = 0; e < 2; ++e) {
-            const int i = 2 * tid + 2 * THREADS * q + e;
-            const long long t = r0 + i;
-            const bool in = t >= 0 && t < n;
-            cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
+        for (int q = 0; q < PAIRS; ++q) {
+            const int i = 2 * tid + 2 * THREADS * q;
+            cp_async8(NB + i, base + i);
         }
+    } else {
+#pragma unroll
+        for (int q = 0; q < PAIRS; ++q)
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const int i = 2 * tid + 2 * THREADS * q + e;
+                const long long t = r0 + i;
+                const bool in = t >= 0 && t < n;
+                cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
+            }
+    }
     cp_async_commit();
 }
 
@@ -199,14 +224,15 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
         const long long t0 = tile * kBoxTile;
         const long long r0 = t0 - HL;  // series index of B[0] and best[0]
-        const bool interior = inside(tile);
+        const bool interior = inside(tile);  // (uniform across the group)
         float2 b[PAIRS], best[PAIRS];
         if (active) {
             cp_async_wait_all();
 #pragma unroll
             for (int q = 0; q < PAIRS; ++q) {
                 const int i = 2 * tid + 2 * THREADS * q;
-                b[q] = make_float2(box_value<T>(NB[i]), box_value<T>(NB[i + 1]));
+                const uint2 raw = *reinterpret_cast<const uint2 *>(NB + i);
+                b[q] = make_float2(box_value<T>(raw.x), box_value<T>(raw.y));
                 *reinterpret_cast<float2 *>(B0 + i) = b[q];
                 best[q] = make_float2(-INFINITY, -INFINITY);
             }
@@ -214,47 +240,94 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
         if (active && tile + 1 < tile_hi)  // in flight while this tile is searched
             box_prefetch<T, PAIRS, THREADS>(NB, r, r0 + kBoxTile, n, tid);
         bar.sync();  // B0 (and inv_w) written (each thread reads back only its own NB words)
+        // The widths of this tile, compiled twice: for tiles whose every staged sample and
+        // boxcar lies inside the series (no per-position range tests) and for the edges.
+        auto widths = [&](auto interior_tag) {
+            constexpr bool INTERIOR = decltype(interior_tag)::value;
+            // SNR of the pair's width-2^l sums v
+            auto snr = [&](float2 v, int l) {
+                const float wm = __fmul_rn((float)(1 << l), mu_f);
+                const float inv = inv_w[l];
+                return mul_f2(add_f2(v, make_float2(-wm, -wm)), make_float2(inv, inv));
+            };
+            // best SNR of pair q over widths 2^l (sums v) and, when l4 >= 0, 2^l4 (sums v4).
+            // Interior tiles need no range tests and keep values at positions past NBEST
+            // (never read); edge tiles take each width where its boxcar lies in the series.
+            auto score = [&](int q, float2 v, int l, float2 v4, int l4) {
+                const int i = 2 * tid + 2 * THREADS * q;
+                if (INTERIOR) {
+                    const float2 sv = snr(v, l);
+                    if (l4 >= 0) {
+                        const float2 s4 = snr(v4, l4);
+                        best[q].x = fmax3(best[q].x, sv.x, s4.x);
+                        best[q].y = fmax3(best[q].y, sv.y, s4.y);
+                    } else {
+                        best[q].x = fmaxf(best[q].x, sv.x);
+                        best[q].y = fmaxf(best[q].y, sv.y);
+                    }
+                    return;
+                }
+                if (i >= NBEST) return;  // i even and NBEST even: i + 1 < NBEST too
+                const long long t = r0 + i;
 #pragma unroll
-        for (int l = 0; l < NW; ++l) {
-            const int w = 1 << l;
-            if (l > 0) {
-                // B_w[i] = B_{w/2}[i] + B_{w/2}[i + w/2]; B_{w/2} is in B0 for odd l, else B1
-                const int h = w >> 1;
-                const float *cur = (l & 1) ? B0 : B1;
-                float *nxt = (l & 1) ? B1 : B0;
+                for (int k = 0; k < 2; ++k) {
+                    const int lk = k ? l4 : l;
+                    if (lk < 0) continue;
+                    const int w = 1 << lk;
+                    const float2 sv = snr(k ? v4 : v, lk);
+                    if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
+                    if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
+                }
+            };
+            if (active) {
+#pragma unroll
+                for (int q = 0; q < PAIRS; ++q) {
+                    if (INTERIOR)
+                        best[q] = snr(b[q], 0);  // (best starts at -inf: max(-inf, x) = x)
+                    else
+                        score(q, b[q], 0, b[q], -1);
+                }
+            }
+            // Two widths per step: from B_u (u = 4^(s-1), in B0 for odd s, else B1)
+            //   B_2u[i] = B_u[i] + B_u[i + u]
+            //   B_4u[i] = B_2u[i] + B_2u[i + 2u],  B_2u[i + 2u] = B_u[i + 2u] + B_u[i + 3u]
+            // the same roundings, operands and order as one width per step, with three
+            // partner loads, one store and one barrier per two widths.
+#pragma unroll
+            for (int s = 1; 2 * s - 1 < NW; ++s) {
+                const int u = 1 << (2 * s - 2);
+                const bool two = 2 * s < NW;       // width 4u searched too
+                const bool more = 2 * s + 1 < NW;  // a further step reads B_4u
+                const float *cur = (s & 1) ? B0 : B1;
+                float *nxt = (s & 1) ? B1 : B0;
                 if (active) {
 #pragma unroll
                     for (int q = 0; q < PAIRS; ++q) {
                         const int i = 2 * tid + 2 * THREADS * q;
-                        // partner sums of positions i and i + 1
-                        const float2 pv = h == 1 ? make_float2(b[q].y, cur[i + 2])
-                                                 : *reinterpret_cast<const float2 *>(cur + i + h);
-                        b[q] = add_f2(b[q], pv);
-                        *reinterpret_cast<float2 *>(nxt + i) = b[q];
+                        float2 p1, p23 = make_float2(0.f, 0.f);
+                        if (u == 1) {
+                            const float2 c = *reinterpret_cast<const float2 *>(cur + i + 2);
+                            p1 = make_float2(b[q].y, c.x);
+                            if (two) p23 = add_f2(c, make_float2(c.y, cur[i + 4]));
+                        } else {
+                            p1 = *reinterpret_cast<const float2 *>(cur + i + u);
+                            if (two)
+                                p23 = add_f2(*reinterpret_cast<const float2 *>(cur + i + 2 * u),
+                                             *reinterpret_cast<const float2 *>(cur + i + 3 * u));
+                        }
+                        const float2 v2 = add_f2(b[q], p1);
+                        b[q] = two ? add_f2(v2, p23) : v2;
+                        score(q, v2, 2 * s - 1, b[q], two ? 2 * s : -1);
+                        if (more) *reinterpret_cast<float2 *>(nxt + i) = b[q];
                     }
                 }
-                bar.sync();
+                if (more) bar.sync();
             }
-            if (active) {
-                const float wm = __fmul_rn((float)w, mu_f);
-                const float inv = inv_w[l];
-#pragma unroll
-                for (int q = 0; q < PAIRS; ++q) {
-                    const int i = 2 * tid + 2 * THREADS * q;
-                    if (i >= NBEST) continue;  // i even and NBEST even: i + 1 < NBEST too
-                    const long long t = r0 + i;
-                    const float2 sv =
-                        mul_f2(add_f2(b[q], make_float2(-wm, -wm)), make_float2(inv, inv));
-                    if (interior) {
-                        best[q].x = fmaxf(best[q].x, sv.x);
-                        best[q].y = fmaxf(best[q].y, sv.y);
-                    } else {
-                        if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
-                        if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
-                    }
-                }
-            }
-        }
+        };
+        if (interior)
+            widths(std::true_type{});
+        else
+            widths(std::false_type{});
         bool any = false;
         if (active) {
 #pragma unroll

@@ -617,7 +617,7 @@ constexpr int kBoxThreads = 256;
 
 // One CTA per (DM, run of `tpc` consecutive tiles): the tile loop of box.cuh.
 template <typename T, int NW>
-__global__ void __launch_bounds__(kBoxThreads, 5)
+__global__ void __launch_bounds__(kBoxThreads, 4)
     k_boxcar(const T *__restrict__ y, long long n, int tpc, double threshold,
              const double2 *__restrict__ musig, DevCand *__restrict__ cands,
              unsigned long long *__restrict__ count, long long cap)

@@ -88,6 +88,12 @@ __device__ __forceinline__ void cp_async4(void *dst, const void *src, uint32_t s
                  "r"(src_bytes)
                  : "memory");
 }
+// 8 bytes, both addresses 8-byte aligned.
+__device__ __forceinline__ void cp_async8(void *dst, const void *src)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_addr(dst)), "l"(src)
+                 : "memory");
+}
 __device__ __forceinline__ void cp_async_commit()
 {
     asm volatile("cp.async.commit_group;" ::: "memory");

@@ -232,12 +232,13 @@ mdsm_status mdsm_ref_detect_device(const float *d_series, int ndms, int nsamp, f
  * device memory once at start-up, or a plugin where allocation is not permitted.  This entry
  * point has no counterpart in the reference.  It calls no cudaMalloc/cudaFree and no allocating
  * library routine: its work arrays live in one fixed device array of about 2 MiB that every GPU
- * loading the library holds until exit.  Limits: ndms*nsamp <= 2^31 values (at most 65536
- * statistics chunks) and cap <= 65536 candidates; larger requests return MDSM_ERANGE.  The
- * first call on a device looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All calls share the array
- * and leave its contents behind (the candidate counter is cleared at each call), so calls that
- * overlap on the GPU race.  Results equal mdsm_ref_detect_device's. */
+ * loading the library holds until exit.  Limits: ndms*nsamp < 2^31 values (MDSM_EINVAL
+ * beyond, as mdsm_ref_detect_device) and cap <= 65536 candidates (MDSM_ERANGE beyond).  Each
+ * call looks up the array's address in the current context (cudaGetSymbolAddress), so a
+ * context torn down and created again (cudaDeviceReset) is handled; like the allocating
+ * detector it synchronises the stream, so it cannot be captured in a CUDA graph.  All calls
+ * share the array and leave its contents behind (the candidate counter is cleared at each
+ * call), so calls that overlap on the GPU race.  Results equal mdsm_ref_detect_device's. */
 mdsm_status mdsm_ref_detect_device_noalloc(const float *d_series, int ndms, int nsamp,
                                            float lowdm, float dmstep, float threshold,
                                            mdsm_candidate *h_cands, long long cap,

@@ -41,6 +41,9 @@ struct FusedRun {
     size_t mom_bytes = 0;
     DevCand *d_cands = nullptr;        // [beam][cap]
     unsigned long long *d_counts = nullptr;
+    std::vector<size_t> mom_off;       // per beam, its rows' moments in d_mom
+    std::vector<int> rest;             // beams whose staging does not fit this shape: their own
+                                       // clip, dedispersion and search launches after the fused one
 };
 
 struct mdsm_batch_s {
@@ -113,8 +116,8 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
     z.clip = clip;
     z.detect = detect;
     const size_t nb = b->plans.size();
-    const FusedShapeInfo si = fused_shape_info(shape);
     z.geoms.resize(nb);
+    std::vector<char> fused(nb, 0);
     for (size_t i = 0; i < nb; ++i) {
         const Plan &p = b->plans[i]->p;
         StageGeom g = p.stages[0];  // geometry; the tables are rebuilt for this shape
@@ -123,20 +126,27 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
         g.d_rel = nullptr;
         g.d_sminspan = nullptr;
         z.geoms[i] = g;
-        MDSM_TRY(fused_tables(shape, z.geoms[i], p.S));
-        // the caller's buffer holds what the plan's own tile shape reads (mdsm_plan_info
-        // in_bytes); a shape whose last tile reads further is not used for this batch
-        if (stage_in_bytes(z.geoms[i], b->in_stride[i], 0) >
-            stage_in_bytes(p.stages[0], b->in_stride[i], 0))
-            return fail(MDSM_EINVAL, "fused batch: this tile shape reads past beam " +
-                                         std::to_string(i) + "'s input");
+        // A beam whose staging does not fit this shape (or whose last tile would read past the
+        // caller's buffer, which holds what the plan's own tile shape reads: mdsm_plan_info
+        // in_bytes) runs on its own launches instead.
+        if (fused_tables(shape, z.geoms[i], p.S) != MDSM_OK ||
+            stage_in_bytes(z.geoms[i], b->in_stride[i], 0) >
+                stage_in_bytes(p.stages[0], b->in_stride[i], 0)) {
+            free_stage(z.geoms[i]);
+            z.rest.push_back((int)i);
+            continue;
+        }
+        fused[i] = 1;
         z.rawcap = std::max(z.rawcap, z.geoms[i].rowcap);
         z.ps = std::max(z.ps, z.geoms[i].ps);
     }
+    if (z.rest.size() == nb)
+        return fail(MDSM_EINVAL, "fused batch: no beam's staging fits this tile shape");
     // (each beam keeps its own phase stride and offsets: the launch expands a beam's chunks
     // with its stride; the shared-memory buffers are sized for the widest)
     // moments and candidates
-    std::vector<size_t> mom_off(nb);
+    std::vector<size_t> &mom_off = z.mom_off;
+    mom_off.assign(nb, 0);
     for (size_t i = 0; i < nb; ++i) {
         mom_off[i] = z.mom_bytes / sizeof(unsigned long long);
         z.mom_bytes += (size_t)b->plans[i]->p.ndms * 3 * sizeof(unsigned long long);
@@ -158,11 +168,12 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
     std::vector<int2> cc, cs;
     const int kFusedBoxTile = 2048, tpc = 16;  // search items: runs of up to 16 tiles
     for (int i : beams) {
+        if (!fused[i]) continue;
         const Plan &p = b->plans[i]->p;
         const StageGeom &g = z.geoms[i];
         unsigned char *in = static_cast<unsigned char *>(const_cast<void *>(b->in[i]));
         int32_t *out = static_cast<int32_t *>(b->out[i]);
-        unsigned long long *mom = z.d_mom + mom_off[i];
+        unsigned long long *mom = detect ? z.d_mom + mom_off[i] : nullptr;  // (for the search)
         ka[i] = fused_kargs(g, g.d_rel, in, b->in_stride[i], out, b->out_stride[i], z.rawcap,
                             g.ps, mom, b->d_err);
         const long long ncols = (long long)p.nsamp + p.maxshift;
@@ -184,7 +195,7 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
         B.nsamp = p.nsamp;
         B.nspec_items =
             clip ? (unsigned)((ncols + kFusedSpecColsHost - 1) / kFusedSpecColsHost) : 0u;
-        B.ndd_done = (unsigned)((dd.size() - dd0) * (size_t)si.compute_warps);
+        B.ndd_done = (unsigned)(dd.size() - dd0);  // one count per dedispersion item
         B.out = out;
         B.out_stride = b->out_stride[i];
         B.mom = mom;
@@ -229,7 +240,9 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
     return MDSM_OK;
 }
 
-// One fused pass: counters and moments zeroed, the launch, the candidates' copies.
+// One fused pass: counters and moments zeroed, the launch, the candidates' copies; then each
+// beam left out of the fused launch on its own launches (clip, its plan's dedispersion with
+// the moments folded, search).
 mdsm_status fused_pass(mdsm_batch *b, cudaStream_t st)
 {
     FusedRun &z = b->fz;
@@ -240,8 +253,33 @@ mdsm_status fused_pass(mdsm_batch *b, cudaStream_t st)
     MDSM_TRY(fused_launch(z.shape, z.f, static_cast<const KArgs *>(z.d_kargs),
                           static_cast<const int4 *>(z.d_dd), z.n_dd, z.rawcap, z.ps, st));
     b->launches = 1;
+    std::vector<char> is_rest(b->plans.size(), 0);
+    for (int i : z.rest) {
+        is_rest[(size_t)i] = 1;
+        const Plan &p = b->plans[(size_t)i]->p;
+        const StageGeom &g = p.stages[0];
+        if (z.clip) {
+            MDSM_TRY(rfi_clip(const_cast<void *>(b->in[(size_t)i]), p.in_dtype, p.nchans,
+                              b->in_stride[(size_t)i], (long long)p.nsamp + p.maxshift, b->k_chan,
+                              b->k_spec, st));
+            b->launches += (b->k_chan > 0) + (b->k_spec > 0);
+        }
+        unsigned long long *mom =
+            z.detect && stage_folds_moments(g) ? z.d_mom + z.mom_off[(size_t)i] : nullptr;
+        MDSM_TRY(launch_stage(g, b->in[(size_t)i], b->in_stride[(size_t)i], 0, b->out[(size_t)i],
+                              b->out_stride[(size_t)i], 0, b->d_err, st, &b->launches, -1, mom,
+                              p.ndms));
+        if (z.detect) {
+            MDSM_TRY(boxcar_launch(b->out[(size_t)i], p.out_dtype, p.ndms, p.nsamp, b->nwidths,
+                                   b->threshold, b->d_det[(size_t)i],
+                                   boxcar_work_bytes(p.ndms, p.nsamp, b->cap), b->cap,
+                                   b->h_cands[(size_t)i], b->h_count[(size_t)i], st, mom));
+            b->launches += p.out_dtype == MDSM_OUT_F32 ? 3 : 2;  // statistics (2 or 1), search
+        }
+    }
     if (z.detect)
         for (size_t i = 0; i < b->plans.size(); ++i) {
+            if (is_rest[i]) continue;
             static_assert(sizeof(DevCand) == sizeof(mdsm_candidate), "record sizes differ");
             MDSM_CUDA_TRY(cudaMemcpyAsync(b->h_count[i], z.d_counts + i, sizeof(long long),
                                           cudaMemcpyDeviceToHost, st));

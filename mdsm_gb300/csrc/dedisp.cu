@@ -262,7 +262,7 @@ using CfgI16T = PackedCfg<2, 16, 1, false, PT, true>;
 // (item, chunk index, channels, flags) beside it; the compute warps take the chunks in order,
 // start an item's sums on its first chunk and store them after its last.  So short items
 // (few channels, as in the subband stages) keep the copies in flight between items.
-constexpr int kChunkFirst = 1, kChunkLast = 2, kChunkStop = 4;
+constexpr int kChunkFirst = 1, kChunkLast = 2, kChunkStop = 4;  // chunk flags (bits 0-2)
 
 // CTA barrier 0 returning whether any thread passed true.  The producer and the compute warps
 // reach it from their own loops, once per chunk each (a barrier counts warps, so the program
@@ -298,7 +298,7 @@ struct OnePlanItems {
         return make_int4(0, blk, rest % ntiles, rest / ntiles);
     }
     __device__ const KArgs &args(int) const { return *a; }
-    __device__ void stored(int) const {}
+    __device__ void item_done(int) const {}
     static constexpr bool kBeamStride = false;  // every chunk has the kernel's phase stride
 };
 
@@ -315,8 +315,8 @@ struct ListItems {
     }
     __device__ int4 item(int it) const { return items[it]; }
     __device__ const KArgs &args(int beam) const { return beams[beam]; }
-    __device__ void stored(int) const {}
-    static constexpr bool kBeamStride = false;
+    __device__ void item_done(int) const {}
+    static constexpr bool kBeamStride = true;  // each beam's chunks with its own phase stride
 };
 
 // The odd samples of a word as 32-bit lanes: uint8, (s1, s3) as uint16 lanes; uint16, s1.
@@ -354,6 +354,14 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         int p_it = -1, p_k = 0, p_nchunks = 0;
         int4 p_w = make_int4(0, 0, 0, 0);
         int2 p_ss = make_int2(0, 0);
+        // the item's beam fields the fills use, in registers (the barrier and copy asm clobber
+        // memory, which would otherwise reload them from the argument list at every fill)
+        struct {
+            const unsigned char *in;
+            long long in_stride, in_group_stride;
+            const int32_t *rel, *sminspan;
+            int nchans, nblk;
+        } a{};
         auto p_next_item = [&]() {
             int it = 0;
             if (lane == 0) it = src.grab();
@@ -361,12 +369,19 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             p_k = 0;
             if (p_it >= 0) {
                 p_w = src.item(p_it);
-                p_nchunks = (src.args(p_w.x).nchans + kPCC - 1) / kPCC;
+                const KArgs &b = src.args(p_w.x);
+                a.in = b.in;
+                a.in_stride = b.in_stride;
+                a.in_group_stride = b.in_group_stride;
+                a.rel = b.rel;
+                a.sminspan = b.sminspan;
+                a.nchans = b.nchans;
+                a.nblk = b.nblk;
+                p_nchunks = (a.nchans + kPCC - 1) / kPCC;
             }
         };
         auto p_load_ss = [&]() {
             if (p_it < 0) return;
-            const KArgs &a = src.args(p_w.x);
             const int c = p_k * kPCC + lane;
             if (c < a.nchans) {
                 const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
@@ -383,7 +398,6 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 __syncwarp();
                 return;
             }
-            const KArgs &a = src.args(p_w.x);
             const long long t0 = (long long)p_w.z * Cfg::PT;
             const size_t bofs = (size_t)(p_w.w * a.nblk + p_w.y) * a.nchans;
             const int c0 = p_k * kPCC;
@@ -406,7 +420,8 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             if (lane == 0) {
                 meta[s] = make_int4(p_it, p_k, nc,
                                     (p_k == 0 ? kChunkFirst : 0) |
-                                        (p_k == p_nchunks - 1 ? kChunkLast : 0));
+                                        (p_k == p_nchunks - 1 ? kChunkLast : 0) |
+                                        (p_w.x << 8));  // the item's beam above the flags
                 mbar_arrive_expect_tx(&bars[s], total);  // releases the meta entry with the phase
             }
             __syncwarp();
@@ -448,6 +463,9 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
 
     unsigned gk = 0;  // chunk sequence number
     bool aborted = false;
+    int sb_beam = -1, sb_nw = 0;  // the last chunk's beam, its phase stride and quad reciprocal
+    unsigned sb_inv = 0;
+    int done_beam = -1;  // beam of an item whose stores are not yet published
     for (;; ++gk) {
         const int s = (int)(gk % kPNR);
         const int pb = (int)(gk & 1u);  // phase buffer of this chunk
@@ -466,9 +484,15 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             if constexpr (Src::kBeamStride) {
                 const int4 mm = meta[s];
                 if (mm.x >= 0) {
-                    nwc = src.args(src.item(mm.x).x).ps >> 2;
+                    const int beam = mm.w >> 8;
+                    if (beam != sb_beam) {  // (consecutive chunks mostly share a beam)
+                        sb_beam = beam;
+                        sb_nw = src.args(beam).ps >> 2;
+                        sb_inv = ((1u << 20) + (unsigned)(sb_nw >> 2) - 1) / (unsigned)(sb_nw >> 2);
+                    }
+                    nwc = sb_nw;
                     nqc = nwc >> 2;
-                    nqc_inv = ((1u << 20) + (unsigned)nqc - 1) / (unsigned)nqc;
+                    nqc_inv = sb_inv;
                 }
             }
             for (int q = tid; q < kPCC * nqc; q += NW * 32) {
@@ -510,6 +534,12 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
         if (cta_any(!ok)) {
             aborted = true;
             break;
+        }
+        // The previous item's rows were all stored before this barrier: one thread publishes
+        // that (its fence is cumulative over the CTA's writes ordered by the barrier).
+        if (done_beam >= 0) {
+            if (tid == 0) src.item_done(done_beam);
+            done_beam = -1;
         }
         if (m.w & kChunkStop) break;
         const int nc = m.z;
@@ -694,7 +724,7 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 }
             }
         }
-        src.stored(w.x);  // this warp's rows of the item are written
+        done_beam = w.x;  // published after the next chunk's barrier
     }
     if (aborted) {
         // let the copies already issued land before the CTA exits (bounded as well)
@@ -742,12 +772,13 @@ __global__ void __launch_bounds__(CfgU8::THREADS, 1)
 // fused batched launch: RFI clip, dedispersion and boxcar search of several uint8 beams in one
 // persistent launch
 // ------------------------------------------------------------------------------------------
-// Four phases over four work lists, each item taken from its own global counter by a whole
-// CTA: (1) clip one channel of one beam; (2) clip one run of columns (spectra) of one beam;
-// (3) dedisperse one (beam, DM block, time tile) through the packed stream, storing int32
-// series and folding each row's exact moments; (4) boxcar-search one run of tiles of one row.
-// Each item first waits (bounded) for its beam's items of the phase before: a count in
-// `done` that the items raise after a fence once their results are written.  A CTA leaves a
+// Four phases over four work lists, each item taken from its own global counter: (1) clip one
+// channel of one beam; (2) clip one run of columns (spectra) of one beam; (3) dedisperse one
+// (beam, DM block, time tile) through the packed stream, storing int32 series and folding
+// each row's exact moments when a search follows; (4) boxcar-search one run of tiles of one
+// row, in one of several independent thread groups of the CTA.  Each item first waits
+// (bounded) for its beam's items of the phase before: a count in `done` that one thread
+// raises, after a CTA barrier and a fence, once the item's results are written.  A CTA leaves a
 // phase only when that phase's list is exhausted, so every item an item waits for has already
 // been taken by a running CTA, which depends only on earlier phases: the waits always end.
 constexpr int kFusedSpecCols = kFusedSpecColsHost;  // columns of one phase-2 item (a thread each)
@@ -823,8 +854,8 @@ __device__ __forceinline__ void mean_sigma_ll(long long s1, long long s2, long l
     *sig = var > 0.0 ? __dsqrt_rn(var) : 0.0;
 }
 
-// Phase 3's item source: the dedispersion list, each item waiting for its beam's clip, each
-// compute warp counting its stores.
+// Phase 3's item source: the dedispersion list, each item waiting for its beam's clip (when
+// there is one), each compute warp counting its stores (when a search follows).
 struct FusedItems {
     const KArgs *beams;
     const int4 *items;
@@ -833,21 +864,23 @@ struct FusedItems {
     const FusedBeam *fb;
     unsigned *done;
     unsigned *err;
+    bool count;  // phase 4 waits on the stores
     __device__ int grab()
     {
         const int it = (int)atomicAdd(counter, 1u);
         if (it >= nitems) return -1;
         const int b = items[it].x;
-        wait_count(&done[3 * b + 1], fb[b].nspec_items, err);  // (a timeout is recorded)
+        const unsigned target = fb[b].nspec_items;
+        if (target) wait_count(&done[3 * b + 1], target, err);  // (a timeout is recorded)
         return it;
     }
     __device__ int4 item(int it) const { return items[it]; }
     __device__ const KArgs &args(int beam) const { return beams[beam]; }
-    __device__ void stored(int beam) const
+    __device__ void item_done(int beam) const
     {
+        if (!count) return;
         __threadfence();
-        __syncwarp();
-        if ((threadIdx.x & 31) == 0) atomicAdd(&done[3 * beam + 2], 1u);
+        atomicAdd(&done[3 * beam + 2], 1u);
     }
     // each beam's chunks are expanded with the beam's own phase stride (KArgs::ps, at most
     // the kernel's), so a narrow beam does not expand the widest beam's row length
@@ -945,7 +978,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1)
     __syncthreads();
     packed_init_barriers(smem);
     {
-        FusedItems src{beams, dd_items, n_dd, &f.counters[2], f.fb, f.done, f.err};
+        FusedItems src{beams, dd_items, n_dd, &f.counters[2], f.fb, f.done, f.err, f.n_bx > 0};
         packed_stream<Cfg>(src, smem, rawcap, ps, f.err);
     }
     __syncthreads();
@@ -1474,20 +1507,8 @@ mdsm_status batch_prepare(BatchState &b, const std::vector<BatchBeam> &beams)
     b.smem = rawcap ? packed_smem<CfgU8>(rawcap, ps) : 0;
     if (b.smem > packed_smem_limit())
         return fail(MDSM_EINVAL, "batch: common staging does not fit");
-    // per packed beam: offsets re-expressed with the common phase stride
-    b.d_rel.assign(beams.size(), nullptr);
-    for (size_t i = 0; i < beams.size(); ++i) {
-        const StageGeom &g = *beams[i].g;
-        if (!in_batch_kernel(g)) continue;
-        std::vector<int32_t> rel(g.rel.size());
-        for (size_t j = 0; j < rel.size(); ++j) {
-            const int a = g.rel[j] / g.ps, q4 = g.rel[j] % g.ps;
-            rel[j] = a * ps + q4;
-        }
-        MDSM_CUDA_TRY(cudaMalloc(&b.d_rel[i], rel.size() * sizeof(int32_t)));
-        MDSM_CUDA_TRY(cudaMemcpy(b.d_rel[i], rel.data(), rel.size() * sizeof(int32_t),
-                                 cudaMemcpyHostToDevice));
-    }
+    // (each packed beam keeps its plan's offsets and phase stride: the launch expands a beam's
+    // chunks with its own stride; the shared-memory buffers are sized for the widest)
     MDSM_CUDA_TRY(cudaMalloc(&b.d_counter, sizeof(unsigned)));
     MDSM_CUDA_TRY(cudaMalloc(&b.d_kargs, std::max<size_t>(1, beams.size()) * sizeof(KArgs)));
     return MDSM_OK;
@@ -1527,7 +1548,7 @@ mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in
         a.out = static_cast<unsigned char *>(out[i]);
         a.out_stride = out_stride[i];
         a.out_group_stride = 0;
-        a.rel = in_batch_kernel(g) ? static_cast<const int32_t *>(b.d_rel[i]) : g.d_rel;
+        a.rel = g.d_rel;
         a.sminspan = g.d_sminspan;
         a.nchans = g.nchans;
         a.ndms = g.ndms;
@@ -1536,8 +1557,8 @@ mdsm_status batch_set_buffers(BatchState &b, const std::vector<const void *> &in
         a.rowcap = in_batch_kernel(g) ? b.rawcap : g.rowcap;
         a.nst = g.nst;
         a.out_i32 = g.out_i32;
-        a.ps = in_batch_kernel(g) ? b.ps : g.ps;
-            a.err = d_err;
+        a.ps = g.ps;
+        a.err = d_err;
     }
     for (int i : order) {
         const StageGeom &g = *b.beams[i].g;
@@ -1595,9 +1616,6 @@ mdsm_status batch_launch(BatchState &b, int mode, cudaStream_t st, int *launches
 
 void batch_release(BatchState &b)
 {
-    for (void *p : b.d_rel)
-        if (p) cudaFree(p);
-    b.d_rel.clear();
     if (b.d_items) cudaFree(b.d_items);
     if (b.d_counter) cudaFree(b.d_counter);
     if (b.d_kargs) cudaFree(b.d_kargs);

@@ -142,6 +142,8 @@ static void sort_cands(mdsm_candidate *c, long long n)
     });
 }
 
+// The candidate count and up to cap records from the device (on stream st, synchronised), in
+// mdsm_candidate order, sorted by (dm, sample).  The staging vector is host memory only.
 static mdsm_status fetch_cands(DevCand *d_c, unsigned long long *d_count, long long cap,
                                mdsm_candidate *h, long long *ncand, cudaStream_t st)
 {
@@ -152,8 +154,9 @@ static mdsm_status fetch_cands(DevCand *d_c, unsigned long long *d_count, long l
     const long long got = std::min<long long>((long long)n, cap);
     if (got > 0 && h) {
         std::vector<DevCand> tmp((size_t)got);
-        MDSM_CUDA_TRY(cudaMemcpy(tmp.data(), d_c, (size_t)got * sizeof(DevCand),
-                                 cudaMemcpyDeviceToHost));
+        MDSM_CUDA_TRY(cudaMemcpyAsync(tmp.data(), d_c, (size_t)got * sizeof(DevCand),
+                                      cudaMemcpyDeviceToHost, st));
+        MDSM_CUDA_TRY(cudaStreamSynchronize(st));
         for (long long i = 0; i < got; ++i) {
             h[i].dm_idx = tmp[i].dm_idx;
             h[i].sample = tmp[i].sample;
@@ -376,13 +379,16 @@ mdsm_status ref_detect_subband(const Plan &p, const float *d_series, long long o
 // the library's allocated scratch buffer.  The array is defined at file scope, so every GPU
 // that loads the library holds it (kNoAllocBytes, about 2 MiB) until the process exits.
 //
-// Limits: at most kNoAllocChunks 32K-value chunks (ndms*nsamp <= 2^31 values) and at most
-// kNoAllocCands stored candidates (cap); larger requests are rejected with MDSM_ERANGE.
+// Limits: ndms*nsamp < 2^31 values (as the allocating detector: MDSM_EINVAL beyond) and at
+// most kNoAllocCands stored candidates (cap; MDSM_ERANGE beyond).
 // Every call uses the same array and leaves its contents behind; the candidate counter is
 // cleared at the start of each call.  Calls whose work overlaps on the GPU (different streams
 // or threads without ordering between them) race on the array.
 // ---------------------------------------------------------------------------------------------
 constexpr unsigned kNoAllocChunks = 65536u;
+// the value count is below 2^31, so 32768-value chunks number at most 2^31 / 2^15
+static_assert((unsigned long long)kNoAllocChunks * 32768ull >= 0xFFFFFFFFull / 2 + 1,
+              "the fixed array holds the statistics of every block the detector accepts");
 constexpr long long kNoAllocCands = 65536;
 constexpr size_t kNoAllocHeader = 256;  // counter at 0, statistics at 16
 constexpr size_t kNoAllocBytes =
@@ -390,28 +396,16 @@ constexpr size_t kNoAllocBytes =
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-namespace {
-std::mutex g_noalloc_mu;
-constexpr int kMaxDevices = 64;
-void *g_noalloc_ptr[kMaxDevices];
-}  // namespace
-
-// The device address of g_noalloc_scratch on the current device.  Host code may not use the
-// symbol's name as a pointer (on the host it names a stand-in, not device memory), so the
-// address is looked up once per device, with that device current, and cached.
+// The device address of g_noalloc_scratch in the current context.  Host code may not use the
+// symbol's name as a pointer (on the host it names a stand-in, not device memory).  The address
+// is looked up on every call (a cheap query): a cached one would go stale when the context is
+// torn down and created again (cudaDeviceReset).
 static mdsm_status noalloc_scratch(char **out)
 {
-    int dev = 0;
-    MDSM_CUDA_TRY(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) return fail(MDSM_EINVAL, "device index out of range");
-    std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_ptr[dev]) {
-        void *ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
-        if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
-        g_noalloc_ptr[dev] = ptr;
-    }
-    *out = static_cast<char *>(g_noalloc_ptr[dev]);
+    void *ptr = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+    *out = static_cast<char *>(ptr);
     return MDSM_OK;
 }
 
@@ -422,15 +416,11 @@ mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float
 {
     const unsigned long long vals64 = (unsigned long long)ndms * (unsigned long long)nsamp;
     if (vals64 > 0xFFFFFFFFull / 2)
-        return fail(MDSM_ERANGE, "reference detector counts values in 32 bits");
+        return fail(MDSM_EINVAL, "reference detector counts values in 32 bits");
     const unsigned vals = (unsigned)vals64;
     const unsigned mod = vals < 32768u ? vals : 32768u;
     unsigned nchunks = 1;
-    while ((unsigned long long)(nchunks + 1) * mod < vals) ++nchunks;
-    if (nchunks > kNoAllocChunks)
-        return fail(MDSM_ERANGE, "no-allocation detector: block needs " + std::to_string(nchunks) +
-                                     " statistics chunks, the fixed array holds " +
-                                     std::to_string(kNoAllocChunks));
+    while ((unsigned long long)(nchunks + 1) * mod < vals) ++nchunks;  // <= kNoAllocChunks
     if (cap < 0) cap = 0;
     if (cap > kNoAllocCands)
         return fail(MDSM_ERANGE, "no-allocation detector: cap " + std::to_string(cap) +
@@ -451,29 +441,8 @@ mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float
                                        d_c, d_count, cap);
     MDSM_CUDA_TRY(cudaGetLastError());
     float hs[2];
-    unsigned long long n = 0;
     MDSM_CUDA_TRY(cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
-    MDSM_CUDA_TRY(cudaMemcpyAsync(&n, d_count, sizeof(n), cudaMemcpyDeviceToHost, st));
-    MDSM_CUDA_TRY(cudaStreamSynchronize(st));
-    const long long got = std::min<long long>((long long)n, cap);
-    if (got > 0 && h_cands) {
-        // the device records (dm, sample, width, snr) land in the caller's array as they are,
-        // then are put in mdsm_candidate order in place
-        static_assert(sizeof(DevCand) == sizeof(mdsm_candidate), "record sizes differ");
-        MDSM_CUDA_TRY(cudaMemcpyAsync(h_cands, d_c, (size_t)got * sizeof(DevCand),
-                                      cudaMemcpyDeviceToHost, st));
-        MDSM_CUDA_TRY(cudaStreamSynchronize(st));
-        for (long long i = 0; i < got; ++i) {
-            DevCand dc;
-            std::memcpy(&dc, &h_cands[i], sizeof dc);
-            h_cands[i].dm_idx = dc.dm_idx;
-            h_cands[i].sample = dc.sample;
-            h_cands[i].snr = dc.snr;
-            h_cands[i].width = dc.width;
-        }
-        sort_cands(h_cands, got);
-    }
-    *ncand = (long long)n;
+    MDSM_TRY(fetch_cands(d_c, d_count, cap, h_cands, ncand, st));  // (synchronises st)
     if (mean) *mean = hs[0];
     if (rms) *rms = hs[1];
     return MDSM_OK;

@@ -132,7 +132,6 @@ struct BatchBeam {
 
 struct BatchState {
     std::vector<BatchBeam> beams;
-    std::vector<void *> d_rel;  // per packed beam: offsets with the common phase stride
     void *d_items = nullptr;    // int4 (beam, DM block, tile, group)
     void *d_kargs = nullptr;    // per-beam kernel arguments
     unsigned *d_counter = nullptr;

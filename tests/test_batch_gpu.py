@@ -166,15 +166,9 @@ def test_fused_launch_every_shape_equals_oracle(lib, orc, cuda, graph):
                 t.zero_()
             b.run(graph=graph)
             torch.cuda.synchronize()
-        if not graph and b.last_launches != 1:
-            # this tile shape does not fit some beam: the batch fell back to the unfused pass
-            # for good, so a new batch goes on with the next shape
-            b.close()
-            b = Batch(plans)
-            b.set_buffers(d_in, d_out)
-            b.enable_clip(4.0, 4.0)
-            b.enable_detect(nwidths=9, threshold=6.0, cap=8192)
-            continue
+        if not graph:
+            # one fused launch, plus the own launches of any beam this shape cannot stage
+            assert b.last_launches >= 1
             info_k = p.info
             xc, y, (dm, samp, wid, snr) = want[k]
             nch, stride = p.input_shape()
@@ -187,7 +181,7 @@ def test_fused_launch_every_shape_equals_oracle(lib, orc, cuda, graph):
             assert np.array_equal(c["dm_idx"], dm) and np.array_equal(c["sample"], samp), (choice, k)
             assert np.array_equal(c["width"], wid) and np.array_equal(c["snr"], snr), (choice, k)
         ran += 1
-    assert ran >= 4
+    assert ran == 8
     b.close()
 
 
@@ -213,20 +207,40 @@ def test_fused_autotune_picks_the_fastest_candidate(lib, cuda):
     b.close()
 
 
-def test_unfusable_beams_fall_back_to_the_unfused_pass(lib, orc, cuda):
-    """A beam whose DM plan is too wide for the packed staging (BEAMS[3]) keeps the whole batch
-    on the unfused launches; the results still equal the oracle's."""
+def test_beam_outside_the_fused_staging_runs_beside_it(lib, orc, cuda):
+    """A beam whose DM plan is too wide for every fused tile shape (BEAMS[3], on the generic
+    kernel) runs on its own clip, dedispersion and search launches after the fused launch of
+    the others: every beam's series and candidates still equal the oracle's."""
+    from mdsm_gb300 import synth
     from mdsm_gb300.batch import Batch, choice_info
     torch = cuda
     plans, xs, d_in, d_out = _setup(torch, seed=40)
+    for k, p in enumerate(plans):
+        nch, stride = p.input_shape()
+        x = synth.gaussian_u8(nch, stride, 80 + k)
+        synth.inject(x, FCH1, -BW / nch, TSAMP, [(300 + 100 * k, 12.0, 2 + k, 45.0)],
+                     K=4148.741601)
+        xs[k] = x
+    _restore(torch, xs, d_in)
     b = Batch(plans)
     b.set_buffers(d_in, d_out)
-    b.enable_detect(nwidths=9, threshold=6.0, cap=1024)
+    b.enable_detect(nwidths=9, threshold=6.0, cap=4096)
     c = b.autotune()
-    assert choice_info(c)["fused"] == 0
-    b.run(graph=False)
-    torch.cuda.synchronize()
-    for k, (p, x) in enumerate(zip(plans, xs)):
-        want = orc.dedisperse(x, p.shift_table(), p.info.nsamp)
-        assert np.array_equal(d_out[k].cpu().numpy(), want), k
+    assert any(choice_info(ch)["fused"] == 1 for ch, _ in b.tune_times())
+    for choice in (c, 10):
+        _set_choice(b, choice)
+        _restore(torch, xs, d_in)
+        b.run(graph=False)
+        torch.cuda.synchronize()
+        if choice_info(choice)["fused"]:
+            # the fused launch, then BEAMS[3]'s dedispersion, statistics and search
+            assert b.last_launches > 1, b.last_launches
+        for k, (p, x) in enumerate(zip(plans, xs)):
+            y = orc.dedisperse(x, p.shift_table(), p.info.nsamp)
+            assert np.array_equal(d_out[k].cpu().numpy(), y), (choice, k)
+            dm, samp, wid, snr = orc.boxcar_detect(y, 9, 6.0)
+            got = b.candidates(k)
+            assert len(dm) > 0
+            assert np.array_equal(got["dm_idx"], dm) and np.array_equal(got["sample"], samp), k
+            assert np.array_equal(got["width"], wid) and np.array_equal(got["snr"], snr), k
     b.close()

@@ -166,7 +166,7 @@ mdsm_status fused_build(mdsm_batch *b, int shape, int order, bool clip, bool det
     std::vector<FusedBeam> fb(nb);
     std::vector<int4> dd, bx;
     std::vector<int2> cc, cs;
-    const int kFusedBoxTile = 2048, tpc = 16;  // search items: runs of up to 16 tiles
+    const int kFusedBoxTile = fused_box_tile(), tpc = 16;  // search items: runs of 16 tiles
     for (int i : beams) {
         if (!fused[i]) continue;
         const Plan &p = b->plans[i]->p;

@@ -27,8 +27,6 @@
 
 namespace mdsm {
 
-constexpr int kBoxTile = 2048;   // output samples per tile
-
 // Two FP32 lanes at once (Blackwell add/mul.f32x2, each lane rounded to nearest as the scalar
 // operation would be).  The operands are formed as register pairs (mov.b64 of two .f32), so
 // packing costs no integer instructions.
@@ -66,25 +64,37 @@ __device__ __forceinline__ float fmax3(float a, float b, float c)
     return r;
 }
 
-// Staged samples for NW widths: the region [t0 - HL, t0 + TILE + HL + wmax - 1), rounded up to
-// whole pairs of positions per thread; each sum buffer has wmax floats more so that partner
-// reads past the region stay inside it (those positions feed no kept boxcar).
-template <int NW, int THREADS>
+// Tile geometry of the search for NW widths (1 .. WMAX = 2^(NW-1)) by a group of THREADS
+// threads, each owning K positions of the staged region (K odd).  A tile's output samples are
+// [t0, t0 + TILE); the region holds the N = THREADS * K samples [t0 - HL, t0 + TILE + HL + WMAX)
+// that its kept boxcars and their neighbourhoods touch, so NBEST = TILE + 2 HL positions carry
+// a best SNR.
+template <int NW, int THREADS, int K>
 struct BoxGeom {
+    static_assert(NW >= 1 && NW <= 9, "widths 1 .. 256");
+    static_assert(K % 2 == 1, "odd positions per thread (no bank conflicts in the chains)");
+    static_assert((THREADS & (THREADS - 1)) == 0, "power-of-two thread count");
     static constexpr int WMAX = 1 << (NW - 1);
     static constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
-    static constexpr int SPAN = kBoxTile + 2 * HL + WMAX;  // samples a kept boxcar can touch
-    static constexpr int NBEST = kBoxTile + 2 * HL;        // positions with a best value
-    static constexpr int PAIRS = (SPAN + 2 * THREADS - 1) / (2 * THREADS);  // per thread
-    // floats; even, so the second buffer and the pairs in it stay 8-byte aligned
-    static constexpr int BUF = PAIRS * 2 * THREADS + (WMAX < 2 ? 2 : WMAX);
-    // shared memory of box_run: two sum buffers, the best SNR of NBEST positions, the next
-    // tile's samples, 1 / (sigma sqrt(w)) per width (16 floats)
-    static constexpr size_t SMEM =
-        (size_t)BUF * 8 + (size_t)NBEST * 4 + (size_t)PAIRS * 2 * THREADS * 4 + 64;
-    static_assert(NW <= 16, "widths");
-    static_assert(BUF % 2 == 0 && NBEST % 2 == 0, "pairs of positions");
-    static_assert((THREADS & (THREADS - 1)) == 0, "power-of-two thread count");
+    static constexpr int N = THREADS * K;
+    static constexpr int TILE = (N - 2 * HL - WMAX) & ~3;  // (a multiple of 4: aligned copies)
+    static constexpr int NBEST = TILE + 2 * HL;
+    static constexpr int STEPS = NW / 2;                          // two-width steps
+    static constexpr int UMAX = STEPS > 0 ? 1 << (2 * (STEPS - 1)) : 1;  // widest chain stride
+    static_assert(UMAX <= THREADS, "a chain stride per residue class");
+    static_assert(TILE >= THREADS, "tile");
+    // the exact path: position pairs (2 tid + 2 THREADS q, +1)
+    static constexpr int PAIRS = (N + 2 * THREADS - 1) / (2 * THREADS);
+    // floats of each sum buffer: the exact path's pairs plus WMAX of partner reads past them,
+    // and the chains' reads up to 3 UMAX past N; even (8-byte aligned pairs)
+    static constexpr int BUF0 = PAIRS * 2 * THREADS + (WMAX < 2 ? 2 : WMAX);
+    static constexpr int BUF1 = N + 3 * UMAX + 4;
+    static constexpr int BUF = ((BUF0 > BUF1 ? BUF0 : BUF1) + 3) / 4 * 4;
+    static constexpr int NBF = N + 4;  // staged samples, 3 zeros of chain reads past them
+    // shared memory of box_run: the staged samples, two sum buffers, the best SNR of NBEST
+    // positions (exact path), 1 / (sigma sqrt(w)) per width (16 floats)
+    static constexpr size_t SMEM = (size_t)NBF * 4 + (size_t)BUF * 8 + (size_t)NBEST * 4 + 64;
+    static_assert(NBEST % 2 == 0 && NBF % 4 == 0, "alignment");
 };
 
 // Best SNR over the widths 1, 2, ..., 2^(NW-1) at series position t (0 <= t < n) and the first
@@ -118,37 +128,6 @@ __device__ __noinline__ void box_best_at(const T *__restrict__ r, long long t, l
     }
     *bv = best;
     *bw = width;
-}
-
-// Asynchronous copy of one tile's samples into NB: this thread's pairs
-// (r0 + 2 tid + 2 THREADS q, +1), zero outside the series.  Only the issuing thread reads
-// them back, so its own wait is the only synchronisation.
-template <typename T, int PAIRS, int THREADS>
-__device__ __forceinline__ void box_prefetch(uint32_t *NB, const T *__restrict__ r, long long r0,
-                                             long long n, int tid)
-{
-    static_assert(sizeof(T) == 4, "4-byte samples");
-    const bool inside = r0 >= 0 && r0 + PAIRS * 2 * THREADS <= n;
-    if (inside && ((uintptr_t)(r + r0) & 7) == 0) {
-        // the whole region inside the series, pairs 8-byte aligned: one 8-byte copy a pair
-        const T *base = r + r0;
-#pragma unroll
-        for (int q = 0; q < PAIRS; ++q) {
-            const int i = 2 * tid + 2 * THREADS * q;
-            cp_async8(NB + i, base + i);
-        }
-    } else {
-#pragma unroll
-        for (int q = 0; q < PAIRS; ++q)
-#pragma unroll
-            for (int e = 0; e < 2; ++e) {
-                const int i = 2 * tid + 2 * THREADS * q + e;
-                const long long t = r0 + i;
-                const bool in = t >= 0 && t < n;
-                cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
-            }
-    }
-    cp_async_commit();
 }
 
 // The search group's barriers.  BoxBarCta: the group is the whole CTA (threads at or past
@@ -188,185 +167,294 @@ __device__ __forceinline__ float box_value(uint32_t raw)
         return (float)(int32_t)raw;
 }
 
+// One tile exactly (the width ladder with every position's best SNR and the range tests of an
+// edge tile, then the candidates): for tiles the fast path flags and for edge tiles.  The
+// samples are read from the series (zero outside it).  B0, B1: BUF floats each; best_s: NBEST.
+// Every thread of the group calls it.
+template <typename T, int NW, int THREADS, int K, class Bar>
+__device__ __noinline__ void box_tile_exact(const T *__restrict__ r, long long n, long long t0,
+                                            float mu_f, float thr, const float *inv_w, int d,
+                                            DevCand *__restrict__ cands,
+                                            unsigned long long *__restrict__ count, long long cap,
+                                            float *B0, float *B1, float *best_s, const Bar &bar,
+                                            int tid, bool active)
+{
+    using G = BoxGeom<NW, THREADS, K>;
+    constexpr int HL = G::HL, NBEST = G::NBEST, PAIRS = G::PAIRS;
+    const long long r0 = t0 - HL;  // series index of B[0] and best[0]
+    float2 b[PAIRS], best[PAIRS];
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < PAIRS; ++q) {
+            const int i = 2 * tid + 2 * THREADS * q;
+            float v[2];
+#pragma unroll
+            for (int e = 0; e < 2; ++e) {
+                const long long t = r0 + i + e;
+                v[e] = t >= 0 && t < n ? (float)__ldg(r + t) : 0.f;
+            }
+            b[q] = make_float2(v[0], v[1]);
+            *reinterpret_cast<float2 *>(B0 + i) = b[q];
+            best[q] = make_float2(-INFINITY, -INFINITY);
+        }
+    }
+    bar.sync();
+    // best SNR of pair q over width 2^l (sums v), where the boxcar lies in the series
+    auto score = [&](int q, float2 v, int l) {
+        const int i = 2 * tid + 2 * THREADS * q;
+        if (i >= NBEST) return;  // i even and NBEST even: i + 1 < NBEST too
+        const int w = 1 << l;
+        const float wm = __fmul_rn((float)w, mu_f);
+        const float2 sv = mul_f2(add_f2(v, make_float2(-wm, -wm)), make_float2(inv_w[l], inv_w[l]));
+        const long long t = r0 + i;
+        if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
+        if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
+    };
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < PAIRS; ++q) score(q, b[q], 0);
+    }
+    // two widths per step, as the fast path's chains: B_2u[i] = B_u[i] + B_u[i + u],
+    // B_4u[i] = B_2u[i] + (B_u[i + 2u] + B_u[i + 3u])
+#pragma unroll
+    for (int s = 1; 2 * s - 1 < NW; ++s) {
+        const int u = 1 << (2 * s - 2);
+        const bool two = 2 * s < NW;
+        const bool more = 2 * s + 1 < NW;
+        const float *cur = (s & 1) ? B0 : B1;
+        float *nxt = (s & 1) ? B1 : B0;
+        if (active) {
+#pragma unroll
+            for (int q = 0; q < PAIRS; ++q) {
+                const int i = 2 * tid + 2 * THREADS * q;
+                float2 p1, p23 = make_float2(0.f, 0.f);
+                if (u == 1) {
+                    const float2 c = *reinterpret_cast<const float2 *>(cur + i + 2);
+                    p1 = make_float2(b[q].y, c.x);
+                    if (two) p23 = add_f2(c, make_float2(c.y, cur[i + 4]));
+                } else {
+                    p1 = *reinterpret_cast<const float2 *>(cur + i + u);
+                    if (two)
+                        p23 = add_f2(*reinterpret_cast<const float2 *>(cur + i + 2 * u),
+                                     *reinterpret_cast<const float2 *>(cur + i + 3 * u));
+                }
+                const float2 v2 = add_f2(b[q], p1);
+                score(q, v2, 2 * s - 1);
+                b[q] = v2;
+                if (two) {
+                    b[q] = add_f2(v2, p23);
+                    score(q, b[q], 2 * s);
+                }
+                if (more) *reinterpret_cast<float2 *>(nxt + i) = b[q];
+            }
+        }
+        if (more) bar.sync();
+    }
+    bool any = false;
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < PAIRS; ++q)
+            if (2 * tid + 2 * THREADS * q < NBEST) any |= best[q].x >= thr || best[q].y >= thr;
+    }
+    if (!bar.any(any)) return;
+    if (active) {
+#pragma unroll
+        for (int q = 0; q < PAIRS; ++q) {
+            const int i = 2 * tid + 2 * THREADS * q;
+            if (i < NBEST) *reinterpret_cast<float2 *>(best_s + i) = best[q];
+        }
+    }
+    bar.sync();
+    if (active) {
+        for (int q = tid; q < G::TILE; q += THREADS) {
+            const long long t = t0 + q;
+            if (t >= n) break;
+            const int i = q + HL;
+            const float bv = best_s[i];
+            if (!(bv >= thr)) continue;
+            float snr;
+            int width;
+            box_best_at<T, NW>(r, t, n, mu_f, inv_w, &snr, &width);
+            const int h = max(width / 2, 1);
+            bool keep = true;
+            for (int u = 1; u <= h && keep; ++u)
+                if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
+            for (int u = 1; u <= h && keep; ++u)
+                if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
+            if (!keep) continue;
+            const unsigned long long at = atomicAdd(count, 1ull);
+            if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, width, snr};
+        }
+    }
+}
+
+// Asynchronous copy of tile `tile`'s region into NB by the group: 16-byte copies where the
+// region lies inside the series and starts 16-byte aligned, else 4-byte copies with zeros
+// outside the series.  Each thread waits for its own copies (cp_async_wait_all); a group
+// barrier then makes all of them visible.
+template <typename T, int NW, int THREADS, int K>
+__device__ __forceinline__ void box_stage(uint32_t *NB, const T *__restrict__ r, long long n,
+                                          long long tile, int tid)
+{
+    using G = BoxGeom<NW, THREADS, K>;
+    static_assert(sizeof(T) == 4, "4-byte samples");
+    const long long r0 = tile * G::TILE - G::HL;
+    if (r0 >= 0 && r0 + G::N <= n && ((uintptr_t)(r + r0) & 15) == 0) {
+        const T *base = r + r0;
+        for (int q = tid; q < G::N / 4; q += THREADS) cp_async16(NB + 4 * q, base + 4 * q);
+    } else {
+        for (int i = tid; i < G::N; i += THREADS) {
+            const long long t = r0 + i;
+            const bool in = t >= 0 && t < n;
+            cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
+        }
+    }
+    cp_async_commit();
+}
+
 // Tiles [tile_lo, tile_hi) of row r (n samples, DM index d) with the row's mean and sigma
 // (sigma > 0), searched by the calling group: `active` threads with group index tid in
 // [0, THREADS) (every thread of the group's barrier calls it); sm holds
-// BoxGeom<NW, THREADS>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr) go
-// to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight (the last tile
-// prefetches nothing); the caller synchronises the group before sm is written again.
-template <typename T, int NW, int THREADS, class Bar>
+// BoxGeom<NW, THREADS, K>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr)
+// go to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight; the caller
+// synchronises the group before sm is written again.
+//
+// Fast path (tiles inside the series): only whether any position < NBEST reaches the
+// threshold at any width is needed, so no position keeps a best SNR.  Step s (chain stride
+// u = 4^(s-1)) gives each thread the residue class r = tid mod u, block b = tid / u: the K
+// positions p_j = r + u (K b + j) and, from the previous step's buffer, B_u at p_j for
+// j < K + 3; it forms B_2u (K + 2 of them) and B_4u = B_2u[j] + B_2u[j + 2] (the same operands
+// and order as the exact path), keeps the maximum SNR of both widths, and stores B_4u at p_j
+// for the next step.  Reads and stores are conflict-free (K odd) and cost about half the
+// shared-memory traffic of the exact path's pairs.  A tile whose maximum reaches the
+// threshold (positions past NBEST may flag it too; they hold real or zero samples) is then
+// searched exactly.
+template <typename T, int NW, int THREADS, int K, class Bar>
 __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, long long tile_lo,
                                         long long tile_hi, double mu, double sig, double threshold,
                                         int d, DevCand *__restrict__ cands,
                                         unsigned long long *__restrict__ count, long long cap,
                                         unsigned char *sm, const Bar &bar, int tid_in, bool active)
 {
-    using G = BoxGeom<NW, THREADS>;
-    constexpr int HL = G::HL, NBEST = G::NBEST, PAIRS = G::PAIRS;
-    float *B0 = reinterpret_cast<float *>(sm), *B1 = B0 + G::BUF;
-    float *best_s = B1 + G::BUF;
-    uint32_t *NB = reinterpret_cast<uint32_t *>(best_s + NBEST);  // next tile's samples
-    float *inv_w = reinterpret_cast<float *>(NB + PAIRS * 2 * THREADS);
-    // (the mask tells the compiler tid < THREADS, so range tests fold at compile time for all
-    // but the last pair)
+    using G = BoxGeom<NW, THREADS, K>;
+    constexpr int N = G::N;
+    uint32_t *NB = reinterpret_cast<uint32_t *>(sm);  // staged samples of the current tile
+    float *A = reinterpret_cast<float *>(NB + G::NBF);
+    float *Bf = A + G::BUF;
+    float *best_s = Bf + G::BUF;
+    float *inv_w = best_s + G::NBEST;
     const int tid = tid_in & (THREADS - 1);
     const float mu_f = __double2float_rn(mu);
     const float thr = __double2float_rn(threshold);
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
     if (active && tid < NW)
         inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
-    // every staged sample and every boxcar of the tile inside the series: no per-element tests
-    auto inside = [&](long long tile) {
-        const long long r0 = tile * kBoxTile - HL;
-        return r0 >= 0 && r0 + PAIRS * 2 * THREADS <= n;
+    // zeros past the region: the chains read up to 3 positions past NB and 3 UMAX past N
+    auto zero_pads = [&]() {
+        if (!active) return;
+        for (int i = N + tid; i < G::BUF; i += THREADS) A[i] = Bf[i] = 0.f;
+        if (tid < G::NBF - N) NB[N + tid] = 0u;
     };
-    if (active) box_prefetch<T, PAIRS, THREADS>(NB, r, tile_lo * kBoxTile - HL, n, tid);
+    zero_pads();
+    auto inside = [&](long long tile) {
+        const long long r0 = tile * G::TILE - G::HL;
+        return r0 >= 0 && r0 + N <= n;
+    };
+    // SNR at width 2^l of sums v
+    auto snr = [&](float v, int l) {
+        const float wm = __fmul_rn((float)(1 << l), mu_f);
+        return __fmul_rn(__fadd_rn(v, -wm), inv_w[l]);
+    };
+    if (active && inside(tile_lo)) box_stage<T, NW, THREADS, K>(NB, r, n, tile_lo, tid);
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
-        const long long t0 = tile * kBoxTile;
-        const long long r0 = t0 - HL;  // series index of B[0] and best[0]
-        const bool interior = inside(tile);  // (uniform across the group)
-        float2 b[PAIRS], best[PAIRS];
-        if (active) {
-            cp_async_wait_all();
-#pragma unroll
-            for (int q = 0; q < PAIRS; ++q) {
-                const int i = 2 * tid + 2 * THREADS * q;
-                const uint2 raw = *reinterpret_cast<const uint2 *>(NB + i);
-                b[q] = make_float2(box_value<T>(raw.x), box_value<T>(raw.y));
-                *reinterpret_cast<float2 *>(B0 + i) = b[q];
-                best[q] = make_float2(-INFINITY, -INFINITY);
-            }
+        const long long t0 = tile * G::TILE;
+        if (!inside(tile)) {  // (uniform) edge tile: exactly, from the series
+            bar.sync();       // (inv_w and the pads written; the previous tile's reads done)
+            box_tile_exact<T, NW, THREADS, K>(r, n, t0, mu_f, thr, inv_w, d, cands, count, cap,
+                                              A, Bf, best_s, bar, tid, active);
+            bar.sync();
+            zero_pads();
+            if (active && tile + 1 < tile_hi && inside(tile + 1))
+                box_stage<T, NW, THREADS, K>(NB, r, n, tile + 1, tid);
+            continue;
         }
-        if (active && tile + 1 < tile_hi)  // in flight while this tile is searched
-            box_prefetch<T, PAIRS, THREADS>(NB, r, r0 + kBoxTile, n, tid);
-        bar.sync();  // B0 (and inv_w) written (each thread reads back only its own NB words)
-        // The widths of this tile, compiled twice: for tiles whose every staged sample and
-        // boxcar lies inside the series (no per-position range tests) and for the edges.
-        auto widths = [&](auto interior_tag) {
-            constexpr bool INTERIOR = decltype(interior_tag)::value;
-            // SNR of the pair's width-2^l sums v
-            auto snr = [&](float2 v, int l) {
-                const float wm = __fmul_rn((float)(1 << l), mu_f);
-                const float inv = inv_w[l];
-                return mul_f2(add_f2(v, make_float2(-wm, -wm)), make_float2(inv, inv));
-            };
-            // best SNR of pair q over widths 2^l (sums v) and, when l4 >= 0, 2^l4 (sums v4).
-            // Interior tiles need no range tests and keep values at positions past NBEST
-            // (never read); edge tiles take each width where its boxcar lies in the series.
-            auto score = [&](int q, float2 v, int l, float2 v4, int l4) {
-                const int i = 2 * tid + 2 * THREADS * q;
-                if (INTERIOR) {
-                    const float2 sv = snr(v, l);
-                    if (l4 >= 0) {
-                        const float2 s4 = snr(v4, l4);
-                        best[q].x = fmax3(best[q].x, sv.x, s4.x);
-                        best[q].y = fmax3(best[q].y, sv.y, s4.y);
-                    } else {
-                        best[q].x = fmaxf(best[q].x, sv.x);
-                        best[q].y = fmaxf(best[q].y, sv.y);
-                    }
-                    return;
-                }
-                if (i >= NBEST) return;  // i even and NBEST even: i + 1 < NBEST too
-                const long long t = r0 + i;
+        if (active) cp_async_wait_all();
+        bar.sync();  // the tile's samples (every thread's copies), inv_w and the pads visible
+        // The SNR (v - w mu) / (sigma sqrt w), rounded as the exact path rounds it, does not
+        // decrease with v: the largest SNR of a width is the SNR of its largest sum, so a thread
+        // keeps only the largest sum of each width and forms NW SNRs at the tile's end.
+        float M[NW];
 #pragma unroll
-                for (int k = 0; k < 2; ++k) {
-                    const int lk = k ? l4 : l;
-                    if (lk < 0) continue;
-                    const int w = 1 << lk;
-                    const float2 sv = snr(k ? v4 : v, lk);
-                    if (t >= 0 && t + w <= n) best[q].x = fmaxf(best[q].x, sv.x);
-                    if (t + 1 >= 0 && t + 1 + w <= n) best[q].y = fmaxf(best[q].y, sv.y);
-                }
-            };
-            if (active) {
-#pragma unroll
-                for (int q = 0; q < PAIRS; ++q) {
-                    if (INTERIOR)
-                        best[q] = snr(b[q], 0);  // (best starts at -inf: max(-inf, x) = x)
-                    else
-                        score(q, b[q], 0, b[q], -1);
-                }
-            }
-            // Two widths per step: from B_u (u = 4^(s-1), in B0 for odd s, else B1)
-            //   B_2u[i] = B_u[i] + B_u[i + u]
-            //   B_4u[i] = B_2u[i] + B_2u[i + 2u],  B_2u[i + 2u] = B_u[i + 2u] + B_u[i + 3u]
-            // the same roundings, operands and order as one width per step, with three
-            // partner loads, one store and one barrier per two widths.
-#pragma unroll
-            for (int s = 1; 2 * s - 1 < NW; ++s) {
-                const int u = 1 << (2 * s - 2);
-                const bool two = 2 * s < NW;       // width 4u searched too
-                const bool more = 2 * s + 1 < NW;  // a further step reads B_4u
-                const float *cur = (s & 1) ? B0 : B1;
-                float *nxt = (s & 1) ? B1 : B0;
-                if (active) {
-#pragma unroll
-                    for (int q = 0; q < PAIRS; ++q) {
-                        const int i = 2 * tid + 2 * THREADS * q;
-                        float2 p1, p23 = make_float2(0.f, 0.f);
-                        if (u == 1) {
-                            const float2 c = *reinterpret_cast<const float2 *>(cur + i + 2);
-                            p1 = make_float2(b[q].y, c.x);
-                            if (two) p23 = add_f2(c, make_float2(c.y, cur[i + 4]));
-                        } else {
-                            p1 = *reinterpret_cast<const float2 *>(cur + i + u);
-                            if (two)
-                                p23 = add_f2(*reinterpret_cast<const float2 *>(cur + i + 2 * u),
-                                             *reinterpret_cast<const float2 *>(cur + i + 3 * u));
-                        }
-                        const float2 v2 = add_f2(b[q], p1);
-                        b[q] = two ? add_f2(v2, p23) : v2;
-                        score(q, v2, 2 * s - 1, b[q], two ? 2 * s : -1);
-                        if (more) *reinterpret_cast<float2 *>(nxt + i) = b[q];
-                    }
-                }
-                if (more) bar.sync();
-            }
+        for (int l = 0; l < NW; ++l) M[l] = -INFINITY;
+        bool staged = false;  // the next tile's copies issued
+        auto stage_next = [&]() {
+            if (active && tile + 1 < tile_hi && inside(tile + 1))
+                box_stage<T, NW, THREADS, K>(NB, r, n, tile + 1, tid);
+            staged = true;
         };
-        if (interior)
-            widths(std::true_type{});
-        else
-            widths(std::false_type{});
-        bool any = false;
-        if (active) {
+        constexpr int S = G::STEPS > 0 ? G::STEPS : 1;  // (NW = 1: width 1 alone)
 #pragma unroll
-            for (int q = 0; q < PAIRS; ++q)
-                if (2 * tid + 2 * THREADS * q < NBEST) any |= best[q].x >= thr || best[q].y >= thr;
-        }
-        // most tiles hold no sample over the threshold: skip the neighbourhood test there
-        if (!bar.any(any)) continue;
-        if (active) {
+        for (int s = 1; s <= S; ++s) {
+            const int u = 1 << (2 * s - 2);
+            const bool two = 2 * s < NW;       // widths 2u and 4u (else 2u alone)
+            const bool more = 2 * s + 1 < NW;  // a further step reads B_4u
+            const int p0 = (tid & (u - 1)) + u * K * (tid / u);  // chain element 0
+            if (active) {
+                // B_u of chain element j (the staged samples for s = 1)
+                auto ld = [&](int j) {
+                    return s == 1 ? box_value<T>(NB[p0 + j]) : ((s & 1) ? Bf : A)[p0 + u * j];
+                };
+                float *nxt = (s & 1) ? A : Bf;
+                // a window over the chain: B_u at j .. j + 3 and B_2u at j .. j + 2; two chain
+                // elements per round (their maxima in one three-input max each)
+                float c0 = ld(0), c1 = ld(1), c2 = ld(2);
+                float w0 = __fadd_rn(c0, c1), w1 = __fadd_rn(c1, c2);
 #pragma unroll
-            for (int q = 0; q < PAIRS; ++q) {
-                const int i = 2 * tid + 2 * THREADS * q;
-                if (i < NBEST) *reinterpret_cast<float2 *>(best_s + i) = best[q];
+                for (int j = 0; j < K; j += 2) {
+                    const bool pair = j + 1 < K;
+                    const float c3 = ld(j + 3), c4 = pair ? ld(j + 4) : 0.f;
+                    const float w2 = __fadd_rn(c2, c3), w3 = pair ? __fadd_rn(c3, c4) : 0.f;
+                    if (s == 1) M[0] = pair ? fmax3(M[0], c0, c1) : fmaxf(M[0], c0);
+                    float o0 = w0, o1 = w1;
+                    if (NW > 1) {
+                        M[2 * s - 1] = pair ? fmax3(M[2 * s - 1], w0, w1) : fmaxf(M[2 * s - 1], w0);
+                        if (two) {
+                            o0 = __fadd_rn(w0, w2);
+                            o1 = pair ? __fadd_rn(w1, w3) : 0.f;
+                            M[2 * s] = pair ? fmax3(M[2 * s], o0, o1) : fmaxf(M[2 * s], o0);
+                        }
+                        if (more) {
+                            nxt[p0 + u * j] = o0;
+                            if (pair) nxt[p0 + u * (j + 1)] = o1;
+                        }
+                    }
+                    c0 = c2;
+                    c1 = c3;
+                    c2 = c4;
+                    w0 = w2;
+                    w1 = w3;
+                }
+            }
+            if (more) {
+                bar.sync();
+                if (s == 1) stage_next();  // the samples are read: copies overlap the search
             }
         }
-        bar.sync();
+        bool hit = false;
         if (active) {
-            for (int q = tid; q < kBoxTile; q += THREADS) {
-                const long long t = t0 + q;
-                if (t >= n) break;
-                const int i = q + HL;
-                const float bv = best_s[i];
-                if (!(bv >= thr)) continue;
-                float snr;
-                int width;
-                box_best_at<T, NW>(r, t, n, mu_f, inv_w, &snr, &width);
-                const int h = max(width / 2, 1);
-                bool keep = true;
-                for (int u = 1; u <= h && keep; ++u)
-                    if (t - u >= 0 && !(best_s[i - u] < bv)) keep = false;
-                for (int u = 1; u <= h && keep; ++u)
-                    if (t + u <= n - 1 && !(best_s[i + u] <= bv)) keep = false;
-                if (!keep) continue;
-                const unsigned long long at = atomicAdd(count, 1ull);
-                if ((long long)at < cap) cands[at] = DevCand{d, (int32_t)t, width, snr};
-            }
+#pragma unroll
+            for (int l = 0; l < NW; ++l) hit |= snr(M[l], l) >= thr;
         }
-        // (the next tile writes best_s only after its own barriers)
+        const bool flagged = bar.any(hit);
+        if (!staged) stage_next();
+        if (flagged) {
+            box_tile_exact<T, NW, THREADS, K>(r, n, t0, mu_f, thr, inv_w, d, cands, count, cap,
+                                              A, Bf, best_s, bar, tid, active);
+            bar.sync();
+            zero_pads();
+        }
     }
+    if (active) cp_async_wait_all();
 }
 
 }  // namespace mdsm

@@ -784,8 +784,10 @@ __global__ void __launch_bounds__(CfgU8::THREADS, 1)
 constexpr int kFusedSpecCols = kFusedSpecColsHost;  // columns of one phase-2 item (a thread each)
 constexpr int kFusedBoxThreads = 128;  // threads of one search group (4 warps)
 constexpr int kFusedBoxWidths = 9;     // widths 1..256
+constexpr int kFusedBoxK = 19;         // positions per thread
+using FusedBoxGeom = BoxGeom<kFusedBoxWidths, kFusedBoxThreads, kFusedBoxK>;
 // shared memory of one search group (16-byte multiple)
-constexpr size_t kFusedBoxSmem = (BoxGeom<kFusedBoxWidths, kFusedBoxThreads>::SMEM + 15) / 16 * 16;
+constexpr size_t kFusedBoxSmem = (FusedBoxGeom::SMEM + 15) / 16 * 16;
 
 // Bounded wait until *ctr >= target (raised by other CTAs after a fence): polling with
 // backoff, about 4 s at most; on timeout sets ERR_WAIT_TIMEOUT and returns false.
@@ -1031,7 +1033,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1)
         if (!g_ok[grp] || !(sig > 0.0)) continue;  // (uniform across the group)
         const int4 w = f.bx_items[it];
         const FusedBeam &B = f.fb[w.x];
-        box_run<int32_t, kFusedBoxWidths, kFusedBoxThreads>(
+        box_run<int32_t, kFusedBoxWidths, kFusedBoxThreads, kFusedBoxK>(
             B.out + (size_t)w.y * (size_t)B.out_stride, B.nsamp, w.z, w.w, mu, sig, f.threshold,
             w.y, B.cands, B.count, f.cap, gsm, gbar, gt, true);
     }
@@ -1230,6 +1232,8 @@ mdsm_status fused_launch_t(const FusedArgs &f, const KArgs *kargs, const int4 *i
 }  // namespace
 
 int fused_num_shapes() { return 4; }
+
+int fused_box_tile() { return FusedBoxGeom::TILE; }
 
 FusedShapeInfo fused_shape_info(int shape)
 {

@@ -583,6 +583,7 @@ mdsm_status series_stats_launch(const void *y, int dtype, int ndms, long long n,
 }
 
 constexpr int kBoxThreads = 256;
+constexpr int kBoxK = 11;  // positions per thread (tiles of 2816 - 2 HL - WMAX samples)
 
 // One CTA per (DM, run of `tpc` consecutive tiles): the tile loop of box.cuh.
 template <typename T, int NW>
@@ -595,11 +596,13 @@ __global__ void __launch_bounds__(kBoxThreads, 4)
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
     if (!(sig > 0.0)) return;
-    const long long ntiles = (n + kBoxTile - 1) / kBoxTile;
+    constexpr int TILE = BoxGeom<NW, kBoxThreads, kBoxK>::TILE;
+    const long long ntiles = (n + TILE - 1) / TILE;
     const long long tile_lo = (long long)blockIdx.x * tpc;
     const long long tile_hi = tile_lo + tpc < ntiles ? tile_lo + tpc : ntiles;
-    box_run<T, NW, kBoxThreads>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold, d,
-                                cands, count, cap, sm, BoxBarCta{}, (int)threadIdx.x, true);
+    box_run<T, NW, kBoxThreads, kBoxK>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold,
+                                       d, cands, count, cap, sm, BoxBarCta{}, (int)threadIdx.x,
+                                       true);
 }
 
 // The boxcar search of every DM row, for 1..9 widths (a template per width count).
@@ -608,12 +611,12 @@ static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, doub
                                  const double2 *musig, DevCand *cands,
                                  unsigned long long *count, long long cap, cudaStream_t st);
 
-// Shared memory of k_boxcar: two sum buffers, the best SNR of NBEST positions and the next
-// tile's samples.
+// Shared memory of k_boxcar: the staged samples, two sum buffers and the best SNR of NBEST
+// positions.
 template <int NW>
 static size_t boxcar_smem()
 {
-    return BoxGeom<NW, kBoxThreads>::SMEM;
+    return BoxGeom<NW, kBoxThreads, kBoxK>::SMEM;
 }
 
 template <typename T, int NW>
@@ -625,8 +628,9 @@ static cudaError_t launch_boxcar_nw(const T *y, int ndms, long long n, double th
     cudaError_t e = cudaFuncSetAttribute(k_boxcar<T, NW>,
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    // runs of up to 8 tiles per CTA while that leaves >= 8192 CTAs (several waves of 5 per SM)
-    const long long ntiles = (n + kBoxTile - 1) / kBoxTile;
+    // runs of up to 8 tiles per CTA while that leaves >= 8192 CTAs (several waves of 4 per SM)
+    constexpr int TILE = BoxGeom<NW, kBoxThreads, kBoxK>::TILE;
+    const long long ntiles = (n + TILE - 1) / TILE;
     int tpc = (int)std::min<long long>(8, std::max<long long>(1, ntiles * ndms / 8192));
     tpc = (int)std::min<long long>(tpc, ntiles);
     dim3 g3((unsigned)((ntiles + tpc - 1) / tpc), (unsigned)ndms);

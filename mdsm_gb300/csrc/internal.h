@@ -175,6 +175,7 @@ struct FusedShapeInfo {
     int dm_block, time_tile, compute_warps;
 };
 int fused_num_shapes();
+int fused_box_tile();  // output samples per tile of the fused launch's search items
 FusedShapeInfo fused_shape_info(int shape);
 mdsm_status fused_tables(int shape, StageGeom &g, const std::vector<int32_t> &S);
 KArgs fused_kargs(const StageGeom &g, const void *d_rel_common, const unsigned char *in,

@@ -463,8 +463,10 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
 
     unsigned gk = 0;  // chunk sequence number
     bool aborted = false;
-    int sb_beam = -1, sb_nw = 0;  // the last chunk's beam, its phase stride and quad reciprocal
-    unsigned sb_inv = 0;
+    // the chunk's phase stride (words), quads per row and their reciprocal: the kernel's, or,
+    // for sources whose beams keep their own strides, those of the last chunk's beam
+    int nwc = nwp, nqc = nq, sb_beam = -1;
+    unsigned nqc_inv = nq_inv;
     int done_beam = -1;  // beam of an item whose stores are not yet published
     for (;; ++gk) {
         const int s = (int)(gk % kPNR);
@@ -479,20 +481,13 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
             // chunk holds (rows past its channels, or the whole stage at the end of the
             // stream, hold earlier data nobody reads), so the expansion does not wait for the
             // chunk's entry.
-            int nwc = nwp, nqc = nq;  // this chunk's phase stride (words) and quads per row
-            unsigned nqc_inv = nq_inv;
             if constexpr (Src::kBeamStride) {
-                const int4 mm = meta[s];
-                if (mm.x >= 0) {
-                    const int beam = mm.w >> 8;
-                    if (beam != sb_beam) {  // (consecutive chunks mostly share a beam)
-                        sb_beam = beam;
-                        sb_nw = src.args(beam).ps >> 2;
-                        sb_inv = ((1u << 20) + (unsigned)(sb_nw >> 2) - 1) / (unsigned)(sb_nw >> 2);
-                    }
-                    nwc = sb_nw;
+                const int beam = m.w >> 8;
+                if (m.x >= 0 && beam != sb_beam) {  // (consecutive chunks mostly share a beam)
+                    sb_beam = beam;
+                    nwc = src.args(beam).ps >> 2;
                     nqc = nwc >> 2;
-                    nqc_inv = sb_inv;
+                    nqc_inv = ((1u << 20) + (unsigned)nqc - 1) / (unsigned)nqc;
                 }
             }
             for (int q = tid; q < kPCC * nqc; q += NW * 32) {

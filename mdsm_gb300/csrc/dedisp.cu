@@ -329,6 +329,15 @@ __device__ __forceinline__ uint32_t odd_lanes(uint32_t w)
         return w >> 16;
 }
 
+// o + (w >> 16) as (w * 2^16) >> 32 + o: one integer multiply-add, issued on the FMA pipe, so
+// that the uint16 kernel's odd-lane sums leave the ALU pipe to the raw-word sums.
+__device__ __forceinline__ uint32_t add_hi16(uint32_t w, uint32_t o)
+{
+    uint32_t d;
+    asm("mad.hi.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(w), "r"(0x10000u), "r"(o));
+    return d;
+}
+
 template <class Cfg, class Src>
 __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int rawcap, int ps,
                                               unsigned *err)
@@ -580,7 +589,10 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
 #pragma unroll
                 for (int j = 0; j < DPW; ++j) {
                     A[j][r] = A[j][r] + wa[j] + wz[j];
-                    O[j][r] += odd_lanes<SW>(wa[j]) + odd_lanes<SW>(wz[j]);
+                    if constexpr (SW == 2)
+                        O[j][r] = add_hi16(wz[j], add_hi16(wa[j], O[j][r]));
+                    else
+                        O[j][r] += odd_lanes<SW>(wa[j]) + odd_lanes<SW>(wz[j]);
                 }
             }
         };
@@ -603,7 +615,10 @@ __device__ __forceinline__ void packed_stream(Src &src, unsigned char *smem, int
                 for (int j = 0; j < DPW; ++j) {
                     const uint32_t wa = reinterpret_cast<const uint32_t *>(pa + oa[j])[32 * r];
                     A[j][r] += wa;
-                    O[j][r] += odd_lanes<SW>(wa);
+                    if constexpr (SW == 2)
+                        O[j][r] = add_hi16(wa, O[j][r]);
+                    else
+                        O[j][r] += odd_lanes<SW>(wa);
                 }
         }
         const bool last = (m.w & kChunkLast) != 0;

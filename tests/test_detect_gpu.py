@@ -77,6 +77,43 @@ def test_boxcar_matches_oracle(lib, orc, cuda, dtype, nw, n):
     assert np.array_equal(cands["snr"], snr)
 
 
+@pytest.mark.parametrize("dtype,nw,thr", [("i32", 1, 6.0), ("f32", 3, 6.0), ("i32", 4, 6.0),
+                                          ("f32", 6, 6.0), ("i32", 8, 6.0), ("f32", 9, 3.5)])
+def test_boxcar_fast_path_and_tile_boundaries(lib, orc, cuda, dtype, nw, thr):
+    """Rows long enough for interior tiles at every width count (the chain fast path), with
+    pulses on both sides of interior tile boundaries (output tiles of 2816 - 2 HL - WMAX
+    samples, rounded down to a multiple of 4) and, at a 3.5 sigma threshold, most tiles flagged
+    for the exact search."""
+    import mdsm_gb300 as m
+    torch = cuda
+    wmax = 1 << (nw - 1)
+    hl = max(wmax // 2, 1)
+    tile = (2816 - 2 * hl - wmax) & ~3
+    n = 6 * tile + 777
+    rng = np.random.default_rng(70 + nw)
+    ndms = 16
+    if dtype == "i32":
+        y = rng.integers(-3000, 3000, (ndms, n)).astype(np.int32)
+        amp = [40000, 9000, 3000]
+    else:
+        y = rng.standard_normal((ndms, n)).astype(np.float32)
+        amp = [np.float32(30.0), np.float32(7.0), np.float32(2.5)]
+    for k in range(1, 6):
+        for j, off in enumerate((-hl - 1, -1, 0, 1, hl)):
+            row = (3 * k + j) % ndms
+            t = k * tile + off
+            w = min(1 << ((k + j) % nw), 64)
+            y[row, t:t + w] += amp[(k + j) % 3]
+    cands, cnt = m.boxcar_detect_device(torch.from_numpy(y).cuda(), nwidths=nw, threshold=thr,
+                                        cap=1 << 20)
+    dm, samp, wid, snr = orc.boxcar_detect(y, nw, thr)
+    assert cnt == len(dm) > 0
+    assert np.array_equal(cands["dm_idx"], dm)
+    assert np.array_equal(cands["sample"], samp)
+    assert np.array_equal(cands["width"], wid)
+    assert np.array_equal(cands["snr"], snr)
+
+
 def test_detrend_normalise_matches_oracle(lib, orc, cuda):
     """src/prototypes/detrend.cu:12-100 restated; double sums in a different order on the two
     sides, so the bar is 1e-5 relative."""

@@ -59,9 +59,12 @@ class ClockSampler:
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
 
     def __init__(self, gpu_index):
+        import tempfile
         self.idx = gpu_index
         self.p = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench_%d.csv" % os.getpid())
+        # the raw samples (MDSM_CLOCKS_DIR keeps them; by default a temporary directory)
+        d = os.environ.get("MDSM_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(d, "clocks_bench_%d_%d.csv" % (os.getpid(), id(self)))
 
     def __enter__(self):
         try:

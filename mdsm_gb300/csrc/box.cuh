@@ -2,20 +2,20 @@
 // standalone search kernel (detect.cu) and the fused batched launch (dedisp.cu).
 //
 // Widths 1, 2, 4, ..., 2^(NW-1); per DM row the mean and sigma come from the caller.  A run of
-// consecutive 2048-sample tiles of one row is searched by a group of THREADS threads: the
-// whole CTA (BoxBarCta) or one of several groups of a CTA, each with its own named barrier and
-// shared memory (BoxBarGroup), so that one wide CTA runs several searches whose barriers
-// overlap.  The samples of the next tile are copied into shared memory
-// (cp.async) while the current one is searched.  Arithmetic per sample and width is FP32,
-// explicitly rounded, in the oracle's order; each thread owns the position pairs
-// (2 tid + 2 THREADS q, +1), keeps their boxcar sums and best SNR in registers across the
-// widths and reads only partner sums from shared memory: two widths per step (B_2u and B_4u
-// from B_u, three 8-byte loads per pair), so two widths cost per pair three shared loads, one
-// shared store, one barrier (the sums alternate between two buffers), and per width three
-// paired FP32 operations and two maxima.  Which
-// width gave the best SNR is needed only where the best passes the threshold (few
-// positions): there box_best_at forms it again, with the same sums.  Candidates are local
-// maxima of the best SNR over max(w/2, 1) samples on each side.
+// consecutive tiles of one row is searched by a group of THREADS threads: the whole CTA
+// (BoxBarCta) or one of several groups of a CTA, each with its own named barrier and shared
+// memory (BoxBarGroup), so that one wide CTA runs several searches whose barriers overlap.
+// The next tile's samples are copied into shared memory (cp.async) while the current one is
+// searched.  Arithmetic per sample and width is FP32, explicitly rounded, in the oracle's
+// order: B_2u[i] = B_u[i] + B_u[i + u], B_4u[i] = B_2u[i] + B_2u[i + 2u], and the SNR
+// (B_w - w mu) / (sigma sqrt w) with 1 / (sigma sqrt w) rounded once per width.
+//
+// Two paths (box_run): a fast path that only decides whether a tile reaches the threshold,
+// over chains of one residue class of each step's stride per thread, keeping the largest sum
+// of each width; and an exact path (box_tile_exact) for the tiles it flags and the edge tiles:
+// every position's best SNR over the widths, then the candidates, local maxima of the best
+// SNR over max(w/2, 1) samples on each side, with the width that gave the best formed again
+// for those few positions (box_best_at).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>

@@ -112,25 +112,29 @@ __global__ void k_ref_finish(const double2 *__restrict__ sums, unsigned mod, uns
     stats[1] = __double2float_rn(__dsqrt_rn(v));
 }
 
-// dedispersion_output.cpp:176-210 (one device, mean == NULL).
+// dedispersion_output.cpp:176-210 (mean == NULL).  Rows are the worker threads' rows in turn,
+// rpt per thread; row k of thread t has DM lowdm + (unsigned)(tshift * t) + k dmstep in float,
+// left to right (:187,194; one thread: rpt = ndms, tshift = 0).
 __global__ void k_ref_detect(const float *__restrict__ buf, int ndms, int nsamp, float lowdm,
                              float dmstep, float threshold, const float *__restrict__ stats,
                              DevCand *__restrict__ cands, unsigned long long *__restrict__ count,
-                             long long cap)
+                             long long cap, int rpt, int tshift)
 {
-    const int k = blockIdx.y;
-    const float thisdm = __fadd_rn(__fadd_rn(lowdm, 0.0f), __fmul_rn((float)(unsigned)k, dmstep));
+    const int row = blockIdx.y;
+    const unsigned t = (unsigned)row / (unsigned)rpt, k = (unsigned)row % (unsigned)rpt;
+    const float thisdm = __fadd_rn(__fadd_rn(lowdm, (float)((unsigned)tshift * t)),
+                                   __fmul_rn((float)k, dmstep));
     if (!((double)thisdm > 1.0)) return;
     const float mean = stats[0], rms = stats[1];
     const float lim = __fmul_rn(rms, threshold);
-    const float *r = buf + (size_t)k * nsamp;
+    const float *r = buf + (size_t)row * nsamp;
     const unsigned nl = (unsigned)nsamp - 4u;
     for (unsigned l = blockIdx.x * blockDim.x + threadIdx.x; l < nl; l += gridDim.x * blockDim.x) {
         const float m = median5(__ldg(r + l), __ldg(r + l + 1), __ldg(r + l + 2), __ldg(r + l + 3),
                                 __ldg(r + l + 4));
         if (__fsub_rn(m, mean) >= lim) {
             const unsigned long long at = atomicAdd(count, 1ull);
-            if ((long long)at < cap) cands[at] = DevCand{k, (int32_t)l, 1, __fdiv_rn(m, rms)};
+            if ((long long)at < cap) cands[at] = DevCand{row, (int32_t)l, 1, __fdiv_rn(m, rms)};
         }
     }
 }
@@ -172,7 +176,21 @@ mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, 
                        float threshold, mdsm_candidate *h_cands, long long cap,
                        long long *ncand, float *mean, float *rms, cudaStream_t st)
 {
-    const unsigned long long vals64 = (unsigned long long)ndms * (unsigned long long)nsamp;
+    return ref_detect_threads(d_series, ndms, nsamp, -1, ndms, 0, lowdm, dmstep, threshold,
+                              h_cands, cap, ncand, mean, rms, st);
+}
+
+mdsm_status ref_detect_threads(const float *d_series, int ndms, int nsamp, long long stat_vals,
+                               int rpt, int tshift, float lowdm, float dmstep, float threshold,
+                               mdsm_candidate *h_cands, long long cap, long long *ncand,
+                               float *mean, float *rms, cudaStream_t st)
+{
+    if (rpt <= 0) return fail(MDSM_EINVAL, "reference detector: rows per thread");
+    const unsigned long long vals64 = stat_vals >= 0
+                                          ? (unsigned long long)stat_vals
+                                          : (unsigned long long)ndms * (unsigned long long)nsamp;
+    if (vals64 == 0 || vals64 > (unsigned long long)ndms * (unsigned long long)nsamp)
+        return fail(MDSM_EINVAL, "reference detector: statistics over the series' values");
     if (vals64 > 0xFFFFFFFFull / 2)
         return fail(MDSM_EINVAL, "reference detector counts values in 32 bits");
     const unsigned vals = (unsigned)vals64;
@@ -197,7 +215,7 @@ mdsm_status ref_detect(const float *d_series, int ndms, int nsamp, float lowdm, 
     k_ref_finish<<<1, 1, 0, st>>>(d_sums, mod, nchunks, d_stats);
     dim3 grid((unsigned)std::min<long long>((nsamp + 255) / 256, 64), (unsigned)ndms);
     k_ref_detect<<<grid, 256, 0, st>>>(d_series, ndms, nsamp, lowdm, dmstep, threshold, d_stats,
-                                       d_c, d_count, cap);
+                                       d_c, d_count, cap, rpt, tshift);
     MDSM_CUDA_TRY(cudaGetLastError());
     float hs[2];
     MDSM_CUDA_TRY(cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));
@@ -303,7 +321,7 @@ mdsm_status ref_detect_chunked(const float *d_series, int ndms, int nsamp, float
                                float dmstep, float threshold, const float *h_mean,
                                const float *h_rms, long long nchunks, int spc,
                                mdsm_candidate *h_cands, long long cap, long long *ncand,
-                               cudaStream_t st)
+                               cudaStream_t st, const float *h_dmv)
 {
     if (spc <= 0 || nchunks < (long long)(nsamp - 5) / spc + 1)
         return fail(MDSM_ERANGE, "chunk statistics: fewer values than (nsamp - 4) / spc");
@@ -313,7 +331,8 @@ mdsm_status ref_detect_chunked(const float *d_series, int ndms, int nsamp, float
     MDSM_TRY(median_work(ndms, nchunks, cap, &w, &lease));
     // the reference's DM of row k: lowdm + k * dmstep in float (dedispersion_output.cpp:194)
     std::vector<float> dmv((size_t)ndms);
-    for (int k = 0; k < ndms; ++k) dmv[(size_t)k] = (lowdm + 0.0f) + (float)(unsigned)k * dmstep;
+    for (int k = 0; k < ndms; ++k)
+        dmv[(size_t)k] = h_dmv ? h_dmv[k] : (lowdm + 0.0f) + (float)(unsigned)k * dmstep;
     MDSM_CUDA_TRY(cudaMemsetAsync(w.count, 0, sizeof(unsigned long long), st));
     MDSM_CUDA_TRY(cudaMemcpyAsync(w.dmv, dmv.data(), dmv.size() * 4, cudaMemcpyHostToDevice, st));
     MDSM_CUDA_TRY(cudaMemcpyAsync(w.cmean, h_mean, (size_t)nchunks * 4, cudaMemcpyHostToDevice, st));
@@ -438,7 +457,7 @@ mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float
     k_ref_finish<<<1, 1, 0, st>>>(d_sums, mod, nchunks, d_stats);
     dim3 grid((unsigned)std::min<long long>((nsamp + 255) / 256, 64), (unsigned)ndms);
     k_ref_detect<<<grid, 256, 0, st>>>(d_series, ndms, nsamp, lowdm, dmstep, threshold, d_stats,
-                                       d_c, d_count, cap);
+                                       d_c, d_count, cap, ndms, 0);
     MDSM_CUDA_TRY(cudaGetLastError());
     float hs[2];
     MDSM_CUDA_TRY(cudaMemcpyAsync(hs, d_stats, sizeof(hs), cudaMemcpyDeviceToHost, st));

@@ -277,11 +277,22 @@ mdsm_status ref_detect_noalloc(const float *d_series, int ndms, int nsamp, float
                                float dmstep, float threshold, mdsm_candidate *h_cands,
                                long long cap, long long *ncand, float *mean, float *rms,
                                cudaStream_t st);
+// process_brute over the rows of several worker threads in turn (rpt rows each, DM of row k
+// of thread t lowdm + (unsigned)(tshift * t) + k dmstep), with the statistics over the first
+// stat_vals values (-1: all of them).
+// Worker thread `thread`'s plan, of nthr threads, for blocks of nsamp samples of the survey
+// (wrapper.cpp; the reference's launchers' DM slices).
+mdsm_status plan_for_thread(const SURVEY *s, int thread, int nthr, int nsamp, mdsm_plan **out);
+mdsm_status ref_detect_threads(const float *d_series, int ndms, int nsamp, long long stat_vals,
+                               int rpt, int tshift, float lowdm, float dmstep, float threshold,
+                               mdsm_candidate *h_cands, long long cap, long long *ncand,
+                               float *mean, float *rms, cudaStream_t st);
+// h_dmv (optional): each row's DM in place of lowdm + k dmstep
 mdsm_status ref_detect_chunked(const float *d_series, int ndms, int nsamp, float lowdm,
                                float dmstep, float threshold, const float *h_mean,
                                const float *h_rms, long long nchunks, int spc,
                                mdsm_candidate *h_cands, long long cap, long long *ncand,
-                               cudaStream_t st);
+                               cudaStream_t st, const float *h_dmv = nullptr);
 struct Plan;
 mdsm_status ref_detect_subband(const Plan &p, const float *d_series, long long out_stride,
                                float threshold, const float *h_mean, const float *h_rms,

@@ -42,17 +42,19 @@ void report(const THREAD_PARAMS *tp, const char *what)
     fprintf(stderr, "mdsm worker %d: %s: %s\n", (int)tp->thread_num, what, mdsm_last_error());
 }
 
-// The thread's plan for blocks of nsamp samples: the DM slice and shift arithmetic the
-// reference's launchers use (dedispersion_thread.cu:64-94, 97-217, 220-243).
-mdsm_status build_plan(const THREAD_PARAMS *tp, int nsamp, mdsm_plan **out)
+}  // namespace
+
+// Worker thread `thread`'s plan (of nthr sharing the sub-DM calls) for blocks of nsamp
+// samples: the DM slice and shift arithmetic the reference's launchers use
+// (dedispersion_thread.cu:64-94, 97-217, 220-243).
+mdsm_status plan_for_thread(const SURVEY *s, int thread, int nthr, int nsamp, mdsm_plan **out)
 {
-    const SURVEY *s = tp->survey;
     if (s->useBruteForce) {
-        const unsigned nthr = s->num_threads ? s->num_threads : 1;
+        // (the brute-force DM ranges split by the survey's thread count)
+        const unsigned nb = s->num_threads ? s->num_threads : 1;
         // dedispersion_thread.cu:76,229: float arithmetic, left to right
-        const float startdm =
-            s->lowdm + s->dmstep * (float)s->tdms / (float)nthr * (float)tp->thread_num;
-        mdsm_segment seg{startdm, s->dmstep, (int)(s->tdms / nthr)};
+        const float startdm = s->lowdm + s->dmstep * (float)s->tdms / (float)nb * (float)thread;
+        mdsm_segment seg{startdm, s->dmstep, (int)(s->tdms / nb)};
         mdsm_brute_desc d;
         memset(&d, 0, sizeof d);
         d.nchans = (int)s->nchans;
@@ -67,12 +69,12 @@ mdsm_status build_plan(const THREAD_PARAMS *tp, int nsamp, mdsm_plan **out)
         d.out_dtype = MDSM_OUT_F32;
         return mdsm_brute_plan_create(&d, out);
     }
-    const int nthr = tp->num_threads ? tp->num_threads : 1;
+    if (nthr < 1) nthr = 1;
     std::vector<SUBBAND_PASSES> passes(s->pass_parameters, s->pass_parameters + s->num_passes);
     for (SUBBAND_PASSES &p : passes) {
         // dedispersion_thread.cu:160-161: the sub-DM calls are split among the threads
         p.ncalls = p.ncalls / nthr;
-        p.lowdm = p.lowdm + p.sub_dmstep * (float)p.ncalls * (float)tp->thread_num;
+        p.lowdm = p.lowdm + p.sub_dmstep * (float)p.ncalls * (float)thread;
     }
     mdsm_subband_desc d;
     memset(&d, 0, sizeof d);
@@ -88,6 +90,13 @@ mdsm_status build_plan(const THREAD_PARAMS *tp, int nsamp, mdsm_plan **out)
     d.in_dtype = MDSM_F32;
     d.out_dtype = MDSM_OUT_F32;
     return mdsm_subband_plan_create(&d, out);
+}
+
+namespace {
+
+mdsm_status build_plan(const THREAD_PARAMS *tp, int nsamp, mdsm_plan **out)
+{
+    return plan_for_thread(tp->survey, tp->thread_num, tp->num_threads, nsamp, out);
 }
 
 // Grow-only device buffer; *fresh tells whether it was (re)allocated.

@@ -12,6 +12,13 @@
  *        manager_driver spectra.f32 out.f32 nchans nsamp fch1 foff tsamp subband nsubs
  *                       "lowdm,highdm,dmstep,sub_dmstep,ncalls,calldms,binsize;..."
  * prints "blocks B outputs O maxshift M dedispersed_size D" on success.
+ *
+ * Environment: MDSM_DRIVER_THREADS=N runs N workers (devices beyond the machine's repeat its
+ * first); MDSM_DRIVER_OUTPUT=dir starts the library's process_output (the reference's output
+ * thread, src/mdsm/dedispersion_manager.cpp:331-344) instead of the capture thread, writing
+ * its candidates to dir/cands.dat at threshold MDSM_DRIVER_THRESHOLD (default 6).  Block k is
+ * handed in with timestamp 1000 + k nsamp tsamp and blockRate tsamp, as next_chunk's callers
+ * pass them (src/mdsm/dedispersion_manager.cpp:416-484).
  */
 #include <pthread.h>
 #include <stdio.h>
@@ -19,6 +26,7 @@
 #include <string.h>
 #include <time.h>
 
+#include "dedispersion_output.h"
 #include "dedispersion_thread.h"
 #include "mdsm_gb300.h"
 
@@ -42,6 +50,8 @@ static pthread_rwlock_t rw_lock = PTHREAD_RWLOCK_INITIALIZER;
 static pthread_t *threads, output_thread;
 static THREAD_PARAMS *threads_params;
 static CAPTURE capture;
+static OUTPUT_PARAMS output_params;
+static int use_output;
 static float *input_buffer, *output_buffer, *dmshifts;
 static unsigned pnsamp, ppnsamp;
 
@@ -90,6 +100,16 @@ static float *initialise(FILE *out)
     unsigned i;
     devices = call_initialise_devices(&survey);
     if (!devices) return NULL;
+    const char *nthr = getenv("MDSM_DRIVER_THREADS");
+    if (nthr && atoi(nthr) > devices->num_devices) {
+        /* more workers than devices: the extra ones share the first device */
+        int n = atoi(nthr);
+        DEVICE_INFO *d = (DEVICE_INFO *)calloc((size_t)n, sizeof(DEVICE_INFO));
+        for (k = 0; k < n; k++) d[k] = devices->devices[k < devices->num_devices ? k : 0];
+        free(devices->devices);
+        devices->devices = d;
+        devices->num_devices = n;
+    }
     num_devices = devices->num_devices;
     survey.num_threads = (unsigned)num_devices;
     threads = (pthread_t *)calloc((size_t)num_devices, sizeof(pthread_t));
@@ -123,7 +143,22 @@ static float *initialise(FILE *out)
     capture.input_barrier = &input_barrier;
     capture.output_barrier = &output_barrier;
     capture.out = out;
-    pthread_create(&output_thread, NULL, capture_output, &capture);
+    if (use_output) {
+        output_params.nthreads = num_devices;
+        output_params.iterations = 2;
+        output_params.maxiters = 2;
+        output_params.output_buffer = output_buffer;
+        output_params.dedispersed_size = outsize;
+        output_params.stop = 0;
+        output_params.rw_lock = &rw_lock;
+        output_params.input_barrier = &input_barrier;
+        output_params.output_barrier = &output_barrier;
+        output_params.start = time(NULL);
+        output_params.survey = &survey;
+        pthread_create(&output_thread, NULL, process_output, &output_params);
+    } else {
+        pthread_create(&output_thread, NULL, capture_output, &capture);
+    }
     for (k = 0; k < num_devices; k++) {
         THREAD_PARAMS *t = &threads_params[k];
         t->iterations = 1;
@@ -151,15 +186,18 @@ static float *initialise(FILE *out)
     return input_buffer;
 }
 
-static void next_chunk(unsigned data_read)
+static void next_chunk(unsigned data_read, unsigned block)
 {
     int k;
     pthread_rwlock_wrlock(&rw_lock);
     barrier(&output_barrier);
     ppnsamp = pnsamp;
     pnsamp = data_read;
+    survey.timestamp = 1000.0 + (double)block * (double)survey.nsamp * (double)survey.tsamp;
+    survey.blockRate = (double)survey.tsamp;
     if (data_read == 0) {
         capture.stop = 1;
+        output_params.stop = 1;
         for (k = 0; k < num_devices; k++) threads_params[k].stop = 1;
     }
     pthread_rwlock_unlock(&rw_lock);
@@ -242,6 +280,15 @@ int main(int argc, char **argv)
         for (unsigned i = 0; i < survey.num_passes; i++)
             survey.tdms += (unsigned)passes[i].ndms;
     }
+    const char *odir = getenv("MDSM_DRIVER_OUTPUT");
+    if (odir && *odir) {
+        use_output = 1;
+        snprintf(survey.basedir, sizeof survey.basedir, "%s", odir);
+        snprintf(survey.fileprefix, sizeof survey.fileprefix, "cands");
+        survey.single_file_mode = 1;
+        const char *thr = getenv("MDSM_DRIVER_THRESHOLD");
+        survey.detection_threshold = thr ? (float)atof(thr) : 6.0f;
+    }
     FILE *fp = fopen(argv[1], "rb"), *out = fopen(argv[2], "wb");
     if (!fp || !out) return 4;
     if (!initialise(out)) {
@@ -257,14 +304,14 @@ int main(int argc, char **argv)
             data_read = read_block(fp, input_buffer, counter);
         }
         if (data_read < survey.nsamp) data_read = 0;  /* whole blocks only */
-        next_chunk(data_read);
+        next_chunk(data_read, counter);
         if (!start_processing(data_read)) break;
         counter++;
     }
     tear_down();
     fclose(fp);
     fclose(out);
-    printf("blocks %u outputs %d maxshift %u dedispersed_size %zu\n", counter, capture.written,
-           survey.maxshift, capture.total);
+    printf("blocks %u outputs %d maxshift %u dedispersed_size %zu threads %d\n", counter,
+           capture.written, survey.maxshift, capture.total, num_devices);
     return 0;
 }

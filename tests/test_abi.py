@@ -21,7 +21,8 @@ def declared_functions():
         src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
         if "extern \"C\"" not in src and fn != "mdsm_gb300.h":
             continue
-        for m in re.finditer(r"\b(mdsm_[A-Za-z0-9_]+|call_[A-Za-z0-9_]+)\s*\(", src):
+        for m in re.finditer(r"\b(mdsm_[A-Za-z0-9_]+|call_[A-Za-z0-9_]+|process_output)\s*\(",
+                             src):
             names.add(m.group(1))
     return sorted(names)
 
@@ -31,7 +32,7 @@ def test_every_declared_symbol_is_exported(lib):
     assert len(names) > 20
     missing = [n for n in names if not hasattr(lib, n)]
     assert not missing, missing
-    assert {"call_dedisperse", "call_initialise_devices"} <= set(names)
+    assert {"call_dedisperse", "call_initialise_devices", "process_output"} <= set(names)
     from mdsm_gb300 import _lib
     bound = set(_lib.SIGNATURES) | set(_lib.SERVER_SYMBOLS)
     mdsm_names = {n for n in names if n.startswith("mdsm_")}
@@ -186,6 +187,47 @@ def test_thread_abi_layouts_match_reference():
             assert getattr(types[t], f).offset == val, key
         else:
             assert ctypes.sizeof(types[key]) == val, key
+
+
+OUTPUT_LAYOUT = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "dedispersion_output.h"
+#define P(T, f) printf(#T "." #f " %zu\n", offsetof(T, f))
+int main(void) {
+  printf("OUTPUT_PARAMS %zu\n", sizeof(OUTPUT_PARAMS));
+  P(OUTPUT_PARAMS, iterations); P(OUTPUT_PARAMS, maxiters); P(OUTPUT_PARAMS, output_buffer);
+  P(OUTPUT_PARAMS, dedispersed_size); P(OUTPUT_PARAMS, stop); P(OUTPUT_PARAMS, rw_lock);
+  P(OUTPUT_PARAMS, input_barrier); P(OUTPUT_PARAMS, output_barrier); P(OUTPUT_PARAMS, start);
+  P(OUTPUT_PARAMS, survey);
+  return 0;
+}
+"""
+
+
+def test_output_abi_layout_matches_reference():
+    """OUTPUT_PARAMS of include/dedispersion_output.h has the reference's member order and
+    types (src/mdsm/dedispersion_output.h:8-28)."""
+    c = ctypes
+
+    class OutputParams(c.Structure):
+        _fields_ = [("nthreads", c.c_int), ("iterations", c.c_int), ("maxiters", c.c_int),
+                    ("output_buffer", c.c_void_p), ("dedispersed_size", c.c_size_t),
+                    ("stop", c.c_ushort), ("rw_lock", c.c_void_p),
+                    ("input_barrier", c.c_void_p), ("output_barrier", c.c_void_p),
+                    ("start", c.c_long), ("survey", c.c_void_p)]
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "t.c")
+        exe = os.path.join(d, "t")
+        open(src, "w").write(OUTPUT_LAYOUT)
+        subprocess.run(["gcc", "-I", INC, "-o", exe, src], check=True)
+        out = subprocess.run([exe], capture_output=True, text=True, check=True).stdout
+    for line in out.splitlines():
+        key, val = line.split()
+        if "." in key:
+            assert getattr(OutputParams, key.split(".")[1]).offset == int(val), key
+        else:
+            assert ctypes.sizeof(OutputParams) == int(val), key
 
 
 def test_qstring_overload_with_header_first():

@@ -36,6 +36,7 @@ struct OutState {
     int plan_nsamp = -1;
     FILE *fp = nullptr;
     long long written = 0;  // samples written to the current file
+    std::vector<mdsm_candidate> cands;  // one block's candidates (kOutCap, allocated once)
 };
 
 void report(const char *what) { fprintf(stderr, "mdsm output: %s: %s\n", what, mdsm_last_error()); }
@@ -104,7 +105,8 @@ mdsm_status search_brute(OutState &o, const OUTPUT_PARAMS *p, int read_nsamp, do
     MDSM_CUDA_TRY(cudaMemcpyAsync(o.d_buf, p->output_buffer, n * 4, cudaMemcpyHostToDevice, o.st));
     // dedispersion_output.cpp:187: the DM offset of each thread, in float, truncated to int
     const int tshift = (int)((float)s->tdms * s->dmstep / (float)nt);
-    std::vector<mdsm_candidate> c((size_t)kOutCap);
+    std::vector<mdsm_candidate> &c = o.cands;
+    c.resize((size_t)kOutCap);
     long long nc = 0;
     const float *y = static_cast<const float *>(o.d_buf);
     const float thr = s->detection_threshold;
@@ -154,7 +156,8 @@ mdsm_status search_subband(OutState &o, const OUTPUT_PARAMS *p, double ts, doubl
     }
     const int spc = s->samplesPerChunk ? (int)s->samplesPerChunk : nsamp;
     const long long nchunks = (nsamp - 5) / spc + 1;
-    std::vector<mdsm_candidate> c((size_t)kOutCap);
+    std::vector<mdsm_candidate> &c = o.cands;
+    c.resize((size_t)kOutCap);
     for (int t = 0; t < nt; ++t) {
         const Plan &pl = o.plans[(size_t)t]->p;
         MDSM_TRY(ensure_buf(o, (size_t)pl.ndms * (size_t)nsamp * 4));

@@ -877,13 +877,15 @@ struct FusedItems {
     unsigned *done;
     unsigned *err;
     bool count;  // phase 4 waits on the stores
+    bool clip;   // the items wait for their beam's spectrum clips
     __device__ int grab()
     {
         const int it = (int)atomicAdd(counter, 1u);
         if (it >= nitems) return -1;
-        const int b = items[it].x;
-        const unsigned target = fb[b].nspec_items;
-        if (target) wait_count(&done[3 * b + 1], target, err);  // (a timeout is recorded)
+        if (clip) {
+            const int b = items[it].x;
+            wait_count(&done[3 * b + 1], fb[b].nspec_items, err);  // (a timeout is recorded)
+        }
         return it;
     }
     __device__ int4 item(int it) const { return items[it]; }
@@ -990,7 +992,8 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1)
     __syncthreads();
     packed_init_barriers(smem);
     {
-        FusedItems src{beams, dd_items, n_dd, &f.counters[2], f.fb, f.done, f.err, f.n_bx > 0};
+        FusedItems src{beams, dd_items, n_dd, &f.counters[2], f.fb, f.done, f.err, f.n_bx > 0,
+                       f.n_cs > 0};
         packed_stream<Cfg>(src, smem, rawcap, ps, f.err);
     }
     __syncthreads();

@@ -98,8 +98,9 @@ mdsm_status search_brute(OutState &o, const OUTPUT_PARAMS *p, int read_nsamp, do
     const int rpt = (int)(s->tdms / nt);
     const int ndms = rpt * (int)nt;
     if (rpt <= 0 || nsamp < 5) return MDSM_OK;
-    if (p->dedispersed_size != (size_t)rpt * (size_t)nsamp)
-        return fail(MDSM_EINVAL, "output thread: each worker's series must be its rows of nsamp");
+    if (p->dedispersed_size != (size_t)rpt * (size_t)nsamp || p->nthreads != (int)nt)
+        return fail(MDSM_EINVAL, "output thread: the buffer must hold num_threads workers' "
+                                 "rows of nsamp");
     const size_t n = (size_t)ndms * (size_t)nsamp;
     MDSM_TRY(ensure_buf(o, n * 4));
     MDSM_CUDA_TRY(cudaMemcpyAsync(o.d_buf, p->output_buffer, n * 4, cudaMemcpyHostToDevice, o.st));
@@ -148,6 +149,8 @@ mdsm_status search_subband(OutState &o, const OUTPUT_PARAMS *p, double ts, doubl
     const SURVEY *s = p->survey;
     const int nt = s->num_threads ? (int)s->num_threads : 1;
     const int nsamp = (int)s->nsamp;
+    if (p->nthreads != nt)
+        return fail(MDSM_EINVAL, "output thread: the buffer must hold num_threads workers' series");
     if (o.plan_nsamp != nsamp || (int)o.plans.size() != nt) {
         drop_plans(o);
         o.plans.assign((size_t)nt, nullptr);

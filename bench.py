@@ -801,6 +801,9 @@ def main():
                     help="leave the serving object out of the default line")
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--batch-beams", type=int, default=32)
+    ap.add_argument("--kernel", default="auto", choices=["auto", "generic"],
+                    help="plain path: the plan's own kernel choice, or the generic kernel "
+                         "(profiling comparisons)")
     ap.add_argument("--no-batched", action="store_true",
                     help="leave the batched object out of the default line")
     args = ap.parse_args()
@@ -846,7 +849,8 @@ def main():
         WORKLOAD = ("profiling case: uint8 2048 ch x 2^16 samples, 512 DM trials 0-500, INT32 "
                     "accumulation (input 168 MB > L2)")
     plan = m.BrutePlan(NCHANS, FCH1, -BW / NCHANS, TSAMP, NSAMP, SEGMENTS, shift_mode="l1",
-                       in_dtype="u8", out_dtype="i32")
+                       in_dtype="u8", out_dtype="i32",
+                       kernel=1 if args.kernel == "generic" else 0)
     info = plan.info
     stream = torch.cuda.Stream()
     gen = torch.Generator(device="cuda")

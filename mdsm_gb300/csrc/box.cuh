@@ -7,13 +7,13 @@
 // memory (BoxBarGroup), so that one wide CTA runs several searches whose barriers overlap.
 // The next tile's samples are copied into shared memory (cp.async) while the current one is
 // searched.  Arithmetic per sample and width is FP32, explicitly rounded, in the oracle's
-// order: B_2u[i] = B_u[i] + B_u[i + u], B_4u[i] = B_2u[i] + B_2u[i + 2u], and the SNR
+// order: B_2w[i] = B_w[i] + B_w[i + w] (a pairwise tree over each boxcar), and the SNR
 // (B_w - w mu) / (sigma sqrt w) with 1 / (sigma sqrt w) rounded once per width.
 //
 // Two paths (box_run): a fast path that only decides whether a tile reaches the threshold,
 // over chains of one residue class of each step's stride per thread, keeping the largest sum
-// of each width; and an exact path (box_tile_exact) for the tiles it flags and the edge tiles:
-// every position's best SNR over the widths, then the candidates, local maxima of the best
+// of each width; and an exact path (box_tile_exact) for the tiles it flags: every position's
+// best SNR over the widths, then the candidates, local maxima of the best
 // SNR over max(w/2, 1) samples on each side, with the width that gave the best formed again
 // for those few positions (box_best_at).
 #pragma once
@@ -65,32 +65,52 @@ __device__ __forceinline__ float fmax3(float a, float b, float c)
 }
 
 // Tile geometry of the search for NW widths (1 .. WMAX = 2^(NW-1)) by a group of THREADS
-// threads, each owning K positions of the staged region (K odd).  A tile's output samples are
-// [t0, t0 + TILE); the region holds the N = THREADS * K samples [t0 - HL, t0 + TILE + HL + WMAX)
-// that its kept boxcars and their neighbourhoods touch, so NBEST = TILE + 2 HL positions carry
-// a best SNR.
-template <int NW, int THREADS, int K>
+// threads, each owning K positions of a region of N = THREADS * K samples (K odd).
+//
+// A tile's output samples are [t0, t0 + TILE).  The fast path stages the region [t0, t0 + N),
+// which holds every boxcar that starts in the tile (TILE <= N - WMAX + 1).  The exact path
+// searches a tile in parts of ETILE output samples [a, a + ETILE), each from a region of
+// NE = THREADS * KE samples [a - HL, a + ETILE + HL + WMAX) that also holds the neighbourhoods
+// of the kept boxcars; NBEST = ETILE + 2 HL positions carry a best SNR.
+template <int NW, int THREADS, int K, int KE = K>
 struct BoxGeom {
     static_assert(NW >= 1 && NW <= 9, "widths 1 .. 256");
     static_assert(K % 2 == 1, "odd positions per thread (no bank conflicts in the chains)");
+    static_assert(KE >= 1 && KE <= K, "the exact path's region within the fast path's");
     static_assert((THREADS & (THREADS - 1)) == 0, "power-of-two thread count");
     static constexpr int WMAX = 1 << (NW - 1);
     static constexpr int HL = WMAX / 2 > 1 ? WMAX / 2 : 1;
     static constexpr int N = THREADS * K;
-    static constexpr int TILE = (N - 2 * HL - WMAX) & ~3;  // (a multiple of 4: aligned copies)
-    static constexpr int NBEST = TILE + 2 * HL;
-    static constexpr int STEPS = NW / 2;                          // two-width steps
-    static constexpr int UMAX = STEPS > 0 ? 1 << (2 * (STEPS - 1)) : 1;  // widest chain stride
+    static constexpr int NE = THREADS * KE;
+    static constexpr int TILE = (N - WMAX + 1) & ~3;  // (a multiple of 4: aligned copies)
+    static constexpr int ETILE = (NE - 2 * HL - WMAX) & ~3;
+    static constexpr int NBEST = ETILE + 2 * HL;
+    static_assert(ETILE >= THREADS && TILE >= ETILE, "tile");
+    // The fast path's chain steps: step s reads B_u (u = 8^(s-1)) and forms up to three
+    // doublings (widths 2u, 4u, 8u); ND(s) of them, LA(s) = 2^ND - 1 chain elements of lookahead.
+    static constexpr int STEPS = (NW + 1) / 3;  // widths 2 .. 2^(NW-1) in steps of three
+    static constexpr int nd(int s) { return NW - 1 - 3 * (s - 1) < 3 ? NW - 1 - 3 * (s - 1) : 3; }
+    static constexpr int la(int s) { return (1 << nd(s)) - 1; }
+    static constexpr int UMAX = STEPS > 0 ? 1 << (3 * (STEPS - 1)) : 1;  // widest chain stride
     static_assert(UMAX <= THREADS, "a chain stride per residue class");
-    static_assert(TILE >= THREADS, "tile");
+    // zeros past N that the chains of steps 2.. read: u LA(s) floats
+    static constexpr int pad_sums()
+    {
+        int p = 0;
+        for (int s = 2; s <= STEPS; ++s) {
+            const int q = (1 << (3 * (s - 1))) * la(s);
+            p = q > p ? q : p;
+        }
+        return p;
+    }
     // the exact path: position pairs (2 tid + 2 THREADS q, +1)
-    static constexpr int PAIRS = (N + 2 * THREADS - 1) / (2 * THREADS);
+    static constexpr int PAIRS = (NE + 2 * THREADS - 1) / (2 * THREADS);
     // floats of each sum buffer: the exact path's pairs plus WMAX of partner reads past them,
-    // and the chains' reads up to 3 UMAX past N; even (8-byte aligned pairs)
+    // and the chains' reads past N; even (8-byte aligned pairs)
     static constexpr int BUF0 = PAIRS * 2 * THREADS + (WMAX < 2 ? 2 : WMAX);
-    static constexpr int BUF1 = N + 3 * UMAX + 4;
+    static constexpr int BUF1 = N + pad_sums();
     static constexpr int BUF = ((BUF0 > BUF1 ? BUF0 : BUF1) + 3) / 4 * 4;
-    static constexpr int NBF = N + 4;  // staged samples, 3 zeros of chain reads past them
+    static constexpr int NBF = N + 8;  // staged samples, 7 zeros of step 1's reads past them
     // shared memory of box_run: the staged samples, two sum buffers, the best SNR of NBEST
     // positions (exact path), 1 / (sigma sqrt(w)) per width (16 floats)
     static constexpr size_t SMEM = (size_t)NBF * 4 + (size_t)BUF * 8 + (size_t)NBEST * 4 + 64;
@@ -167,13 +187,14 @@ __device__ __forceinline__ float box_value(uint32_t raw)
         return (float)(int32_t)raw;
 }
 
-// One tile exactly (the width ladder with every position's best SNR and the range tests of an
-// edge tile, then the candidates): for tiles the fast path flags and for edge tiles.  The
-// samples are read from the series (zero outside it).  B0, B1: BUF floats each; best_s: NBEST.
-// Every thread of the group calls it.
+// Output samples [t0, t0 + cnt) (cnt <= ETILE) exactly: the width ladder with every
+// position's best SNR and the range tests of the series' ends, then the candidates; for the
+// tiles the fast path flags.  The samples are read from the series (zero outside it).  B0, B1:
+// BUF floats each; best_s: NBEST.  Every thread of the group calls it.
 template <typename T, int NW, int THREADS, int K, class Bar>
 __device__ __noinline__ void box_tile_exact(const T *__restrict__ r, long long n, long long t0,
-                                            float mu_f, float thr, const float *inv_w, int d,
+                                            int cnt, float mu_f, float thr, const float *inv_w,
+                                            int d,
                                             DevCand *__restrict__ cands,
                                             unsigned long long *__restrict__ count, long long cap,
                                             float *B0, float *B1, float *best_s, const Bar &bar,
@@ -266,7 +287,7 @@ __device__ __noinline__ void box_tile_exact(const T *__restrict__ r, long long n
     }
     bar.sync();
     if (active) {
-        for (int q = tid; q < G::TILE; q += THREADS) {
+        for (int q = tid; q < cnt; q += THREADS) {
             const long long t = t0 + q;
             if (t >= n) break;
             const int i = q + HL;
@@ -288,55 +309,68 @@ __device__ __noinline__ void box_tile_exact(const T *__restrict__ r, long long n
     }
 }
 
-// Asynchronous copy of tile `tile`'s region into NB by the group: 16-byte copies where the
-// region lies inside the series and starts 16-byte aligned, else 4-byte copies with zeros
-// outside the series.  Each thread waits for its own copies (cp_async_wait_all); a group
-// barrier then makes all of them visible.
+// Asynchronous copy of the fast path's region [t0, t0 + N) of tile `tile` into NB by the group:
+// 16-byte copies where the region lies inside the series and starts 16-byte aligned, else
+// 4-byte copies with zeros past the series.  Each thread waits for its own copies
+// (cp_async_wait_all); a group barrier then makes all of them visible.
 template <typename T, int NW, int THREADS, int K>
 __device__ __forceinline__ void box_stage(uint32_t *NB, const T *__restrict__ r, long long n,
                                           long long tile, int tid)
 {
     using G = BoxGeom<NW, THREADS, K>;
     static_assert(sizeof(T) == 4, "4-byte samples");
-    const long long r0 = tile * G::TILE - G::HL;
-    if (r0 >= 0 && r0 + G::N <= n && ((uintptr_t)(r + r0) & 15) == 0) {
+    const long long r0 = tile * G::TILE;
+    if (r0 + G::N <= n && ((uintptr_t)(r + r0) & 15) == 0) {
         const T *base = r + r0;
         for (int q = tid; q < G::N / 4; q += THREADS) cp_async16(NB + 4 * q, base + 4 * q);
     } else {
         for (int i = tid; i < G::N; i += THREADS) {
             const long long t = r0 + i;
-            const bool in = t >= 0 && t < n;
+            const bool in = t < n;
             cp_async4(NB + i, in ? r + t : r, in ? 4u : 0u);
         }
     }
     cp_async_commit();
 }
 
+// m = max(m, c[0], .., c[K - 1]) in three-input maxima.
+template <int K>
+__device__ __forceinline__ void box_fold(float &m, const float *c)
+{
+#pragma unroll
+    for (int j = 0; j + 1 < K; j += 2) m = fmax3(m, c[j], c[j + 1]);
+    if (K & 1) m = fmaxf(m, c[K - 1]);
+}
+
 // Tiles [tile_lo, tile_hi) of row r (n samples, DM index d) with the row's mean and sigma
 // (sigma > 0), searched by the calling group: `active` threads with group index tid in
 // [0, THREADS) (every thread of the group's barrier calls it); sm holds
-// BoxGeom<NW, THREADS, K>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr)
+// BoxGeom<NW, THREADS, K, KE>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr)
 // go to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight; the caller
 // synchronises the group before sm is written again.
 //
-// Fast path (tiles inside the series): only whether any position < NBEST reaches the
-// threshold at any width is needed, so no position keeps a best SNR.  Step s (chain stride
-// u = 4^(s-1)) gives each thread the residue class r = tid mod u, block b = tid / u: the K
-// positions p_j = r + u (K b + j) and, from the previous step's buffer, B_u at p_j for
-// j < K + 3; it forms B_2u (K + 2 of them) and B_4u = B_2u[j] + B_2u[j + 2] (the same operands
-// and order as the exact path), keeps the maximum SNR of both widths, and stores B_4u at p_j
-// for the next step.  Reads and stores are conflict-free (K odd) and cost about half the
-// shared-memory traffic of the exact path's pairs.  A tile whose maximum reaches the
-// threshold (positions past NBEST may flag it too; they hold real or zero samples) is then
-// searched exactly.
-template <typename T, int NW, int THREADS, int K, class Bar>
+// Fast path (every tile): only whether a boxcar that starts in the tile reaches the threshold
+// at some width is needed, so no position keeps a best SNR.  Step s (chain stride u = 8^(s-1))
+// gives each thread the residue class tid mod u, block b = tid / u: the K positions
+// p_j = (tid mod u) + u (K b + j) and, from the previous step's buffer (the staged samples for
+// s = 1), B_u at p_j for j < K + LA(s).  In registers it forms up to three doublings over the
+// chain, B_2u[j] = B_u[j] + B_u[j + 1], B_4u[j] = B_2u[j] + B_2u[j + 2] and
+// B_8u[j] = B_4u[j] + B_4u[j + 4] (the exact path's operands and order), keeps the largest sum
+// of each width over its K positions and stores the last for the next step.  Reads and stores
+// are conflict-free (K odd).  The SNR (v - w mu) / (sigma sqrt w), rounded as the exact path
+// rounds it, does not decrease with v, so the largest SNR of a width is the SNR of its largest
+// sum.  Positions whose boxcars reach past the region (or past the series, staged as zeros)
+// take part too: their sums hold real samples and zeros, and a tile they flag is only searched
+// exactly, where the range tests apply.  A flagged tile is searched exactly in parts of ETILE
+// output samples.
+template <typename T, int NW, int THREADS, int K, int KE = K, class Bar = BoxBarCta>
 __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, long long tile_lo,
                                         long long tile_hi, double mu, double sig, double threshold,
                                         int d, DevCand *__restrict__ cands,
                                         unsigned long long *__restrict__ count, long long cap,
                                         unsigned char *sm, const Bar &bar, int tid_in, bool active)
 {
-    using G = BoxGeom<NW, THREADS, K>;
+    using G = BoxGeom<NW, THREADS, K, KE>;
     constexpr int N = G::N;
     uint32_t *NB = reinterpret_cast<uint32_t *>(sm);  // staged samples of the current tile
     float *A = reinterpret_cast<float *>(NB + G::NBF);
@@ -349,90 +383,61 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
     if (active && tid < NW)
         inv_w[tid] = __double2float_rn(__ddiv_rn(1.0, __dmul_rn(sig, __dsqrt_rn((double)(1 << tid)))));
-    // zeros past the region: the chains read up to 3 positions past NB and 3 UMAX past N
+    // zeros past the region: the chains read up to 7 positions past NB and LA u past N
     auto zero_pads = [&]() {
         if (!active) return;
         for (int i = N + tid; i < G::BUF; i += THREADS) A[i] = Bf[i] = 0.f;
         if (tid < G::NBF - N) NB[N + tid] = 0u;
     };
     zero_pads();
-    auto inside = [&](long long tile) {
-        const long long r0 = tile * G::TILE - G::HL;
-        return r0 >= 0 && r0 + N <= n;
-    };
     // SNR at width 2^l of sums v
     auto snr = [&](float v, int l) {
         const float wm = __fmul_rn((float)(1 << l), mu_f);
         return __fmul_rn(__fadd_rn(v, -wm), inv_w[l]);
     };
-    if (active && inside(tile_lo)) box_stage<T, NW, THREADS, K>(NB, r, n, tile_lo, tid);
+    if (active) box_stage<T, NW, THREADS, K>(NB, r, n, tile_lo, tid);
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
         const long long t0 = tile * G::TILE;
-        if (!inside(tile)) {  // (uniform) edge tile: exactly, from the series
-            bar.sync();       // (inv_w and the pads written; the previous tile's reads done)
-            box_tile_exact<T, NW, THREADS, K>(r, n, t0, mu_f, thr, inv_w, d, cands, count, cap,
-                                              A, Bf, best_s, bar, tid, active);
-            bar.sync();
-            zero_pads();
-            if (active && tile + 1 < tile_hi && inside(tile + 1))
-                box_stage<T, NW, THREADS, K>(NB, r, n, tile + 1, tid);
-            continue;
-        }
         if (active) cp_async_wait_all();
         bar.sync();  // the tile's samples (every thread's copies), inv_w and the pads visible
-        // The SNR (v - w mu) / (sigma sqrt w), rounded as the exact path rounds it, does not
-        // decrease with v: the largest SNR of a width is the SNR of its largest sum, so a thread
-        // keeps only the largest sum of each width and forms NW SNRs at the tile's end.
         float M[NW];
 #pragma unroll
         for (int l = 0; l < NW; ++l) M[l] = -INFINITY;
         bool staged = false;  // the next tile's copies issued
         auto stage_next = [&]() {
-            if (active && tile + 1 < tile_hi && inside(tile + 1))
-                box_stage<T, NW, THREADS, K>(NB, r, n, tile + 1, tid);
+            if (active && tile + 1 < tile_hi) box_stage<T, NW, THREADS, K>(NB, r, n, tile + 1, tid);
             staged = true;
         };
-        constexpr int S = G::STEPS > 0 ? G::STEPS : 1;  // (NW = 1: width 1 alone)
+        if (G::STEPS == 0 && active) {  // width 1 alone
+            float c[K];
 #pragma unroll
-        for (int s = 1; s <= S; ++s) {
-            const int u = 1 << (2 * s - 2);
-            const bool two = 2 * s < NW;       // widths 2u and 4u (else 2u alone)
-            const bool more = 2 * s + 1 < NW;  // a further step reads B_4u
+            for (int j = 0; j < K; ++j) c[j] = box_value<T>(NB[K * tid + j]);
+            box_fold<K>(M[0], c);
+        }
+#pragma unroll
+        for (int s = 1; s <= G::STEPS; ++s) {
+            const int u = 1 << (3 * (s - 1));
+            const int nd = G::nd(s), la = G::la(s);
+            const bool more = s < G::STEPS;  // a further step reads B_8u
             const int p0 = (tid & (u - 1)) + u * K * (tid / u);  // chain element 0
             if (active) {
-                // B_u of chain element j (the staged samples for s = 1)
-                auto ld = [&](int j) {
-                    return s == 1 ? box_value<T>(NB[p0 + j]) : ((s & 1) ? Bf : A)[p0 + u * j];
-                };
-                float *nxt = (s & 1) ? A : Bf;
-                // a window over the chain: B_u at j .. j + 3 and B_2u at j .. j + 2; two chain
-                // elements per round (their maxima in one three-input max each)
-                float c0 = ld(0), c1 = ld(1), c2 = ld(2);
-                float w0 = __fadd_rn(c0, c1), w1 = __fadd_rn(c1, c2);
+                float c[K + 7];
+                const float *src = (s & 1) ? Bf : A;
 #pragma unroll
-                for (int j = 0; j < K; j += 2) {
-                    const bool pair = j + 1 < K;
-                    const float c3 = ld(j + 3), c4 = pair ? ld(j + 4) : 0.f;
-                    const float w2 = __fadd_rn(c2, c3), w3 = pair ? __fadd_rn(c3, c4) : 0.f;
-                    if (s == 1) M[0] = pair ? fmax3(M[0], c0, c1) : fmaxf(M[0], c0);
-                    float o0 = w0, o1 = w1;
-                    if (NW > 1) {
-                        M[2 * s - 1] = pair ? fmax3(M[2 * s - 1], w0, w1) : fmaxf(M[2 * s - 1], w0);
-                        if (two) {
-                            o0 = __fadd_rn(w0, w2);
-                            o1 = pair ? __fadd_rn(w1, w3) : 0.f;
-                            M[2 * s] = pair ? fmax3(M[2 * s], o0, o1) : fmaxf(M[2 * s], o0);
-                        }
-                        if (more) {
-                            nxt[p0 + u * j] = o0;
-                            if (pair) nxt[p0 + u * (j + 1)] = o1;
-                        }
-                    }
-                    c0 = c2;
-                    c1 = c3;
-                    c2 = c4;
-                    w0 = w2;
-                    w1 = w3;
+                for (int j = 0; j < K + la; ++j)
+                    c[j] = s == 1 ? box_value<T>(NB[p0 + j]) : src[p0 + u * j];
+                if (s == 1) box_fold<K>(M[0], c);
+#pragma unroll
+                for (int e = 1; e <= nd; ++e) {  // c[j] = B_{2^e u}[j], j < K + la + 1 - 2^e
+                    const int h = 1 << (e - 1);
+#pragma unroll
+                    for (int j = 0; j < K + la + 1 - 2 * h; ++j) c[j] = __fadd_rn(c[j], c[j + h]);
+                    box_fold<K>(M[3 * (s - 1) + e], c);
+                }
+                if (more) {
+                    float *nxt = (s & 1) ? A : Bf;
+#pragma unroll
+                    for (int j = 0; j < K; ++j) nxt[p0 + u * j] = c[j];
                 }
             }
             if (more) {
@@ -448,8 +453,13 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
         const bool flagged = bar.any(hit);
         if (!staged) stage_next();
         if (flagged) {
-            box_tile_exact<T, NW, THREADS, K>(r, n, t0, mu_f, thr, inv_w, d, cands, count, cap,
-                                              A, Bf, best_s, bar, tid, active);
+            // (every thread is past the fast path's reads of the sum buffers)
+            for (int a = 0; a < G::TILE && t0 + a < n; a += G::ETILE) {
+                if (a > 0) bar.sync();  // the previous part's candidate reads done
+                box_tile_exact<T, NW, THREADS, KE>(r, n, t0 + a, min(G::ETILE, G::TILE - a),
+                                                  mu_f, thr, inv_w, d, cands, count, cap, A,
+                                                  Bf, best_s, bar, tid, active);
+            }
             bar.sync();
             zero_pads();
         }

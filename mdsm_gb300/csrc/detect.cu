@@ -602,7 +602,8 @@ mdsm_status series_stats_launch(const void *y, int dtype, int ndms, long long n,
 }
 
 constexpr int kBoxThreads = 256;
-constexpr int kBoxK = 11;  // positions per thread (tiles of 2816 - 2 HL - WMAX samples)
+constexpr int kBoxK = 15;   // positions per thread (tiles of 3840 - WMAX + 1 samples, rounded)
+constexpr int kBoxKE = 7;   // the exact path's positions per thread (its region 1792 samples)
 
 // One CTA per (DM, run of `tpc` consecutive tiles): the tile loop of box.cuh.
 template <typename T, int NW>
@@ -615,11 +616,11 @@ __global__ void __launch_bounds__(kBoxThreads, 4)
     const int d = blockIdx.y;
     const double mu = musig[d].x, sig = musig[d].y;
     if (!(sig > 0.0)) return;
-    constexpr int TILE = BoxGeom<NW, kBoxThreads, kBoxK>::TILE;
+    constexpr int TILE = BoxGeom<NW, kBoxThreads, kBoxK, kBoxKE>::TILE;
     const long long ntiles = (n + TILE - 1) / TILE;
     const long long tile_lo = (long long)blockIdx.x * tpc;
     const long long tile_hi = tile_lo + tpc < ntiles ? tile_lo + tpc : ntiles;
-    box_run<T, NW, kBoxThreads, kBoxK>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold,
+    box_run<T, NW, kBoxThreads, kBoxK, kBoxKE>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold,
                                        d, cands, count, cap, sm, BoxBarCta{}, (int)threadIdx.x,
                                        true);
 }
@@ -635,7 +636,7 @@ static cudaError_t launch_boxcar(const T *y, int ndms, long long n, int nw, doub
 template <int NW>
 static size_t boxcar_smem()
 {
-    return BoxGeom<NW, kBoxThreads, kBoxK>::SMEM;
+    return BoxGeom<NW, kBoxThreads, kBoxK, kBoxKE>::SMEM;
 }
 
 template <typename T, int NW>
@@ -648,10 +649,12 @@ static cudaError_t launch_boxcar_nw(const T *y, int ndms, long long n, double th
                                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     // runs of up to 8 tiles per CTA while that leaves >= 8192 CTAs (several waves of 4 per SM)
-    constexpr int TILE = BoxGeom<NW, kBoxThreads, kBoxK>::TILE;
+    constexpr int TILE = BoxGeom<NW, kBoxThreads, kBoxK, kBoxKE>::TILE;
     const long long ntiles = (n + TILE - 1) / TILE;
     int tpc = (int)std::min<long long>(8, std::max<long long>(1, ntiles * ndms / 8192));
     tpc = (int)std::min<long long>(tpc, ntiles);
+    const long long runs = (ntiles + tpc - 1) / tpc;
+    tpc = (int)((ntiles + runs - 1) / runs);  // the same number of runs, evened out
     dim3 g3((unsigned)((ntiles + tpc - 1) / tpc), (unsigned)ndms);
     k_boxcar<T, NW><<<g3, kBoxThreads, smem, st>>>(y, n, tpc, threshold, musig, cands, count, cap);
     return cudaGetLastError();

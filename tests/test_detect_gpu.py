@@ -52,7 +52,8 @@ def test_ref_detector_on_dedispersed_block(lib, orc, cuda):
 @pytest.mark.parametrize("dtype,nw,n", [("i32", 9, 9000), ("f32", 9, 9000), ("i32", 1, 4097),
                                         ("f32", 2, 2049), ("i32", 5, 301), ("i32", 9, 12289)])
 def test_boxcar_matches_oracle(lib, orc, cuda, dtype, nw, n):
-    """Interior tiles (no bounds tests) and edge tiles, 1 to 9 widths, odd lengths."""
+    """Tiles inside the rows (16-byte copies) and the last tile of each row (staged with zeros
+    past the row), 1 to 9 widths, odd lengths."""
     import mdsm_gb300 as m
     torch = cuda
     rng = np.random.default_rng(12 + nw + n)
@@ -77,20 +78,25 @@ def test_boxcar_matches_oracle(lib, orc, cuda, dtype, nw, n):
     assert np.array_equal(cands["snr"], snr)
 
 
-@pytest.mark.parametrize("dtype,nw,thr", [("i32", 1, 6.0), ("f32", 3, 6.0), ("i32", 4, 6.0),
-                                          ("f32", 6, 6.0), ("i32", 8, 6.0), ("f32", 9, 3.5)])
-def test_boxcar_fast_path_and_tile_boundaries(lib, orc, cuda, dtype, nw, thr):
-    """Rows long enough for interior tiles at every width count (the chain fast path), with
-    pulses on both sides of interior tile boundaries (output tiles of 2816 - 2 HL - WMAX
-    samples, rounded down to a multiple of 4) and, at a 3.5 sigma threshold, most tiles flagged
-    for the exact search."""
+@pytest.mark.parametrize("dtype,nw,thr,tail", [("i32", 1, 6.0, 777), ("f32", 3, 6.0, 776),
+                                               ("i32", 4, 6.0, 777), ("f32", 6, 6.0, 776),
+                                               ("i32", 8, 6.0, 777), ("f32", 9, 3.5, 777),
+                                               ("i32", 9, 6.0, 776)])
+def test_boxcar_fast_path_and_tile_boundaries(lib, orc, cuda, dtype, nw, thr, tail):
+    """Rows long enough for several tiles at every width count, with pulses on both sides of
+    the tile boundaries (tiles of 3840 - WMAX + 1 samples, rounded down to a multiple of 4: a
+    staged region of 256 threads x 15) and of the exact search's part boundaries inside a tile
+    (parts of 1792 - 2 HL - WMAX samples, rounded the same way: 256 x 7); rows of 16-byte
+    multiples (tail 776) and not (777, staged in 4-byte copies); at a 3.5 sigma threshold most
+    tiles are flagged for the exact search."""
     import mdsm_gb300 as m
     torch = cuda
     wmax = 1 << (nw - 1)
     hl = max(wmax // 2, 1)
-    tile = (2816 - 2 * hl - wmax) & ~3
-    n = 6 * tile + 777
-    rng = np.random.default_rng(70 + nw)
+    tile = (3840 - wmax + 1) & ~3
+    part = (1792 - 2 * hl - wmax) & ~3
+    n = 6 * tile + tail
+    rng = np.random.default_rng(70 + nw + tail)
     ndms = 16
     if dtype == "i32":
         y = rng.integers(-3000, 3000, (ndms, n)).astype(np.int32)
@@ -101,9 +107,10 @@ def test_boxcar_fast_path_and_tile_boundaries(lib, orc, cuda, dtype, nw, thr):
     for k in range(1, 6):
         for j, off in enumerate((-hl - 1, -1, 0, 1, hl)):
             row = (3 * k + j) % ndms
-            t = k * tile + off
             w = min(1 << ((k + j) % nw), 64)
-            y[row, t:t + w] += amp[(k + j) % 3]
+            for t in (k * tile + off, (k - 1) * tile + part + off, (k - 1) * tile + 2 * part + off):
+                if 0 <= t and t + w <= n:
+                    y[row, t:t + w] += amp[(k + j) % 3]
     cands, cnt = m.boxcar_detect_device(torch.from_numpy(y).cuda(), nwidths=nw, threshold=thr,
                                         cap=1 << 20)
     dm, samp, wid, snr = orc.boxcar_detect(y, nw, thr)

@@ -638,6 +638,8 @@ mdsm_status mdsm_batch_candidates(mdsm_batch *b, int beam, mdsm_candidate *out, 
         return fail(MDSM_EINVAL, "batch: detection not enabled or bad beam");
     MDSM_CUDA_TRY(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
     const long long n = *b->h_count[beam];
+    if ((unsigned long long)n & kBoxCountLate)
+        return fail(MDSM_ETIMEOUT, "batch: a staging wait of the search ran out");
     const long long got = std::min<long long>(std::min<long long>(n, b->cap), cap);
     std::vector<mdsm_candidate> tmp(b->h_cands[beam], b->h_cands[beam] + std::min(n, b->cap));
     devcand_to_candidate(tmp.data(), (long long)tmp.size());

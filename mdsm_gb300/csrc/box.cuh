@@ -89,6 +89,7 @@ struct BoxGeom {
     // The fast path's chain steps: step s reads B_u (u = 8^(s-1)) and forms up to three
     // doublings (widths 2u, 4u, 8u); ND(s) of them, LA(s) = 2^ND - 1 chain elements of lookahead.
     static constexpr int STEPS = (NW + 1) / 3;  // widths 2 .. 2^(NW-1) in steps of three
+    static_assert(STEPS <= 3, "three chain steps at most");
     static constexpr int nd(int s) { return NW - 1 - 3 * (s - 1) < 3 ? NW - 1 - 3 * (s - 1) : 3; }
     static constexpr int la(int s) { return (1 << nd(s)) - 1; }
     static constexpr int UMAX = STEPS > 0 ? 1 << (3 * (STEPS - 1)) : 1;  // widest chain stride
@@ -112,8 +113,9 @@ struct BoxGeom {
     static constexpr int BUF = ((BUF0 > BUF1 ? BUF0 : BUF1) + 3) / 4 * 4;
     static constexpr int NBF = N + 8;  // staged samples, 7 zeros of step 1's reads past them
     // shared memory of box_run: the staged samples, two sum buffers, the best SNR of NBEST
-    // positions (exact path), 1 / (sigma sqrt(w)) per width (16 floats)
-    static constexpr size_t SMEM = (size_t)NBF * 4 + (size_t)BUF * 8 + (size_t)NBEST * 4 + 64;
+    // positions (exact path), 1 / (sigma sqrt(w)) per width (16 floats), the bulk-copy
+    // mbarrier (16 bytes)
+    static constexpr size_t SMEM = (size_t)NBF * 4 + (size_t)BUF * 8 + (size_t)NBEST * 4 + 80;
     static_assert(NBEST % 2 == 0 && NBF % 4 == 0, "alignment");
 };
 
@@ -342,12 +344,74 @@ __device__ __forceinline__ void box_fold(float &m, const float *c)
     if (K & 1) m = fmaxf(m, c[K - 1]);
 }
 
+// c[j] = c[j] + c[j + H] for j < CNT, in place in ascending j (the partners are not yet
+// updated); for H >= 2 the operand pairs (j, j + 1) and (j + H, j + H + 1) are register pairs,
+// added in FP32x2.
+template <int CNT, int H>
+__device__ __forceinline__ void box_double(float *c)
+{
+    if constexpr (H == 1) {
+#pragma unroll
+        for (int j = 0; j < CNT; ++j) c[j] = __fadd_rn(c[j], c[j + 1]);
+    } else {
+#pragma unroll
+        for (int j = 0; j + 1 < CNT; j += 2) {
+            const float2 v = add_f2(make_float2(c[j], c[j + 1]), make_float2(c[j + H], c[j + H + 1]));
+            c[j] = v.x;
+            c[j + 1] = v.y;
+        }
+        if constexpr ((CNT & 1) != 0) c[CNT - 1] = __fadd_rn(c[CNT - 1], c[CNT - 1 + H]);
+    }
+}
+
+// Step S of the fast path's chains for one thread (see box_run): B_u (u = 8^(S-1)) of its chain
+// and LA(S) further chain elements from the staged samples (S = 1) or the previous step's
+// buffer, ND(S) doublings in registers with the largest sum of each width folded into M, and
+// the last doubling stored for the next step.
+template <typename T, int NW, int THREADS, int K, int S>
+__device__ __forceinline__ void box_chain_step(const uint32_t *NB, float *A, float *Bf, float *M,
+                                               int tid)
+{
+    using G = BoxGeom<NW, THREADS, K>;
+    constexpr int u = 1 << (3 * (S - 1)), nd = G::nd(S), la = G::la(S);
+    const int p0 = (tid & (u - 1)) + u * K * (tid / u);  // chain element 0
+    float c[K + la];
+    const float *src = (S & 1) ? Bf : A;
+#pragma unroll
+    for (int j = 0; j < K + la; ++j) c[j] = S == 1 ? box_value<T>(NB[p0 + j]) : src[p0 + u * j];
+    if constexpr (S == 1) box_fold<K>(M[0], c);
+    // c[j] = B_{2^e u}[j] for j < K + la + 1 - 2^e after doubling e
+    if constexpr (nd >= 1) {
+        box_double<K + la - 1, 1>(c);
+        box_fold<K>(M[3 * (S - 1) + 1], c);
+    }
+    if constexpr (nd >= 2) {
+        box_double<K + la - 3, 2>(c);
+        box_fold<K>(M[3 * (S - 1) + 2], c);
+    }
+    if constexpr (nd >= 3) {
+        box_double<K + la - 7, 4>(c);
+        box_fold<K>(M[3 * (S - 1) + 3], c);
+    }
+    if constexpr (S < G::STEPS) {  // a further step reads B_8u
+        float *nxt = (S & 1) ? A : Bf;
+#pragma unroll
+        for (int j = 0; j < K; ++j) nxt[p0 + u * j] = c[j];
+    }
+}
+
 // Tiles [tile_lo, tile_hi) of row r (n samples, DM index d) with the row's mean and sigma
 // (sigma > 0), searched by the calling group: `active` threads with group index tid in
 // [0, THREADS) (every thread of the group's barrier calls it); sm holds
 // BoxGeom<NW, THREADS, K, KE>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr)
 // go to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight; the caller
 // synchronises the group before sm is written again.
+//
+// Staging (kBulk): a tile whose region lies inside the series and starts 16-byte aligned
+// arrives by one bulk copy (cp.async.bulk, issued by the group's thread 0 on an mbarrier in
+// sm), and every thread waits on the mbarrier's phase, bounded, instead of at a group barrier;
+// a wait that runs out sets kBoxCountLate in *count and the search goes on (its results are
+// then void).  Other tiles, and every tile without kBulk, arrive by per-thread cp.async.
 //
 // Fast path (every tile): only whether a boxcar that starts in the tile reaches the threshold
 // at some width is needed, so no position keeps a best SNR.  Step s (chain stride u = 8^(s-1))
@@ -363,7 +427,8 @@ __device__ __forceinline__ void box_fold(float &m, const float *c)
 // take part too: their sums hold real samples and zeros, and a tile they flag is only searched
 // exactly, where the range tests apply.  A flagged tile is searched exactly in parts of ETILE
 // output samples.
-template <typename T, int NW, int THREADS, int K, int KE = K, class Bar = BoxBarCta>
+template <typename T, int NW, int THREADS, int K, int KE = K, bool kBulk = false,
+          class Bar = BoxBarCta>
 __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, long long tile_lo,
                                         long long tile_hi, double mu, double sig, double threshold,
                                         int d, DevCand *__restrict__ cands,
@@ -377,7 +442,12 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
     float *Bf = A + G::BUF;
     float *best_s = Bf + G::BUF;
     float *inv_w = best_s + G::NBEST;
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(inv_w + 16);
     const int tid = tid_in & (THREADS - 1);
+    if (kBulk && active && tid == 0) {
+        mbar_init(mbar, 1);
+        fence_mbar_init();
+    }
     const float mu_f = __double2float_rn(mu);
     const float thr = __double2float_rn(threshold);
     // 1 / (sigma sqrt(w)) in FP64, rounded to FP32, once per width (FP64 is a slow pipe here)
@@ -395,17 +465,48 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
         const float wm = __fmul_rn((float)(1 << l), mu_f);
         return __fmul_rn(__fadd_rn(v, -wm), inv_w[l]);
     };
-    if (active) box_stage<T, NW, THREADS, K>(NB, r, n, tile_lo, tid);
+    // whether tile `tile` arrives by one bulk copy (uniform across the group)
+    auto bulk = [&](long long tile) {
+        const long long r0 = tile * G::TILE;
+        return kBulk && r0 + N <= n && ((uintptr_t)(r + r0) & 15) == 0;
+    };
+    auto stage = [&](long long tile) {
+        if (!active) return;
+        if (bulk(tile)) {
+            if (tid == 0) {
+                fence_proxy_async_smem();  // (after the group's reads of NB, at a barrier)
+                mbar_arrive_expect_tx(mbar, (uint32_t)N * 4u);
+                bulk_g2s(NB, r + tile * G::TILE, (uint32_t)N * 4u, mbar);
+            }
+        } else {
+            box_stage<T, NW, THREADS, K>(NB, r, n, tile, tid);
+        }
+    };
+    uint32_t parity = 0;  // of the next bulk-copied tile's phase
+    bool late = false;    // a bulk-copy wait of this thread ran out
+    if (kBulk) bar.sync();  // the mbarrier initialised (before any thread waits on it)
+    stage(tile_lo);
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
         const long long t0 = tile * G::TILE;
-        if (active) cp_async_wait_all();
-        bar.sync();  // the tile's samples (every thread's copies), inv_w and the pads visible
+        if (bulk(tile)) {
+            // the bulk copy's bytes are visible to each thread that sees the phase complete;
+            // inv_w is visible since the barrier before the loop; every thread is past the
+            // previous tile's reads of the sum buffers (its last barrier)
+            if (active && !mbar_wait_bounded(mbar, parity, nullptr, 0)) {
+                late = true;
+                atomicOr(count, kBoxCountLate);
+            }
+            parity ^= 1u;
+        } else {
+            if (active) cp_async_wait_all();
+            bar.sync();  // the tile's samples (every thread's copies), inv_w and the pads visible
+        }
         float M[NW];
 #pragma unroll
         for (int l = 0; l < NW; ++l) M[l] = -INFINITY;
         bool staged = false;  // the next tile's copies issued
         auto stage_next = [&]() {
-            if (active && tile + 1 < tile_hi) box_stage<T, NW, THREADS, K>(NB, r, n, tile + 1, tid);
+            if (tile + 1 < tile_hi) stage(tile + 1);
             staged = true;
         };
         if (G::STEPS == 0 && active) {  // width 1 alone
@@ -414,35 +515,16 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
             for (int j = 0; j < K; ++j) c[j] = box_value<T>(NB[K * tid + j]);
             box_fold<K>(M[0], c);
         }
-#pragma unroll
-        for (int s = 1; s <= G::STEPS; ++s) {
-            const int u = 1 << (3 * (s - 1));
-            const int nd = G::nd(s), la = G::la(s);
-            const bool more = s < G::STEPS;  // a further step reads B_8u
-            const int p0 = (tid & (u - 1)) + u * K * (tid / u);  // chain element 0
-            if (active) {
-                float c[K + 7];
-                const float *src = (s & 1) ? Bf : A;
-#pragma unroll
-                for (int j = 0; j < K + la; ++j)
-                    c[j] = s == 1 ? box_value<T>(NB[p0 + j]) : src[p0 + u * j];
-                if (s == 1) box_fold<K>(M[0], c);
-#pragma unroll
-                for (int e = 1; e <= nd; ++e) {  // c[j] = B_{2^e u}[j], j < K + la + 1 - 2^e
-                    const int h = 1 << (e - 1);
-#pragma unroll
-                    for (int j = 0; j < K + la + 1 - 2 * h; ++j) c[j] = __fadd_rn(c[j], c[j + h]);
-                    box_fold<K>(M[3 * (s - 1) + e], c);
-                }
-                if (more) {
-                    float *nxt = (s & 1) ? A : Bf;
-#pragma unroll
-                    for (int j = 0; j < K; ++j) nxt[p0 + u * j] = c[j];
-                }
-            }
-            if (more) {
+        if constexpr (G::STEPS >= 1) {
+            if (active) box_chain_step<T, NW, THREADS, K, 1>(NB, A, Bf, M, tid);
+            if constexpr (G::STEPS >= 2) {
                 bar.sync();
-                if (s == 1) stage_next();  // the samples are read: copies overlap the search
+                stage_next();  // the samples are read: copies overlap the search
+                if (active) box_chain_step<T, NW, THREADS, K, 2>(NB, A, Bf, M, tid);
+                if constexpr (G::STEPS >= 3) {
+                    bar.sync();
+                    if (active) box_chain_step<T, NW, THREADS, K, 3>(NB, A, Bf, M, tid);
+                }
             }
         }
         bool hit = false;
@@ -461,10 +543,12 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
                                                   Bf, best_s, bar, tid, active);
             }
             bar.sync();
-            zero_pads();
+            zero_pads();  // (visible to the chains' reads past the next tile's first barrier)
         }
     }
     if (active) cp_async_wait_all();
+    // a copy whose wait ran out may still be in flight: one more bounded wait for the last
+    if (kBulk && late && tid == 0) mbar_wait_bounded(mbar, parity ^ 1u, nullptr, 0);
 }
 
 }  // namespace mdsm

@@ -154,6 +154,7 @@ static mdsm_status fetch_cands(DevCand *d_c, unsigned long long *d_count, long l
     unsigned long long n = 0;
     MDSM_CUDA_TRY(cudaMemcpyAsync(&n, d_count, sizeof(n), cudaMemcpyDeviceToHost, st));
     MDSM_CUDA_TRY(cudaStreamSynchronize(st));
+    if (n & kBoxCountLate) return fail(MDSM_ETIMEOUT, "boxcar detector: a staging wait ran out");
     *ncand = (long long)n;
     const long long got = std::min<long long>((long long)n, cap);
     if (got > 0 && h) {
@@ -620,9 +621,9 @@ __global__ void __launch_bounds__(kBoxThreads, 4)
     const long long ntiles = (n + TILE - 1) / TILE;
     const long long tile_lo = (long long)blockIdx.x * tpc;
     const long long tile_hi = tile_lo + tpc < ntiles ? tile_lo + tpc : ntiles;
-    box_run<T, NW, kBoxThreads, kBoxK, kBoxKE>(y + (size_t)d * n, n, tile_lo, tile_hi, mu, sig, threshold,
-                                       d, cands, count, cap, sm, BoxBarCta{}, (int)threadIdx.x,
-                                       true);
+    box_run<T, NW, kBoxThreads, kBoxK, kBoxKE, true>(y + (size_t)d * n, n, tile_lo, tile_hi, mu,
+                                                     sig, threshold, d, cands, count, cap, sm,
+                                                     BoxBarCta{}, (int)threadIdx.x, true);
 }
 
 // The boxcar search of every DM row, for 1..9 widths (a template per width count).

@@ -40,6 +40,10 @@ enum : unsigned {
 
 size_t dtype_size(int dtype);
 
+// Set in the candidate count of the boxcar search (k_boxcar) when one of its bounded staging
+// waits ran out: the count and records of that search are not valid.
+constexpr unsigned long long kBoxCountLate = 1ull << 62;
+
 // candidate record as the device kernels write it
 struct DevCand {
     int32_t dm_idx, sample, width;

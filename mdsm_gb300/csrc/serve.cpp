@@ -216,6 +216,10 @@ void Server::harvest(Slot &s)
     r.done_time = now_s();
     r.ncand = *s.h_count;
     r.status = MDSM_OK;
+    if ((unsigned long long)r.ncand & kBoxCountLate) {  // the search's staging wait ran out
+        r.status = MDSM_ETIMEOUT;
+        r.ncand = 0;
+    }
     const long long got = std::max<long long>(0, std::min<long long>(r.ncand, desc.cand_cap));
     devcand_to_candidate(s.h_cands, got);
     std::vector<mdsm_candidate> c(s.h_cands, s.h_cands + got);

@@ -275,7 +275,9 @@ mdsm_status mdsm_ref_detect_subband_device(const mdsm_plan *plan, const float *d
  * 1,2,4..2^(nwidths-1); per-DM mean/sigma in FP64; boxcar sums and SNR = (sum - w*mean) /
  * (sigma*sqrt(w)) in FP32, explicitly rounded in a fixed order; per-sample
  * best width; non-maximum suppression with radius max(w/2,1).  d_series is [ndms][nsamp] of
- * dtype MDSM_OUT_F32 or MDSM_OUT_I32.  Candidates sorted by dm then sample. */
+ * dtype MDSM_OUT_F32 or MDSM_OUT_I32.  Candidates sorted by dm then sample.  MDSM_ETIMEOUT if
+ * a bounded wait for the search's staging copies ran out (no candidates are then returned; the
+ * same status reaches a serving block's result and mdsm_batch_candidates). */
 mdsm_status mdsm_boxcar_detect_device(const void *d_series, int series_dtype, int ndms,
                                       int nsamp, int nwidths, double threshold,
                                       mdsm_candidate *h_cands, long long cap, long long *ncand,

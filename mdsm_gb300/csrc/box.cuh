@@ -404,8 +404,8 @@ __device__ __forceinline__ void box_chain_step(const uint32_t *NB, float *A, flo
 // (sigma > 0), searched by the calling group: `active` threads with group index tid in
 // [0, THREADS) (every thread of the group's barrier calls it); sm holds
 // BoxGeom<NW, THREADS, K, KE>::SMEM bytes of the group's own.  Candidates (d, sample, width, snr)
-// go to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight; the caller
-// synchronises the group before sm is written again.
+// go to cands[atomicAdd(count)] below cap.  When it returns, no copy is in flight and no
+// mbarrier lives in sm; the caller synchronises the group before sm is written again.
 //
 // Staging (kBulk): a tile whose region lies inside the series and starts 16-byte aligned
 // arrives by one bulk copy (cp.async.bulk, issued by the group's thread 0 on an mbarrier in
@@ -547,8 +547,11 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
         }
     }
     if (active) cp_async_wait_all();
-    // a copy whose wait ran out may still be in flight: one more bounded wait for the last
-    if (kBulk && late && tid == 0) mbar_wait_bounded(mbar, parity ^ 1u, nullptr, 0);
+    if (kBulk && active && tid == 0) {
+        // a copy whose wait ran out may still be in flight: one more bounded wait for the last
+        if (late) mbar_wait_bounded(mbar, parity ^ 1u, nullptr, 0);
+        mbar_inval(mbar);  // (every thread's waits are behind the last group barrier)
+    }
 }
 
 }  // namespace mdsm

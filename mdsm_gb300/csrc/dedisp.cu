@@ -999,9 +999,7 @@ __global__ void __launch_bounds__(Cfg::THREADS, 1)
     __syncthreads();
     if (tid == 0) {  // the barriers' memory is used for other data from here on
         uint64_t *bars = reinterpret_cast<uint64_t *>(smem);
-        for (int k = 0; k < kPNR; ++k)
-            asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(&bars[k]))
-                         : "memory");
+        for (int k = 0; k < kPNR; ++k) mbar_inval(&bars[k]);
     }
 
     // ---- phase 4: boxcar search, one run of tiles of one row per item ----

@@ -19,6 +19,12 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
                  : "memory");
 }
 
+// Ends an mbarrier's life, so that its memory may be reused (or initialised again).
+__device__ __forceinline__ void mbar_inval(uint64_t *bar)
+{
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_addr(bar)) : "memory");
+}
+
 // Makes initialised mbarriers visible to the async (bulk-copy) proxy.
 __device__ __forceinline__ void fence_mbar_init()
 {

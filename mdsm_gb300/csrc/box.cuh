@@ -5,17 +5,18 @@
 // consecutive tiles of one row is searched by a group of THREADS threads: the whole CTA
 // (BoxBarCta) or one of several groups of a CTA, each with its own named barrier and shared
 // memory (BoxBarGroup), so that one wide CTA runs several searches whose barriers overlap.
-// The next tile's samples are copied into shared memory (cp.async) while the current one is
-// searched.  Arithmetic per sample and width is FP32, explicitly rounded, in the oracle's
+// The next tile's samples are copied into shared memory (one bulk copy on an mbarrier, or
+// per-thread cp.async) while the current one is searched.  Arithmetic per sample and width is
+// FP32, explicitly rounded, in the oracle's
 // order: B_2w[i] = B_w[i] + B_w[i + w] (a pairwise tree over each boxcar), and the SNR
 // (B_w - w mu) / (sigma sqrt w) with 1 / (sigma sqrt w) rounded once per width.
 //
 // Two paths (box_run): a fast path that only decides whether a tile reaches the threshold,
 // over chains of one residue class of each step's stride per thread, keeping the largest sum
 // of each width; and an exact path (box_tile_exact) for the tiles it flags: every position's
-// best SNR over the widths, then the candidates, local maxima of the best
-// SNR over max(w/2, 1) samples on each side, with the width that gave the best formed again
-// for those few positions (box_best_at).
+// best SNR over the widths, then the candidates, local maxima of the best SNR over
+// max(w/2, 1) samples on each side, with the width that gave the best formed again for those
+// few positions (box_best_at).
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -196,8 +197,7 @@ __device__ __forceinline__ float box_value(uint32_t raw)
 template <typename T, int NW, int THREADS, int K, class Bar>
 __device__ __noinline__ void box_tile_exact(const T *__restrict__ r, long long n, long long t0,
                                             int cnt, float mu_f, float thr, const float *inv_w,
-                                            int d,
-                                            DevCand *__restrict__ cands,
+                                            int d, DevCand *__restrict__ cands,
                                             unsigned long long *__restrict__ count, long long cap,
                                             float *B0, float *B1, float *best_s, const Bar &bar,
                                             int tid, bool active)

@@ -485,7 +485,7 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
     uint32_t parity = 0;  // of the next bulk-copied tile's phase
     bool late = false;    // a bulk-copy wait of this thread ran out
     if (kBulk) bar.sync();  // the mbarrier initialised (before any thread waits on it)
-    stage(tile_lo);
+    if (tile_lo < tile_hi) stage(tile_lo);  // (no copy is left in flight for an empty run)
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
         const long long t0 = tile * G::TILE;
         if (bulk(tile)) {

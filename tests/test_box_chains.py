@@ -116,3 +116,30 @@ def test_standalone_search_fits_four_ctas_per_sm(nw):
     threads, k, ke = _shapes()[0]
     g = geom(nw, threads, k, ke)
     assert 4 * (g["smem"] + SMEM_PER_CTA_RESERVED) <= SMEM_PER_SM
+
+
+@pytest.mark.parametrize("nw", range(1, 10))
+@pytest.mark.parametrize("shape", _shapes(), ids=["k_boxcar", "fused"])
+def test_exact_path_reads_stay_in_its_buffers(shape, nw):
+    """box_tile_exact: position pairs i = 2 tid + 2 THREADS q (q < PAIRS) of its own region;
+    step s (u = 4^(s-1)) reads the float2 partners at i + u and, when it forms two widths, at
+    i + 2u and i + 3u (i + 2 .. i + 4 for u = 1); the candidate pass reads best[q + HL +- h]
+    for h <= max(w/2, 1) <= HL and q < ETILE."""
+    threads, k, ke = shape
+    g = geom(nw, threads, k, ke)
+    pairs = (threads * ke + 2 * threads - 1) // (2 * threads)
+    imax = 2 * (threads - 1) + 2 * threads * (pairs - 1)
+    top = imax + 1  # the pair's own values
+    s = 1
+    while 2 * s - 1 < nw:
+        u = 1 << (2 * s - 2)
+        two = 2 * s < nw
+        if u == 1:
+            top = max(top, imax + (4 if two else 3))
+        else:
+            top = max(top, imax + (3 * u if two else u) + 1)
+        s += 1
+    assert top < g["buf"]
+    assert pairs * 2 * threads >= g["nbest"]  # every position with a best SNR is formed
+    h = max(g["wmax"] // 2, 1)
+    assert h <= g["hl"] and (g["etile"] - 1) + g["hl"] + h < g["nbest"]

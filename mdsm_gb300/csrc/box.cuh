@@ -409,9 +409,11 @@ __device__ __forceinline__ void box_chain_step(const uint32_t *NB, float *A, flo
 //
 // Staging (kBulk): a tile whose region lies inside the series and starts 16-byte aligned
 // arrives by one bulk copy (cp.async.bulk, issued by the group's thread 0 on an mbarrier in
-// sm), and every thread waits on the mbarrier's phase, bounded, instead of at a group barrier;
-// a wait that runs out sets kBoxCountLate in *count and the search goes on (its results are
-// then void).  Other tiles, and every tile without kBulk, arrive by per-thread cp.async.
+// sm), and every thread waits on the mbarrier's phase, bounded, instead of at a group barrier.
+// A wait that runs out sets kBoxCountLate in *count (the search's results are then void); the
+// group learns of it at the tile's closing vote and leaves the run together, after a bounded
+// wait for a copy still in flight.  Other tiles, and every tile without kBulk, arrive by
+// per-thread cp.async.
 //
 // Fast path (every tile): only whether a boxcar that starts in the tile reaches the threshold
 // at some width is needed, so no position keeps a best SNR.  Step s (chain stride u = 8^(s-1))
@@ -470,20 +472,22 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
         const long long r0 = tile * G::TILE;
         return kBulk && r0 + N <= n && ((uintptr_t)(r + r0) & 15) == 0;
     };
+    uint32_t nwait = 0;  // bulk-copy phases waited for (the next copy's phase parity: nwait & 1)
+    int tail = -1;       // thread 0: the parity of a copy it issued and has not seen complete
+    bool late = false;   // a bulk-copy wait of this thread ran out
     auto stage = [&](long long tile) {
         if (!active) return;
         if (bulk(tile)) {
-            if (tid == 0) {
+            if (tid == 0 && !late) {  // (never an arrival on a phase that may be incomplete)
                 fence_proxy_async_smem();  // (after the group's reads of NB, at a barrier)
                 mbar_arrive_expect_tx(mbar, (uint32_t)N * 4u);
                 bulk_g2s(NB, r + tile * G::TILE, (uint32_t)N * 4u, mbar);
+                tail = (int)(nwait & 1u);
             }
         } else {
             box_stage<T, NW, THREADS, K>(NB, r, n, tile, tid);
         }
     };
-    uint32_t parity = 0;  // of the next bulk-copied tile's phase
-    bool late = false;    // a bulk-copy wait of this thread ran out
     if (kBulk) bar.sync();  // the mbarrier initialised (before any thread waits on it)
     if (tile_lo < tile_hi) stage(tile_lo);  // (no copy is left in flight for an empty run)
     for (long long tile = tile_lo; tile < tile_hi; ++tile) {
@@ -492,11 +496,15 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
             // the bulk copy's bytes are visible to each thread that sees the phase complete;
             // inv_w is visible since the barrier before the loop; every thread is past the
             // previous tile's reads of the sum buffers (its last barrier)
-            if (active && !mbar_wait_bounded(mbar, parity, nullptr, 0)) {
-                late = true;
-                atomicOr(count, kBoxCountLate);
+            if (active) {
+                if (mbar_wait_bounded(mbar, nwait & 1u, nullptr, 0)) {
+                    if (tid == 0) tail = -1;
+                } else {
+                    late = true;
+                    atomicOr(count, kBoxCountLate);
+                }
             }
-            parity ^= 1u;
+            ++nwait;
         } else {
             if (active) cp_async_wait_all();
             bar.sync();  // the tile's samples (every thread's copies), inv_w and the pads visible
@@ -532,7 +540,8 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
 #pragma unroll
             for (int l = 0; l < NW; ++l) hit |= snr(M[l], l) >= thr;
         }
-        const bool flagged = bar.any(hit);
+        const bool flagged = bar.any(hit || late);
+        if (kBulk && flagged && bar.any(late)) break;  // a wait ran out: the group stops together
         if (!staged) stage_next();
         if (flagged) {
             // (every thread is past the fast path's reads of the sum buffers)
@@ -548,8 +557,8 @@ __device__ __forceinline__ void box_run(const T *__restrict__ r, long long n, lo
     }
     if (active) cp_async_wait_all();
     if (kBulk && active && tid == 0) {
-        // a copy whose wait ran out may still be in flight: one more bounded wait for the last
-        if (late) mbar_wait_bounded(mbar, parity ^ 1u, nullptr, 0);
+        // a copy still in flight (the group stopped after a wait ran out): one more bounded wait
+        if (tail >= 0) mbar_wait_bounded(mbar, (uint32_t)tail, nullptr, 0);
         mbar_inval(mbar);  // (every thread's waits are behind the last group barrier)
     }
 }
